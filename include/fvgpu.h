@@ -1,0 +1,172 @@
+/*
+ * fvgpu.h -- C ABI of libfvgpu: the residual evaluation and Runge-Kutta stage
+ * update of the octree finite-volume solver FV_140823, on one GB300 (sm_103a).
+ *
+ * The reference path is, per RK stage (the stage sequence of the missing
+ * driver advancetimeexplicit, loop.c:48):
+ *     faceinterp(run)                 faceinterp.c:21-61   (MUSCL, ischeme 2)
+ *     gradcalc(run)                   gradcalc.c:9-47      (viscous, ns 1)
+ *     RHS(run) / RHS_nb(run, inner)   RHS.c:3-13, RHS_nb.c:3-15
+ *        -> residual_faces_AMR        residual_faces_AMR.c:10-202
+ *     RK(irk, run)                    RK.c:3-56
+ * all of them `void` functions over the host leaf list `run->topo->locl`.
+ * Here the host flattens its leaves once per adaptation (fvgpu_mesh_soa),
+ * uploads them with fvgpu_upload_mesh, and the state stays resident in HBM;
+ * each reference call has a counterpart below that works on the resident
+ * state.  Reference semantics kept exactly: operation order per cell and
+ * face (the FP64 path is bit-identical to the reference up to its use of
+ * libm pow(x, 2.0), for which the correctly rounded x*x is used), the stage
+ * formulas of RK.c, boundary codes of bc.c, EOS models 1-3.
+ *
+ * Conventions
+ *   - every call returns FVGPU_OK (0) or a negative FVGPU_ERR_* code; the
+ *     reference instead printf()s and calls exit(0) (residual_faces_AMR.c:
+ *     186-194, hllc_euler.c:52-55, compute_wave_speeds.c:84-87);
+ *   - kernels never trap: a non-finite residual or a failed EOS sets a device
+ *     error word (first cell + code), which the next synchronising call turns
+ *     into FVGPU_ERR_NONFINITE / FVGPU_ERR_EOS; fvgpu_last_error() reports it;
+ *   - host buffers are caller-owned; device buffers belong to the context;
+ *   - state arrays are structure-of-arrays, U[v * ld + c] for variable v of
+ *     cell c (ld >= ncells);
+ *   - one context per host thread; each context owns one CUDA stream.
+ */
+#ifndef FVGPU_H
+#define FVGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FVGPU_OK 0
+#define FVGPU_ERR_ARG (-1)          /* invalid argument */
+#define FVGPU_ERR_CUDA (-2)         /* CUDA runtime error (message in fvgpu_last_error) */
+#define FVGPU_ERR_NOMEM (-3)        /* device allocation failed */
+#define FVGPU_ERR_STATE (-4)        /* call order (e.g. no mesh uploaded) */
+#define FVGPU_ERR_NONFINITE (-5)    /* a residual / state became NaN or Inf */
+#define FVGPU_ERR_EOS (-6)          /* mixture EOS has no real pressure root */
+#define FVGPU_ERR_UNSUPPORTED (-7)  /* configuration the library does not implement */
+#define FVGPU_ERR_MESH (-8)         /* mesh tables failed validation at upload */
+#define FVGPU_ERR_NODEVICE (-9)     /* no CUDA device */
+#define FVGPU_ERR_TIMEOUT (-10)     /* a bounded device wait gave up */
+
+/* arithmetic of the residual */
+#define FVGPU_FP64 0   /* everything in FP64, reference operation order */
+#define FVGPU_MIXED 1  /* reconstruction, EOS and fluxes in FP32; residual
+                          accumulation, RK update, sums and dt in FP64 */
+
+/* RK schemes = stage lists of RK(irk) (RK.c:16-47) */
+#define FVGPU_SCHEME_EULER 1   /* RK(0), RK(1) */
+#define FVGPU_SCHEME_SSPRK2 2  /* RK(0), RK(1), RK(4) */
+#define FVGPU_SCHEME_SSPRK3 3  /* RK(0), RK(1), RK(2), RK(3) */
+
+/* what fvgpu_download() copies */
+#define FVGPU_FIELD_S 0    /* state S            [neq][ncells] */
+#define FVGPU_FIELD_SN 1   /* step-start state SN [neq][ncells] */
+#define FVGPU_FIELD_RHS 2  /* residual RHS       [neq][ncells] */
+#define FVGPU_FIELD_SF 3   /* MUSCL face values SF [6][neq][ncells] */
+#define FVGPU_FIELD_SG 4   /* gradients SG       [neq+1][3][ncells] */
+
+/* Neighbour code per (face, cell), as in the mesh builder (fvmesh.h):
+ * >= 0 neighbour cell; -1-bc for a boundary face (bc 1..4, bc.c:19-49);
+ * <= FVGPU_HANG0: 1:4 hanging face, record FVGPU_HANG0 - code. */
+#define FVGPU_HANG0 (-16)
+
+/* Solver constants read by the residual path (CON / PAR, strdata.h:199-358;
+ * positional .ct input, inputset.c:39-110). */
+typedef struct fvgpu_config {
+  int model;       /* 1 ideal/stiffened gas, 2 barotropic liquid, 3 two-phase mixture */
+  int ns;          /* 1 = viscous (Navier-Stokes) fluxes */
+  int ischeme;     /* 1 first order, 2 MUSCL / minmod */
+  int iprimtv;     /* must be 0: see DESIGN notes on cons2primtv */
+  int eos;         /* 1 = viscous work term in the energy flux (flux_viscous.c:227) */
+  int precision;   /* FVGPU_FP64 or FVGPU_MIXED */
+  int device;      /* CUDA device ordinal */
+  int reserved0;
+  double gamma;    /* PAR.matergama[0] */
+  double pinf;     /* PAR.materpinf[0] */
+  double visc;     /* PAR.matervisc[0] */
+  double ymin;     /* CON.ymin (mass-fraction clip of facercnstr.c:43-44) */
+  double inflow[8];/* conservative ghost state of bc code 1 (bc_inlet.c) */
+  double reserved[4];
+} fvgpu_config;
+
+/* Flattened mesh, structure of arrays ([face][cell] = f * ncells + c). */
+typedef struct fvgpu_mesh_soa {
+  int64_t ncells;
+  int64_t nhang;
+  const int32_t *nbr;       /* [6][ncells] neighbour code */
+  const int32_t *nbr_face;  /* [6][ncells] neighbour's face index (neigfc), -1 at boundaries */
+  const double *area;       /* [6][ncells] Area[f][0] of single-neighbour / boundary faces */
+  const double *dcf;        /* [6][ncells] distance.c dist_cf of face f */
+  const double *dcc;        /* [6][ncells] distance.c dist_cc of face f */
+  const double *vol;        /* [ncells] */
+  const int32_t *hang_nbr;  /* [nhang][4] fine neighbours of a 1:4 face, sub-face order */
+  const double *hang_area;  /* [nhang][4] Area[f][0..3] of a 1:4 face */
+  const double *frames;     /* [6][9] face frame per face index: n, t1, t2 */
+  const int32_t *level;     /* [ncells] octree level (used by the mixed path) */
+} fvgpu_mesh_soa;
+
+typedef struct fvgpu_ctx fvgpu_ctx;
+
+/* ---- lifetime --------------------------------------------------------- */
+int fvgpu_create(const fvgpu_config *cfg, fvgpu_ctx **out);
+int fvgpu_destroy(fvgpu_ctx *ctx);
+/* Switch FP64 <-> mixed arithmetic; keeps mesh and state. */
+int fvgpu_set_precision(fvgpu_ctx *ctx, int precision);
+
+/* ---- data in / out ---------------------------------------------------- */
+/* Validates and uploads the tables (once per adaptation); resets the state. */
+int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *mesh);
+/* S <- U (host, [neq][ld]); LEAF.S of every leaf (strdata.h:80). */
+int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld);
+int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld);
+/* Copy a device field (FVGPU_FIELD_*) to host memory (densely packed). */
+int fvgpu_download(fvgpu_ctx *ctx, int field, double *out);
+
+/* ---- the reference's calls -------------------------------------------- */
+/* faceinterp(run), faceinterp.c:21-61: SF from S. */
+int fvgpu_faceinterp(fvgpu_ctx *ctx);
+/* gradcalc(run), gradcalc.c:9-47: SG from S. */
+int fvgpu_gradcalc(fvgpu_ctx *ctx);
+/* RHS(run), RHS.c:3-13: RHS from S, SF, SG (as the reference, faceinterp /
+ * gradcalc must have been called first when ischeme == 2 / ns == 1). */
+int fvgpu_rhs(fvgpu_ctx *ctx);
+/* RHS_nb(run, inner_outer), RHS_nb.c:3-15: RHS of the cells whose inner flag
+ * equals inner_outer (flags from fvgpu_set_inner; inner_el.c:3-30). */
+int fvgpu_set_inner(fvgpu_ctx *ctx, const int32_t *inner);
+int fvgpu_rhs_nb(fvgpu_ctx *ctx, int inner_outer);
+/* RK(irk, run), RK.c:3-56, with CON.dt = dt. */
+int fvgpu_rk(fvgpu_ctx *ctx, int irk, double dt);
+
+/* ---- fused time stepping ---------------------------------------------- */
+/* nsteps full RK steps (scheme FVGPU_SCHEME_*).  dt > 0: fixed step (the
+ * reference's CON.dt).  dt <= 0: each step uses the CFL step
+ *     dt = cfl / max_c (sum_faces A (|u.n| + c)) / (2 V)
+ * reduced on the device from the step-start state.  Each step is one CUDA
+ * graph launch. */
+int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps);
+/* dt = cfl / lambda_max of the current state (no state change). */
+int fvgpu_compute_dt(fvgpu_ctx *ctx, double cfl, double *dt);
+/* sums[v] = sum_c S[v][c] * V[c] (v < neq), sums[neq] = sum_c V[c]
+ * (conservationcalc.c:19-34), FP64, fixed reduction order. */
+int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
+
+/* ---- adjoint ----------------------------------------------------------- */
+/* dJdU = (dR/dU)^T w for the residual R(U) of the current state (FP64),
+ * w and dJdU host arrays [neq][ld]. */
+int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld);
+
+/* ---- diagnostics -------------------------------------------------------- */
+/* Error of the last failing call: code, offending cell (-1 if none) and text. */
+int fvgpu_last_error(fvgpu_ctx *ctx, int *code, int64_t *cell, char *msg, int msglen);
+/* Number of conserved variables of the configured model (5 or 4). */
+int fvgpu_neq(const fvgpu_ctx *ctx);
+/* Block until all work queued on the context's stream has finished. */
+int fvgpu_synchronize(fvgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,106 @@
+/*
+ * fvmesh.h -- host-side octree mesh builder and flattener (C ABI).
+ *
+ * The reference keeps its forest of octrees on the host (split.c, merge.c,
+ * elconn.c, rebuildconn.c) and walks the leaf list `run->topo->locl` on every
+ * residual evaluation.  This library is the synthetic stand-in for that host:
+ * it builds an axis-aligned, 2:1 face-balanced octree over a box, orders the
+ * leaves along a Morton curve and flattens leaves and faces -- including the
+ * 1:4 hanging faces -- into the structure-of-arrays tables that
+ * libfvgpu uploads once per adaptation (fvgpu.h, fvgpu_mesh_soa).
+ *
+ * Conventions taken from the reference's hexahedron tables (operatetp.c):
+ *   local node n has bit0 = +x, bit1 = +y, bit2 = +z
+ *   face f: 0 = -y, 1 = +x, 2 = +y, 3 = -x, 4 = -z, 5 = +z
+ *   opposite face (fcopp, operatetp.c:481-490): 0<->2, 1<->3, 4<->5
+ * MUSCL stencil distances follow distance.c:3-148 term by term.
+ *
+ * Every function returns 0 on success and a negative FVMESH_ERR_* code on
+ * failure; fvmesh_last_error() returns a message for the calling thread.
+ */
+#ifndef FVMESH_H
+#define FVMESH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FVMESH_ERR_ARG      (-1)   /* bad argument */
+#define FVMESH_ERR_BALANCE  (-2)   /* 2:1 face balance violated */
+#define FVMESH_ERR_LEVEL    (-3)   /* level outside [1, FVMESH_MAX_LEVEL] */
+#define FVMESH_ERR_NOMEM    (-4)
+
+#define FVMESH_MAX_LEVEL 18
+
+/* Boundary codes carried in fvmesh face tables (bc.c:19-49). */
+#define FVMESH_BC_NONE        0
+#define FVMESH_BC_INFLOW      1
+#define FVMESH_BC_TRANSMISSIVE 2
+#define FVMESH_BC_REFLECTIVE  3
+#define FVMESH_BC_NOSLIP      4
+
+/* Neighbour code stored per (face, cell):
+ *   code >= 0            : the single neighbour cell (same level or one coarser)
+ *   -8 <= code <= -1     : boundary face with bc = -1 - code
+ *   code <= FVMESH_HANG0 : 1:4 hanging face, record index = FVMESH_HANG0 - code */
+#define FVMESH_HANG0 (-16)
+
+typedef struct fvmesh fvmesh;
+
+/* Flattened tables. The caller allocates every array with the sizes given by
+ * fvmesh_sizes() and passes the pointers; fvmesh_flatten() fills them.
+ * Layout is structure-of-arrays: [face][cell] means index f*ncells + c. */
+typedef struct fvmesh_tables {
+  int32_t *level;      /* [ncells] octree level (root = 0) */
+  int32_t *ijk;        /* [3][ncells] integer position at the cell's level */
+  int32_t *nbr;        /* [6][ncells] neighbour code, see above */
+  int32_t *nbr_face;   /* [6][ncells] neighbour's face index (neigfc), -1 at boundaries */
+  double  *area;       /* [6][ncells] face area (single-neighbour and boundary faces) */
+  double  *dcf;        /* [6][ncells] centroid-to-face distance, distance.c */
+  double  *dcc;        /* [6][ncells] centroid-to-centroid distance, distance.c */
+  double  *vol;        /* [ncells] */
+  double  *centroid;   /* [3][ncells] */
+  int32_t *hang_nbr;   /* [nhang][4] fine neighbours of a 1:4 face, sub-face order */
+  double  *hang_area;  /* [nhang][4] sub-face areas */
+  int32_t *hang_cell;  /* [nhang] owning (coarse) cell */
+  int32_t *hang_face;  /* [nhang] owning face index */
+  double  *frames;     /* [6][9] per face index: n(3), t1(3), t2(3) */
+} fvmesh_tables;
+
+/* Box [lo, lo+len] refined uniformly to base_level.  periodic[a] != 0 wraps
+ * axis a; side_bc[f] is the boundary code of the domain side facing the same
+ * way as face f (ignored on periodic axes). */
+int fvmesh_create_uniform(const double lo[3], const double len[3], int base_level,
+                          const int periodic[3], const int side_bc[6], fvmesh **out);
+void fvmesh_destroy(fvmesh *m);
+
+/* Number of leaves and of 1:4 hanging-face records. */
+int fvmesh_sizes(const fvmesh *m, int64_t *ncells, int64_t *nhang);
+
+/* Leaf levels and centroids (centroids as distance.c forms them: node average). */
+int fvmesh_leaves(const fvmesh *m, int32_t *level, double *centroid /*[3][n]*/);
+
+/* Refine every leaf whose flag is nonzero (up to max_level), then refine more
+ * leaves until every face sees at most one level of difference.  Leaves are
+ * re-sorted along the Morton curve. */
+int fvmesh_refine(fvmesh *m, const uint8_t *flags, int max_level);
+
+/* Fill the flattened tables (caller-allocated, sizes from fvmesh_sizes). */
+int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t);
+
+/* Node coordinates as the reference stores them in CELL.nd (8 nodes, local
+ * numbering above) for the cell at (level, i, j, k); i, j, k may lie outside
+ * the box (periodic images).  Used by the reference harness. */
+int fvmesh_cell_nodes(const fvmesh *m, int level, int i, int j, int k, double xyz[8][3]);
+
+/* Domain description. */
+int fvmesh_domain(const fvmesh *m, double lo[3], double len[3], int periodic[3], int side_bc[6]);
+
+const char *fvmesh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

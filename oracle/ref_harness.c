@@ -1,0 +1,372 @@
+/*
+ * ref_harness.c -- runs the reference's own residual / RK code on a mesh
+ * given as flattened tables.  TEST INFRASTRUCTURE ONLY: it is linked with the
+ * reference's hot-path sources, compiled unchanged (oracle/build.py), into
+ * oracle/_ref/libfvref.so, and is loaded only by tests/ and by the fixture
+ * generator under tests/golden/.
+ *
+ * The reference cannot run as shipped (its time-step driver
+ * advancetimeexplicit, loop.c:48, is missing, and so are brchconn,
+ * cellallocation, bc_reflective and bc_wall).  This harness supplies:
+ *   - a serial MPI_Wtime / MPI_Allreduce / MPI_Barrier;
+ *   - bc_reflective / bc_wall as no-ops (the reference declares them,
+ *     bc.c:38,42, but defines neither);
+ *   - the BRANCH / CELL / LEAF objects the residual walks, built directly from
+ *     the tables (bypassing brchconn / cellallocation): leaf list
+ *     `run->topo->locl`, `neigtr/lfc_neigs/neigfc/nsfc`, parent branches for
+ *     distance.c, a level-0 `glob` branch for boundary faces, and periodic
+ *     image branches that share the real leaf's state but carry translated
+ *     node coordinates (the reference has no periodic boundary; this mirrors
+ *     its proxy "keen" branches, forestconn.c:36-57);
+ *   - the stage sequence of the missing driver: RK(0), then per stage
+ *     faceinterp (MUSCL) -> gradcalc (viscous) -> RHS -> RK(k).
+ * Leaf storage (LEAF.S, SN, RHS, SF, SG) is allocated by the reference's own
+ * memallocation.c / leafallocation.c, scratch by createutility.c.
+ * Node coordinates use the mesh builder's rule x = lo + I * (len / 2^level).
+ */
+#include "strdata.h"
+
+#include <stdint.h>
+#include <time.h>
+
+/* ---- serial MPI stand-ins --------------------------------------------- */
+double MPI_Wtime(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype dt, MPI_Op op, MPI_Comm c) {
+  size_t w = dt == MPI_DOUBLE ? sizeof(double) : (dt == MPI_LONG ? sizeof(long) : sizeof(int));
+  (void)op;
+  (void)c;
+  memmove(r, s, (size_t)n * w);
+  return 0;
+}
+int MPI_Barrier(MPI_Comm c) {
+  (void)c;
+  return 0;
+}
+
+/* ---- reference symbols that are declared but never defined -------------- */
+void bc_reflective(struct BRANCH *crnt, int f, RUN *run) {
+  (void)crnt;
+  (void)f;
+  (void)run;
+}
+void bc_wall(struct BRANCH *crnt, int f, struct RUN *run) {
+  (void)crnt;
+  (void)f;
+  (void)run;
+}
+
+/* ---- harness ------------------------------------------------------------- */
+typedef struct refh_config {
+  int model, ns, ischeme, iprimtv, neq, eos, i_case, pad;
+  double gamma, pinf, visc, ymin, dt;
+} refh_config;
+
+typedef struct refh {
+  RUN *run;
+  int64_t n;
+  BRANCH **cells;
+  BRANCH *glob;
+  BRANCH **extra; /* parents and images, kept for teardown */
+  int64_t nextra, capextra;
+  double lo[3], len[3];
+  int periodic[3];
+} refh;
+
+static const int kAxis[6] = {1, 0, 1, 0, 2, 2};
+static const int kSign[6] = {-1, +1, +1, -1, -1, +1};
+
+static double coordv(const refh *h, int level, int a, int64_t I) {
+  return h->lo[a] + (double)I * ldexp(h->len[a], -level);
+}
+
+static CELL *make_cell_nodes(const refh *h, int level, const int64_t p[3]) {
+  CELL *cl = calloc(1, sizeof(CELL));
+  cl->nd = calloc(8, sizeof(ND));
+  for (int n = 0; n < 8; ++n) {
+    cl->nd[n].num = n;
+    cl->nd[n].x = coordv(h, level, 0, p[0] + (n & 1));
+    cl->nd[n].y = coordv(h, level, 1, p[1] + ((n >> 1) & 1));
+    cl->nd[n].z = coordv(h, level, 2, p[2] + ((n >> 2) & 1));
+  }
+  return cl;
+}
+
+static void keep(refh *h, BRANCH *b) {
+  if (h->nextra == h->capextra) {
+    h->capextra = h->capextra ? 2 * h->capextra : 1024;
+    h->extra = realloc(h->extra, (size_t)h->capextra * sizeof(BRANCH *));
+  }
+  h->extra[h->nextra++] = b;
+}
+
+static int64_t fdiv2(int64_t a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); }
+
+/* Parent branch: distance.c only reads its node coordinates and node count
+ * (distance.c:163-171, 182-190). */
+static BRANCH *make_parent(refh *h, int level, const int64_t p[3]) {
+  BRANCH *b = calloc(1, sizeof(BRANCH));
+  int64_t q[3] = {fdiv2(p[0]), fdiv2(p[1]), fdiv2(p[2])};
+  b->level = level - 1;
+  b->nlnd = 8;
+  b->nlfc = 6;
+  b->cl = make_cell_nodes(h, level - 1, q);
+  keep(h, b);
+  return b;
+}
+
+/* Periodic image of a real branch at the unwrapped position p: same leaf
+ * (state), translated nodes and parent. */
+static BRANCH *make_image(refh *h, BRANCH *real, const int64_t p[3]) {
+  BRANCH *b = calloc(1, sizeof(BRANCH));
+  *b = *real;
+  b->cl = make_cell_nodes(h, real->level, p);
+  b->prnt = make_parent(h, real->level, p);
+  keep(h, b);
+  return b;
+}
+
+/* Branch to use for neighbour `idx` when the unwrapped position at its level
+ * is `up`: the real branch, or an image if the link wraps around. */
+static BRANCH *neighbour_branch(refh *h, int64_t idx, const int32_t *ijk, const int64_t up[3]) {
+  BRANCH *real = h->cells[idx];
+  int64_t n = h->n;
+  if (ijk[idx] == up[0] && ijk[n + idx] == up[1] && ijk[2 * n + idx] == up[2]) return real;
+  return make_image(h, real, up);
+}
+
+refh *refh_create(const refh_config *cfg, int64_t n, const int32_t *level, const int32_t *ijk,
+                  const int32_t *nbr, const int32_t *nbr_face, const double *area,
+                  const double *vol, const double *centroid, const int32_t *hang_nbr,
+                  const double *hang_area, const double *frames, const double lo[3],
+                  const double len[3], const int periodic[3]) {
+  refh *h = calloc(1, sizeof(refh));
+  for (int a = 0; a < 3; ++a) {
+    h->lo[a] = lo[a];
+    h->len[a] = len[a];
+    h->periodic[a] = periodic[a];
+  }
+  h->n = n;
+  RUN *run = calloc(1, sizeof(RUN));
+  h->run = run;
+  run->con = calloc(1, sizeof(CON));
+  run->par = calloc(1, sizeof(PAR));
+  run->sol = calloc(1, sizeof(SOL));
+  run->sol1 = calloc(1, sizeof(SOL));
+  run->topo = calloc(1, sizeof(FOREST));
+  CON *con = run->con;
+  con->model = cfg->model;
+  con->ns = cfg->ns;
+  con->ischeme = cfg->ischeme;
+  con->iprimtv = cfg->iprimtv;
+  con->neq = cfg->neq;
+  con->nprimitiv = cfg->neq; /* inputset.c:130-222 for models 1 and 3 */
+  con->neq_temp = cfg->neq;
+  con->turb = 0;
+  con->eos = cfg->eos;
+  con->i_case = cfg->i_case;
+  con->ymin = cfg->ymin;
+  con->dt = cfg->dt;
+  con->verbose = 0;
+  con->rank = 0;
+  run->par->matergama[0] = cfg->gamma;
+  run->par->materpinf[0] = cfg->pinf;
+  run->par->matervisc[0] = cfg->visc;
+
+  h->glob = calloc(1, sizeof(BRANCH));
+  h->glob->level = 0;
+  run->topo->glob = h->glob;
+
+  h->cells = calloc((size_t)n, sizeof(BRANCH *));
+  for (int64_t c = 0; c < n; ++c) {
+    BRANCH *b = calloc(1, sizeof(BRANCH));
+    h->cells[c] = b;
+    int64_t p[3] = {ijk[c], ijk[n + c], ijk[2 * n + c]};
+    b->type = 0;
+    b->nlfc = 6;
+    b->nlnd = 8;
+    b->level = level[c];
+    b->root = (int)c;
+    b->part = 0;
+    b->cl = make_cell_nodes(h, level[c], p);
+    b->prnt = make_parent(h, level[c], p);
+    CELL *cl = b->cl;
+    cl->nx = calloc(6, sizeof(double));
+    cl->ny = calloc(6, sizeof(double));
+    cl->nz = calloc(6, sizeof(double));
+    cl->nxt1 = calloc(6, sizeof(double));
+    cl->nyt1 = calloc(6, sizeof(double));
+    cl->nzt1 = calloc(6, sizeof(double));
+    cl->nxt2 = calloc(6, sizeof(double));
+    cl->nyt2 = calloc(6, sizeof(double));
+    cl->nzt2 = calloc(6, sizeof(double));
+    cl->Area = calloc(6, sizeof(double *));
+    cl->fc = calloc(6, sizeof(FC));
+    cl->Vol = vol[c];
+    cl->xc = centroid[c];
+    cl->yc = centroid[n + c];
+    cl->zc = centroid[2 * n + c];
+    b->neigtr = calloc(6, sizeof(BRANCH **));
+    b->lfc_neigs = calloc(6, sizeof(int));
+    b->neigfc = calloc(6, sizeof(int));
+    b->nsfc = calloc(6, sizeof(int));
+    for (int f = 0; f < 6; ++f) {
+      cl->Area[f] = calloc(4, sizeof(double));
+      b->neigtr[f] = calloc(4, sizeof(BRANCH *));
+      const double *fr = frames + 9 * f;
+      cl->nx[f] = fr[0];
+      cl->ny[f] = fr[1];
+      cl->nz[f] = fr[2];
+      cl->nxt1[f] = fr[3];
+      cl->nyt1[f] = fr[4];
+      cl->nzt1[f] = fr[5];
+      cl->nxt2[f] = fr[6];
+      cl->nyt2[f] = fr[7];
+      cl->nzt2[f] = fr[8];
+    }
+    if (c > 0) {
+      h->cells[c - 1]->lnxt = b;
+      b->lprv = h->cells[c - 1];
+    }
+  }
+  run->topo->locl = n > 0 ? h->cells[0] : NULL;
+
+  /* connectivity */
+  for (int64_t c = 0; c < n; ++c) {
+    BRANCH *b = h->cells[c];
+    const int l = level[c];
+    for (int f = 0; f < 6; ++f) {
+      const int32_t code = nbr[(int64_t)f * n + c];
+      const int a = kAxis[f];
+      int64_t u[3] = {ijk[c], ijk[n + c], ijk[2 * n + c]};
+      u[a] += kSign[f];
+      if (code < 0 && code >= -8) { /* boundary */
+        b->cl->fc[f].bc = -1 - code;
+        b->lfc_neigs[f] = 1;
+        b->nsfc[f] = 1;
+        b->neigfc[f] = -1;
+        b->neigtr[f][0] = h->glob;
+        b->cl->Area[f][0] = area[(int64_t)f * n + c];
+        continue;
+      }
+      b->cl->fc[f].bc = 0;
+      b->neigfc[f] = nbr_face[(int64_t)f * n + c];
+      if (code >= 0) {
+        b->lfc_neigs[f] = 1;
+        b->nsfc[f] = 1;
+        b->cl->Area[f][0] = area[(int64_t)f * n + c];
+        int64_t up[3] = {u[0], u[1], u[2]};
+        if (level[code] == l - 1)
+          for (int q = 0; q < 3; ++q) up[q] = fdiv2(up[q]);
+        b->neigtr[f][0] = neighbour_branch(h, code, ijk, up);
+      } else { /* 1:4 hanging face */
+        const int64_t r = -16 - (int64_t)code;
+        b->lfc_neigs[f] = 4;
+        b->nsfc[f] = 4;
+        for (int s = 0; s < 4; ++s) {
+          const int64_t k = hang_nbr[4 * r + s];
+          b->cl->Area[f][s] = hang_area[4 * r + s];
+          /* fine neighbour's unwrapped position = actual + 2 * wrap shift */
+          const int64_t nl = (int64_t)1 << l;
+          int64_t w = u[a];
+          if (w < 0 || w >= nl) w = (w + nl) % nl;
+          const int64_t shift = 2 * (u[a] - w);
+          int64_t up[3] = {ijk[k], ijk[n + k], ijk[2 * n + k]};
+          up[a] += shift;
+          b->neigtr[f][s] = neighbour_branch(h, k, ijk, up);
+        }
+      }
+    }
+  }
+
+  memallocation(run); /* sol/sol1 + every leaf (leafallocation.c) */
+  createutility(run); /* RUN scratch (createutility.c) */
+  /* images share the real leaf storage */
+  for (int64_t e = 0; e < h->nextra; ++e) {
+    BRANCH *b = h->extra[e];
+    if (b->root >= 0 && b->nlfc == 6 && b->neigtr != NULL) b->el = h->cells[b->root]->el;
+  }
+  return h;
+}
+
+void refh_destroy(refh *h) {
+  /* The reference has no matching free routines for most of these objects
+   * (leafdeallocation.c frees only part of SG); the harness lives for one
+   * test and releases the branch shells only. */
+  if (!h) return;
+  for (int64_t e = 0; e < h->nextra; ++e) free(h->extra[e]);
+  free(h->extra);
+  free(h->cells);
+  free(h);
+}
+
+void refh_set_dt(refh *h, double dt) { h->run->con->dt = dt; }
+
+void refh_set_state(refh *h, const double *U) {
+  const int neq = h->run->con->neq;
+  for (int64_t c = 0; c < h->n; ++c)
+    for (int v = 0; v < neq; ++v) h->cells[c]->el->S[v] = U[(int64_t)v * h->n + c];
+}
+
+/* which: 0 = S, 1 = SN, 2 = RHS, 3 = SF [6][neq][n], 4 = SG [neq+1][3][n] */
+void refh_get(const refh *h, int which, double *out) {
+  const int neq = h->run->con->neq;
+  const int64_t n = h->n;
+  for (int64_t c = 0; c < n; ++c) {
+    LEAF *el = h->cells[c]->el;
+    switch (which) {
+      case 0:
+        for (int v = 0; v < neq; ++v) out[(int64_t)v * n + c] = el->S[v];
+        break;
+      case 1:
+        for (int v = 0; v < neq; ++v) out[(int64_t)v * n + c] = el->SN[v];
+        break;
+      case 2:
+        for (int v = 0; v < neq; ++v) out[(int64_t)v * n + c] = el->RHS[v];
+        break;
+      case 3:
+        for (int f = 0; f < 6; ++f)
+          for (int v = 0; v < neq; ++v) out[((int64_t)f * neq + v) * n + c] = el->SF[f][v];
+        break;
+      case 4:
+        for (int v = 0; v <= neq; ++v)
+          for (int d = 0; d < 3; ++d) out[((int64_t)v * 3 + d) * n + c] = el->SG[v][d];
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+void refh_faceinterp(refh *h) { faceinterp(h->run); }
+void refh_gradcalc(refh *h) { gradcalc(h->run); }
+void refh_rhs(refh *h) { RHS(h->run); }
+void refh_rk(refh *h, int irk) { RK(irk, h->run); }
+
+/* One time step with the stage list `stages` (e.g. {1,2,3} for SSP-RK3,
+ * {1,4} for SSP-RK2, {1} for forward Euler). */
+void refh_step(refh *h, const int *stages, int nstages) {
+  RUN *run = h->run;
+  RK(0, run);
+  for (int s = 0; s < nstages; ++s) {
+    if (run->con->ischeme == 2) faceinterp(run);
+    if (run->con->ns == 1) gradcalc(run);
+    RHS(run);
+    RK(stages[s], run);
+  }
+}
+
+/* Conservation sums, conservationcalc.c:19-34 without the file output. */
+void refh_conservation(const refh *h, double *sums) {
+  const int neq = h->run->con->neq;
+  for (int v = 0; v <= neq; ++v) sums[v] = 0.0;
+  BRANCH *crnt = h->run->topo->locl;
+  while (crnt != NULL) {
+    for (int v = 0; v < neq; ++v) sums[v] += crnt->el->S[v] * crnt->cl->Vol;
+    sums[neq] += crnt->cl->Vol;
+    crnt = crnt->lnxt;
+  }
+}

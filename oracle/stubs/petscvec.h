@@ -1,0 +1,2 @@
+/* Empty stand-in for <petscvec.h>: the reference header includes it, but nothing on
+ * the residual/RK path uses its declarations. Written for the oracle harness. */
