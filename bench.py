@@ -1,0 +1,380 @@
+"""Throughput of the residual + RK step on the 128^3 periodic workload.
+
+One "step" is one full SSP-RK3 time step of the solver (CFL time-step
+reduction + 3 stages of reconstruction, HLLC fluxes, residual and RK update)
+over every cell of the 128^3 = 2,097,152-cell periodic ideal-gas case
+(seeded synthetic state: sinusoidal density, 8-mode Fourier velocities,
+noisy pressure).  The metric is Mcell-updates/s = cells x steps / s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fvgpu|reference]
+
+--impl fvgpu (default) times libfvgpu on the GPU: `value` is the headline
+precision (FP32-mixed when the library supports the case, else FP64) with
+the state resident in HBM; `fp64` holds the FP64 path; `e2e` repeats the
+measurement through the C ABI with the state copied from / to pinned host
+memory every step.  --impl reference times the CPU implementation of the
+same step (the oracle's C restatement of the reference, all host threads).
+Under torchrun each rank runs an independent replica (the path has no
+inter-rank exchange in this build); value = all ranks' cells / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "Mcell-updates/s FP32-mixed vs FP64 plain at ≤1e-6 rel err; adjoint/fwd cost"
+UNIT = "Mcell-updates/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_median": statistics.median(power) if power else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def build_case(level: int):
+    from fv_140823_gb300 import cases
+    return cases.periodic(level=level)
+
+
+def algorithmic_bytes_per_cell_step(neq: int = 5, n_nb: int = 6) -> int:
+    """Compulsory HBM bytes of one SSP-RK3 step per cell with FP64 state:
+    stage 1 reads U and writes U1, stages 2 and 3 read U_k and U and write
+    (8 state passes of neq doubles), plus per stage the n_nb int32 neighbour
+    ids and the 8-byte volume.  neq=5, n_nb=6: 320 + 96 = 416 B."""
+    return 8 * neq * (2 + 3 + 3) + 3 * (4 * n_nb + 8)
+
+
+def traffic_per_launch(kernel: str, ncells: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/traffic.json: bytes per cell of a captured launch), or None."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            t = json.load(fh)
+        return float(t[kernel]["bytes_per_cell"]) * ncells
+    except Exception:
+        return None
+
+
+def time_steps(torch, s, stream, flush, steps: int, cfl: float, scheme="ssprk3"):
+    """Per-step device times (ms), each step bracketed by events on the
+    library's stream, with an L2 flush before each step outside the events."""
+    times = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(scheme, cfl=cfl, nsteps=1)
+            e1.record(stream)
+            times.append((e0, e1))
+    torch.cuda.synchronize()
+    s.synchronize()
+    return [a.elapsed_time(b) for a, b in times]
+
+
+def run_gpu(args):
+    import torch
+
+    from fv_140823_gb300 import abi
+    from fv_140823_gb300.solver import FvGpuError, Solver
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    case = build_case(args.level)
+    t = case.tables
+    n = t.ncells
+    cfl = case.cfl
+
+    results = {}
+    hbm_peak, peak_kind = peaks()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    precisions = [abi.MIXED, abi.FP64] if args.precision == "auto" else (
+        [abi.MIXED] if args.precision == "mixed" else [abi.FP64])
+    states = {}
+    for prec in precisions:
+        cfg = case.cfg
+        cfg.precision = prec
+        cfg.device = local
+        try:
+            s = Solver(t, cfg)
+        except FvGpuError as e:
+            if e.code == abi.ERR_UNSUPPORTED:
+                results[prec] = {"unsupported": str(e)}
+                continue
+            raise
+        stream = torch.cuda.ExternalStream(s.stream_handle())
+        s.set_state(case.U)
+        s.step("ssprk3", cfl=cfl, nsteps=args.warmup)
+        s.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        ms = time_steps(torch, s, stream, flush, args.steps, cfl)
+        clk = clocks.stop()
+        total_ms = float(sum(ms))
+        if dist:
+            tt = torch.tensor([total_ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            total_ms = float(tt.item())
+        value = ws * n * args.steps / (total_ms * 1e-3) / 1e6
+        # live per-kernel timing (eager, events between launches on the library stream)
+        s.set_state(case.U)
+        kms, klaunch = s.profile_step("ssprk3", cfl=cfl, nsteps=max(3, min(args.steps, 10)))
+        dom = int(np.argmax(kms))
+        launches_per_step = int(sum(klaunch)) / max(3, min(args.steps, 10))
+        avg_ms = kms[dom] / max(klaunch[dom], 1)
+        # algorithmic bytes of one stage launch: one third of the step's compulsory bytes
+        alg_bytes = algorithmic_bytes_per_cell_step(case.cfg.neq) / 3.0 * n
+        achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
+        kname = abi.KIND_NAMES[dom]
+        traffic = traffic_per_launch(f"{'mixed' if prec == abi.MIXED else 'fp64'}_{kname}", n)
+        # end to end through the C ABI with pinned host buffers
+        hostU = torch.from_numpy(np.ascontiguousarray(case.U)).pin_memory()
+        hostOut = torch.empty_like(hostU).pin_memory()
+        import ctypes as C
+        e2e_ms = []
+        lib = s.lib
+        for it in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = lib.fvgpu_upload_state(s._ctx, C.c_void_p(hostU.data_ptr()), C.c_int64(n))
+            rc |= lib.fvgpu_step(s._ctx, abi.SCHEME_SSPRK3, 0.0, cfl, 1)
+            rc |= lib.fvgpu_download_state(s._ctx, C.c_void_p(hostOut.data_ptr()), C.c_int64(n))
+            e1.record(stream)
+            e1.synchronize()
+            if rc:
+                raise RuntimeError(f"e2e step failed rc={rc}")
+            if it >= args.warmup:
+                e2e_ms.append(e0.elapsed_time(e1))
+        e2e_total = float(sum(e2e_ms))
+        if dist:
+            tt = torch.tensor([e2e_total], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_total = float(tt.item())
+        e2e_value = ws * n * args.steps / (e2e_total * 1e-3) / 1e6
+        # state after a fixed number of steps at a fixed dt, for the error check
+        s.set_state(case.U)
+        dt0 = s.compute_dt(cfl)
+        s.step("ssprk3", dt=dt0, nsteps=args.err_steps)
+        states[prec] = (s.state(), dt0)
+        results[prec] = {
+            "value": value, "ms_per_step": total_ms / args.steps, "clocks": clk,
+            "kernel_ms": {abi.KIND_NAMES[k]: float(kms[k]) for k in range(len(kms)) if klaunch[k]},
+            "kernel_launches": {abi.KIND_NAMES[k]: int(klaunch[k]) for k in range(len(kms)) if klaunch[k]},
+            "launches_per_step": launches_per_step,
+            "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes,
+                         "avg_launch_ms": avg_ms},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(hostU.numel() * 8),
+                    "d2h_bytes_per_step": int(hostOut.numel() * 8)},
+        }
+        s.close()
+    err = None
+    if abi.MIXED in states and abi.FP64 in states:
+        a, b = states[abi.MIXED][0], states[abi.FP64][0]
+        names = ["rho", "rho_u", "rho_v", "rho_w", "E"]
+        err = {names[v]: float(np.linalg.norm(a[v] - b[v]) / np.linalg.norm(b[v])) for v in range(a.shape[0])}
+    return results, err, case, ws, rank, dist
+
+
+def cpu_baseline(case, steps: int = 1):
+    """The oracle's C restatement on the host cores (all threads), a bounded
+    sample: `steps` SSP-RK3 steps of the full mesh."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from pyoracle import Oracle, ref_available
+    threads = os.cpu_count() or 1
+    Oracle.set_threads(threads)
+    orc = Oracle(case.tables, case.cfg)
+    dt = orc.cfl_dt(case.U, case.cfl)
+    t0 = time.perf_counter()
+    S = case.U
+    for _ in range(steps):
+        S = orc.step(S, dt, "ssprk3", 1)
+    el = time.perf_counter() - t0
+    return {"value": case.tables.ncells * steps / el / 1e6, "unit": UNIT, "cores": Oracle.threads(),
+            "kind": "port",
+            "sample": f"{steps} SSP-RK3 step(s) of the full {case.tables.ncells}-cell mesh, "
+                      f"CFL dt, C restatement of the reference path with {Oracle.threads()} OpenMP threads"
+                      + ("" if not ref_available() else "; oracle/_ref present but serial")}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    case = build_case(args.level)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from pyoracle import Oracle
+    threads = os.cpu_count() or 1
+    Oracle.set_threads(threads)
+    orc = Oracle(case.tables, case.cfg)
+    S = case.U
+    for _ in range(args.warmup):
+        S = orc.step(S, orc.cfl_dt(S, case.cfl), "ssprk3", 1)
+    per = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        dt = orc.cfl_dt(S, case.cfl)
+        S = orc.step(S, dt, "ssprk3", 1)
+        per.append(time.perf_counter() - t0)
+    total = sum(per)
+    value = case.tables.ncells * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(case, args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
+                         "sample": f"every step is one full SSP-RK3 step (CFL dt) of the "
+                                   f"{case.tables.ncells}-cell mesh on {Oracle.threads()} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_of(case, args):
+    return {"workload": f"periodic ideal gas {2 ** args.level}^3 uniform octree (level {args.level}), "
+                        f"{case.tables.ncells} cells, SSP-RK3, CFL 0.5, MUSCL/minmod + HLLC, seed 1234",
+            "cells": case.tables.ncells, "scheme": "ssprk3", "cfl": 0.5, "parallelism": "replicas",
+            "l2": "flushed before every timed step (256 MiB write on the library stream)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fvgpu", choices=["fvgpu", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
+    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--err-steps", type=int, default=50)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+    from fv_140823_gb300 import abi
+    results, err, case, ws, rank, dist = run_gpu(args)
+    if rank == 0:
+        head = abi.MIXED if "value" in results.get(abi.MIXED, {}) else abi.FP64
+        r = results[head]
+        line = {
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if head == abi.MIXED else "f64", "data": "synthetic",
+            "config": config_of(case, args), "precision": "mixed" if head == abi.MIXED else "fp64",
+            "e2e": r["e2e"], "roofline": r["roofline"], "clocks": r["clocks"],
+            "gpu_launches": int(round(r["launches_per_step"] * args.steps)),
+            "kernel_ms": r["kernel_ms"], "kernel_launches": r["kernel_launches"],
+        }
+        if abi.FP64 in results and head != abi.FP64 and "value" in results[abi.FP64]:
+            f = results[abi.FP64]
+            line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "roofline": f["roofline"],
+                            "e2e": f["e2e"], "kernel_ms": f["kernel_ms"]}
+            line["mixed_over_fp64"] = r["value"] / f["value"]
+        elif abi.MIXED in results and "unsupported" in results[abi.MIXED]:
+            line["mixed"] = results[abi.MIXED]
+        if err is not None:
+            line["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps, **err}
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(case)
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -37,6 +37,14 @@ def build_mesh() -> str:
     return out
 
 
+def _file_flags(path: str) -> list[str]:
+    """Per-file nvcc flags from a leading ``// fvbuild: <flags>`` line."""
+    with open(path) as fh:
+        first = fh.readline()
+    tag = "// fvbuild:"
+    return first[len(tag):].split() if first.startswith(tag) else []
+
+
 def gpu_sources() -> list[str]:
     d = os.path.join(CSRC, "gpu")
     if not os.path.isdir(d):
@@ -59,7 +67,7 @@ def build_gpu(extra_flags: list[str] | None = None) -> str | None:
     for s in srcs:
         o = os.path.join(obj_dir, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
-        jobs.append(["nvcc", *flags, "-c", s, "-o", o])
+        jobs.append(["nvcc", *flags, *_file_flags(s), "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(_run, jobs))
     out = os.path.join(LIB, "libfvgpu.so")

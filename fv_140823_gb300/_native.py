@@ -46,3 +46,49 @@ def load_mesh_lib() -> C.CDLL:
         lib.fvmesh_last_error.restype = C.c_char_p
         lib._fv_typed = True
     return lib
+
+
+# Every entry point declared in include/fvgpu.h, with its ctypes signature.
+_GPU_SIGS = {
+    "fvgpu_create": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+    "fvgpu_destroy": ([C.c_void_p], C.c_int),
+    "fvgpu_set_precision": ([C.c_void_p, C.c_int], C.c_int),
+    "fvgpu_upload_mesh": ([C.c_void_p, C.c_void_p], C.c_int),
+    "fvgpu_upload_state": ([C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_download_state": ([C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_download": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "fvgpu_faceinterp": ([C.c_void_p], C.c_int),
+    "fvgpu_gradcalc": ([C.c_void_p], C.c_int),
+    "fvgpu_rhs": ([C.c_void_p], C.c_int),
+    "fvgpu_set_inner": ([C.c_void_p, C.c_void_p], C.c_int),
+    "fvgpu_rhs_nb": ([C.c_void_p, C.c_int], C.c_int),
+    "fvgpu_rk": ([C.c_void_p, C.c_int, C.c_double], C.c_int),
+    "fvgpu_step": ([C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int], C.c_int),
+    "fvgpu_compute_dt": ([C.c_void_p, C.c_double, C.POINTER(C.c_double)], C.c_int),
+    "fvgpu_conservation": ([C.c_void_p, C.c_void_p], C.c_int),
+    "fvgpu_residual_vjp": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_last_error": ([C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.c_char_p, C.c_int],
+                         C.c_int),
+    "fvgpu_neq": ([C.c_void_p], C.c_int),
+    "fvgpu_synchronize": ([C.c_void_p], C.c_int),
+    "fvgpu_profile_step": ([C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
+                           C.c_int),
+    "fvgpu_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+}
+
+
+def gpu_symbols() -> list[str]:
+    return list(_GPU_SIGS)
+
+
+def load_gpu_lib() -> C.CDLL:
+    lib = _load("libfvgpu.so")
+    if not getattr(lib, "_fv_typed", False):
+        for name, (args, res) in _GPU_SIGS.items():
+            fn = getattr(lib, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = res
+        lib._fv_typed = True
+    return lib

@@ -1,0 +1,867 @@
+// C ABI of libfvgpu (include/fvgpu.h): context, resident mesh and state,
+// the reference's RHS / RK calls, graph-captured time steps, reductions.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fv_kernels.cuh"
+#include "fv_mixed.cuh"
+#include "fvgpu.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t b) {
+    release();
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+  template <typename T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+struct GraphKey {
+  int scheme, cfl, precision;
+  bool operator<(const GraphKey &o) const {
+    if (scheme != o.scheme) return scheme < o.scheme;
+    if (cfl != o.cfl) return cfl < o.cfl;
+    return precision < o.precision;
+  }
+};
+
+// device scalars, one allocation
+struct Scalars {
+  double dt;
+  double lambda;
+  double lambda_tmp;
+  double cfl;
+  unsigned long long err;
+  unsigned long long pad[3];
+};
+
+}  // namespace
+
+struct fvgpu_ctx {
+  fvgpu_config cfg{};
+  int neq = 5;
+  cudaStream_t stream = nullptr;
+  fv::Phys ph{};
+  // mesh
+  int64_t n = 0, nhang = 0;
+  bool has_mesh = false;
+  DevBuf nbr, nbr_face, area, dcf, dcc, vol, hang_nbr, hang_area, level, inner;
+  // state and work arrays
+  DevBuf S, SN, R, SF, SG;
+  DevBuf scal;      // Scalars
+  DevBuf partial;   // conservation partial sums
+  Scalars *h_scal = nullptr;  // pinned mirror
+  bool lambda_valid = false;
+  bool has_inner = false;
+  // mixed-precision path resources
+  fv::MixedResources mixed;
+  fv::LaunchMarks marks;
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  std::map<GraphKey, int> graph_launches;  // kernels per captured step
+  // last error
+  int last_code = 0;
+  int64_t last_cell = -1;
+  std::string last_msg;
+
+  fv::MeshView view() const {
+    fv::MeshView m;
+    m.n = n;
+    m.nhang = nhang;
+    m.nbr = nbr.as<int32_t>();
+    m.nbr_face = nbr_face.as<int32_t>();
+    m.area = area.as<double>();
+    m.dcf = dcf.as<double>();
+    m.dcc = dcc.as<double>();
+    m.vol = vol.as<double>();
+    m.hang_nbr = hang_nbr.as<int32_t>();
+    m.hang_area = hang_area.as<double>();
+    return m;
+  }
+  Scalars *d_scal() const { return scal.as<Scalars>(); }
+  double *d_dt() const { return &d_scal()->dt; }
+  double *d_lambda() const { return &d_scal()->lambda; }
+  double *d_lambda_tmp() const { return &d_scal()->lambda_tmp; }
+  unsigned long long *d_err() const { return &d_scal()->err; }
+
+  void drop_graphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+};
+
+namespace {
+
+int set_err(fvgpu_ctx *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) {
+    ctx->last_code = code;
+    ctx->last_cell = -1;
+    ctx->last_msg = buf;
+  } else {
+    g_create_error = buf;
+  }
+  return code;
+}
+
+#define FV_CUDA(ctx, call)                                                                   \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return set_err(ctx, e_ == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA, \
+                     "%s: %s", #call, cudaGetErrorString(e_));                               \
+  } while (0)
+
+#define FV_LAUNCHED(ctx) FV_CUDA(ctx, cudaGetLastError())
+
+// Conservation: fixed partition of the cells over kConsBlocks blocks, fixed
+// in-block tree, fixed final tree -> the same sums on every run.
+constexpr int kConsBlocks = 1024;
+constexpr int kConsThreads = 256;
+
+__global__ void k_cons_partial(int neq, int64_t n, const double *__restrict__ S, const double *__restrict__ vol,
+                               double *__restrict__ partial) {
+  __shared__ double red[kConsThreads];
+  const int64_t per = (n + kConsBlocks - 1) / kConsBlocks;
+  const int64_t lo = int64_t(blockIdx.x) * per;
+  const int64_t hi = lo + per < n ? lo + per : n;
+  for (int v = 0; v <= neq; ++v) {
+    double acc = 0.0;
+    for (int64_t c = lo + threadIdx.x; c < hi; c += kConsThreads)
+      acc += v < neq ? S[v * n + c] * vol[c] : vol[c];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = kConsThreads / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[v * kConsBlocks + blockIdx.x] = red[0];
+    __syncthreads();
+  }
+}
+
+__global__ void k_cons_final(int neq, const double *__restrict__ partial, double *__restrict__ sums) {
+  __shared__ double red[kConsThreads];
+  for (int v = 0; v <= neq; ++v) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < kConsBlocks; b += kConsThreads) acc += partial[v * kConsBlocks + b];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = kConsThreads / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[v] = red[0];
+    __syncthreads();
+  }
+}
+
+__global__ void k_dt(const double *lambda_in, double *lambda_reset, const double *cflp, double *dt,
+                     unsigned long long *err) {
+  const double lam = *lambda_in;
+  const double cfl = *cflp;
+  if (!(lam > 0.0) || isinf(lam) || isnan(lam)) {
+    *dt = 0.0;
+    if (err && *err == 0ull) *err = (fv::kErrNonFinite << 40) | 0xffffffffffull;
+  } else {
+    *dt = cfl / lam;
+  }
+  if (lambda_reset) *lambda_reset = 0.0;
+}
+
+__global__ void k_set_double(double *p, double v) { *p = v; }
+
+int check_device_error(fvgpu_ctx *ctx) {
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned long long e = ctx->h_scal->err;
+  if (e != 0ull) {
+    const int code = int(e >> 40);
+    const int64_t cell = int64_t(e & 0xffffffffffull);
+    const int rc = code == int(fv::kErrEos) ? FVGPU_ERR_EOS : FVGPU_ERR_NONFINITE;
+    set_err(ctx, rc, "device error %d at cell %lld (%s)", code, (long long)cell,
+            code == 1 ? "non-finite residual or time step" : code == 2 ? "EOS without a real root"
+                                                                       : "HLLC wave speeds not finite");
+    ctx->last_cell = cell == 0xffffffffffll ? -1 : cell;
+    // clear so the context stays usable
+    ctx->h_scal->err = 0ull;
+    FV_CUDA(ctx, cudaMemcpyAsync(ctx->d_err(), &ctx->h_scal->err, sizeof(unsigned long long),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return rc;
+  }
+  return FVGPU_OK;
+}
+
+// Pull the device error word into the pinned mirror (async) and check.
+int sync_and_check(fvgpu_ctx *ctx) {
+  FV_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scal->err, ctx->d_err(), sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  return check_device_error(ctx);
+}
+
+int validate_config(const fvgpu_config *c, char *why, size_t whylen) {
+  if (c->model < 1 || c->model > 3) {
+    snprintf(why, whylen,
+             "model %d unsupported (1-3; the reference's model 4 accumulates no flux, "
+             "residual_faces_AMR.c:216-236)",
+             c->model);
+    return FVGPU_ERR_UNSUPPORTED;
+  }
+  if (c->iprimtv != 0) {
+    snprintf(why, whylen,
+             "iprimtv=1 unsupported: the reference's cons2primtv reads sol->r, which "
+             "facevalues_MUSCL never sets (cons2primtv.c:5, facevalues_MUSCL.c:3-56)");
+    return FVGPU_ERR_UNSUPPORTED;
+  }
+  if (c->ischeme != 1 && c->ischeme != 2) {
+    snprintf(why, whylen, "ischeme must be 1 or 2");
+    return FVGPU_ERR_ARG;
+  }
+  if (c->ns != 0 && c->ns != 1) {
+    snprintf(why, whylen, "ns must be 0 or 1");
+    return FVGPU_ERR_ARG;
+  }
+  if (c->precision != FVGPU_FP64 && c->precision != FVGPU_MIXED) {
+    snprintf(why, whylen, "precision must be FVGPU_FP64 or FVGPU_MIXED");
+    return FVGPU_ERR_ARG;
+  }
+  if (c->model == 1 && !(c->gamma > 1.0)) {
+    snprintf(why, whylen, "gamma must exceed 1");
+    return FVGPU_ERR_ARG;
+  }
+  return FVGPU_OK;
+}
+
+fv::Phys make_phys(const fvgpu_config &c, int neq, const double *frames) {
+  fv::Phys p{};
+  p.model = c.model;
+  p.ns = c.ns;
+  p.ischeme = c.ischeme;
+  p.eos = c.eos;
+  p.neq = neq;
+  p.gamma = c.gamma;
+  p.pinf = c.pinf;
+  p.visc = c.visc;
+  p.ymin = c.ymin;
+  for (int i = 0; i < 8; ++i) p.inflow[i] = c.inflow[i];
+  if (frames)
+    for (int i = 0; i < 54; ++i) p.frames[i] = frames[i];
+  return p;
+}
+
+// Host-side validation of the flattened tables: every index in range,
+// geometry positive and finite, and each face link reciprocated by the
+// neighbour's face (1:1, coarse-to-fine and fine-to-coarse).
+int validate_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
+  const int64_t n = m->ncells, nh = m->nhang;
+  if (n <= 0 || n >= (int64_t(1) << 31)) return set_err(ctx, FVGPU_ERR_MESH, "ncells %lld out of range", (long long)n);
+  if (nh < 0 || nh > 6 * n) return set_err(ctx, FVGPU_ERR_MESH, "nhang %lld out of range", (long long)nh);
+  if (!m->nbr || !m->nbr_face || !m->area || !m->dcf || !m->dcc || !m->vol || !m->frames ||
+      (nh > 0 && (!m->hang_nbr || !m->hang_area)))
+    return set_err(ctx, FVGPU_ERR_ARG, "null mesh array");
+  for (int i = 0; i < 54; ++i)
+    if (!std::isfinite(m->frames[i])) return set_err(ctx, FVGPU_ERR_MESH, "non-finite face frame");
+  for (int64_t c = 0; c < n; ++c)
+    if (!(m->vol[c] > 0.0) || !std::isfinite(m->vol[c]))
+      return set_err(ctx, FVGPU_ERR_MESH, "cell %lld: volume must be positive", (long long)c);
+  std::vector<uint8_t> hang_seen(size_t(nh), 0);
+  for (int f = 0; f < 6; ++f) {
+    for (int64_t c = 0; c < n; ++c) {
+      const int64_t i = f * n + c;
+      const int32_t code = m->nbr[i];
+      const double A = m->area[i], dcf = m->dcf[i], dcc = m->dcc[i];
+      if (!(dcf >= 0.0) || !(dcc >= 0.0) || !std::isfinite(dcf) || !std::isfinite(dcc))
+        return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: bad stencil distance", (long long)c, f);
+      if (code < 0 && code > FVGPU_HANG0) {
+        const int bc = -1 - code;
+        if (bc < 1 || bc > 4)
+          return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: boundary code %d not in 1..4", (long long)c, f, bc);
+        if (bc == 1 && ctx->cfg.model != 1)
+          return set_err(ctx, FVGPU_ERR_UNSUPPORTED,
+                         "inflow boundaries need model 1 (asinvalues_multiphase.c:22 fills the other side)");
+        if (!(A > 0.0) || !std::isfinite(A))
+          return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: area must be positive", (long long)c, f);
+        continue;
+      }
+      const int nf = m->nbr_face[i];
+      if (nf < 0 || nf > 5)
+        return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: neighbour face %d", (long long)c, f, nf);
+      if (!(dcc > 0.0))
+        return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: interior face needs dcc > 0", (long long)c, f);
+      if (code >= 0) {
+        if (code >= n) return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: neighbour %d out of range", (long long)c, f, code);
+        if (!(A > 0.0) || !std::isfinite(A))
+          return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: area must be positive", (long long)c, f);
+        // reciprocity: neighbour's face nf points back at c, or is a 1:4 face containing c
+        const int32_t back = m->nbr[int64_t(nf) * n + code];
+        bool ok = back == c;
+        if (!ok && back <= FVGPU_HANG0) {
+          const int64_t r = int64_t(FVGPU_HANG0) - back;
+          if (r < nh)
+            for (int s = 0; s < 4; ++s) ok |= m->hang_nbr[4 * r + s] == c;
+        }
+        if (!ok)
+          return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: neighbour %d does not link back", (long long)c, f, code);
+      } else {
+        const int64_t r = int64_t(FVGPU_HANG0) - code;
+        if (r >= nh) return set_err(ctx, FVGPU_ERR_MESH, "cell %lld face %d: hanging record %lld out of range", (long long)c, f, (long long)r);
+        if (hang_seen[size_t(r)]) return set_err(ctx, FVGPU_ERR_MESH, "hanging record %lld used twice", (long long)r);
+        hang_seen[size_t(r)] = 1;
+        for (int s = 0; s < 4; ++s) {
+          const int32_t k = m->hang_nbr[4 * r + s];
+          const double a = m->hang_area[4 * r + s];
+          if (k < 0 || k >= n) return set_err(ctx, FVGPU_ERR_MESH, "hanging record %lld: neighbour out of range", (long long)r);
+          if (!(a > 0.0) || !std::isfinite(a)) return set_err(ctx, FVGPU_ERR_MESH, "hanging record %lld: area must be positive", (long long)r);
+          if (m->nbr[int64_t(nf) * n + k] != c)
+            return set_err(ctx, FVGPU_ERR_MESH, "hanging record %lld: fine neighbour %d does not link back", (long long)r, k);
+        }
+      }
+    }
+  }
+  return FVGPU_OK;
+}
+
+int ensure_state(fvgpu_ctx *ctx) {
+  if (!ctx) return FVGPU_ERR_ARG;
+  if (!ctx->has_mesh) return set_err(ctx, FVGPU_ERR_STATE, "no mesh uploaded");
+  return FVGPU_OK;
+}
+
+// ---- launch sequences -------------------------------------------------------
+
+int enqueue_faceinterp(fvgpu_ctx *ctx) {
+  ctx->marks.mark(FVGPU_KIND_FACEINTERP);
+  fv::launch_faceinterp_fp64(ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->SF.as<double>(), ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+int enqueue_gradcalc(fvgpu_ctx *ctx) {
+  ctx->marks.mark(FVGPU_KIND_GRADCALC);
+  fv::launch_gradcalc_fp64(ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->SG.as<double>(), ctx->d_err(),
+                           ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+fv::ResidualArgs residual_args(fvgpu_ctx *ctx) {
+  fv::ResidualArgs a{};
+  a.U = ctx->S.as<double>();
+  a.SF = ctx->SF.as<double>();
+  a.SG = ctx->SG.as<double>();
+  a.R = ctx->R.as<double>();
+  a.S_out = ctx->S.as<double>();
+  a.SN = ctx->SN.as<double>();
+  a.dt = ctx->d_dt();
+  a.lambda = nullptr;
+  a.inner = nullptr;
+  a.inner_outer = 0;
+  a.irk = 0;
+  a.err = ctx->d_err();
+  return a;
+}
+
+int enqueue_rhs(fvgpu_ctx *ctx, const int32_t *inner, int inner_outer) {
+  fv::ResidualArgs a = residual_args(ctx);
+  a.inner = inner;
+  a.inner_outer = inner_outer;
+  ctx->marks.mark(FVGPU_KIND_RESIDUAL);
+  fv::launch_residual_fp64(ctx->ph, ctx->view(), a, ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+// One RK step: stages of `scheme`; CFL dt from lambda when cfl_mode.
+int enqueue_step_fp64(fvgpu_ctx *ctx, int scheme, bool cfl_mode) {
+  static const int kStages[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 4, 0}, {1, 2, 3}};
+  static const int kN[4] = {0, 1, 2, 3};
+  if (cfl_mode) {
+    ctx->marks.mark(FVGPU_KIND_DT);
+    k_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_lambda(), ctx->d_lambda(), &ctx->d_scal()->cfl, ctx->d_dt(),
+                                   ctx->d_err());
+    FV_LAUNCHED(ctx);
+  }
+  const int ns = kN[scheme];
+  const fv::MeshView mv = ctx->view();
+  if (ctx->cfg.ischeme == 1) {
+    ctx->marks.mark(FVGPU_KIND_RK);
+    fv::launch_rk_fp64(0, ctx->ph, mv, ctx->S.as<double>(), ctx->SN.as<double>(), ctx->R.as<double>(),
+                       ctx->d_dt(), nullptr, ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  for (int k = 0; k < ns; ++k) {
+    const int irk = kStages[scheme][k];
+    const bool last = k == ns - 1;
+    if (ctx->cfg.ischeme == 2) {
+      int rc = enqueue_faceinterp(ctx);
+      if (rc) return rc;
+    }
+    if (ctx->cfg.ns == 1) {
+      int rc = enqueue_gradcalc(ctx);
+      if (rc) return rc;
+    }
+    if (ctx->cfg.ischeme == 2) {
+      fv::ResidualArgs a = residual_args(ctx);
+      a.R = nullptr;
+      a.irk = irk;
+      a.lambda = (last && cfl_mode) ? ctx->d_lambda() : nullptr;
+      ctx->marks.mark(FVGPU_KIND_RESIDUAL);
+      fv::launch_residual_fp64(ctx->ph, mv, a, ctx->stream);
+      FV_LAUNCHED(ctx);
+    } else {
+      int rc = enqueue_rhs(ctx, nullptr, 0);
+      if (rc) return rc;
+      ctx->marks.mark(FVGPU_KIND_RK);
+      fv::launch_rk_fp64(irk, ctx->ph, mv, ctx->S.as<double>(), ctx->SN.as<double>(), ctx->R.as<double>(),
+                         ctx->d_dt(), (last && cfl_mode) ? ctx->d_lambda() : nullptr, ctx->stream);
+      FV_LAUNCHED(ctx);
+    }
+  }
+  return FVGPU_OK;
+}
+
+int enqueue_step(fvgpu_ctx *ctx, int scheme, bool cfl_mode) {
+  if (ctx->cfg.precision == FVGPU_MIXED)
+    return fv::enqueue_step_mixed(ctx->mixed, ctx->ph, ctx->view(), scheme, cfl_mode, ctx->S.as<double>(),
+                                  ctx->SN.as<double>(), ctx->d_dt(), ctx->d_lambda(), &ctx->d_scal()->cfl,
+                                  ctx->d_err(), ctx->marks, ctx->stream) == cudaSuccess
+               ? FVGPU_OK
+               : set_err(ctx, FVGPU_ERR_CUDA, "mixed step launch: %s", cudaGetErrorString(cudaGetLastError()));
+  return enqueue_step_fp64(ctx, scheme, cfl_mode);
+}
+
+int ensure_lambda(fvgpu_ctx *ctx) {
+  if (ctx->lambda_valid) return FVGPU_OK;
+  FV_CUDA(ctx, cudaMemsetAsync(ctx->d_lambda(), 0, sizeof(double), ctx->stream));
+  ctx->marks.mark(FVGPU_KIND_DT);
+  fv::launch_lambda_fp64(ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->d_lambda(), ctx->stream);
+  FV_LAUNCHED(ctx);
+  ctx->lambda_valid = true;
+  return FVGPU_OK;
+}
+
+}  // namespace
+
+namespace fv {
+void launch_dt_from_lambda(const double *lambda_in, double *lambda_reset, const double *cfl, double *dt,
+                           unsigned long long *err, cudaStream_t st) {
+  k_dt<<<1, 1, 0, st>>>(lambda_in, lambda_reset, cfl, dt, err);
+}
+}  // namespace fv
+
+extern "C" {
+
+int fvgpu_create(const fvgpu_config *cfg, fvgpu_ctx **out) {
+  if (!cfg || !out) return set_err(nullptr, FVGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  char why[256];
+  int rc = validate_config(cfg, why, sizeof why);
+  if (rc) return set_err(nullptr, rc, "%s", why);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(nullptr, FVGPU_ERR_NODEVICE, "no CUDA device");
+  }
+  if (cfg->device < 0 || cfg->device >= ndev) return set_err(nullptr, FVGPU_ERR_ARG, "device %d out of range", cfg->device);
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return set_err(nullptr, FVGPU_ERR_CUDA, "cudaSetDevice failed");
+  fvgpu_ctx *ctx = new fvgpu_ctx();
+  ctx->cfg = *cfg;
+  ctx->neq = cfg->model == 2 ? 4 : 5;
+  ctx->ph = make_phys(*cfg, ctx->neq, nullptr);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      ctx->scal.alloc(sizeof(Scalars)) != cudaSuccess ||
+      cudaMallocHost((void **)&ctx->h_scal, sizeof(Scalars)) != cudaSuccess ||
+      ctx->partial.alloc(sizeof(double) * (kConsBlocks * (fv::kNeqMax + 1) + 8)) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return set_err(nullptr, FVGPU_ERR_CUDA, "context allocation failed");
+  }
+  memset(ctx->h_scal, 0, sizeof(Scalars));
+  if (cudaMemset(ctx->scal.p, 0, sizeof(Scalars)) != cudaSuccess) {
+    delete ctx;
+    return set_err(nullptr, FVGPU_ERR_CUDA, "cudaMemset failed");
+  }
+  *out = ctx;
+  return FVGPU_OK;
+}
+
+int fvgpu_destroy(fvgpu_ctx *ctx) {
+  if (!ctx) return FVGPU_OK;
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->drop_graphs();
+  fv::release_mixed(ctx->mixed);
+  if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return FVGPU_OK;
+}
+
+int fvgpu_neq(const fvgpu_ctx *ctx) { return ctx ? ctx->neq : 0; }
+
+int fvgpu_set_precision(fvgpu_ctx *ctx, int precision) {
+  if (!ctx) return FVGPU_ERR_ARG;
+  if (precision != FVGPU_FP64 && precision != FVGPU_MIXED)
+    return set_err(ctx, FVGPU_ERR_ARG, "precision must be FVGPU_FP64 or FVGPU_MIXED");
+  if (precision == ctx->cfg.precision) return FVGPU_OK;
+  cudaSetDevice(ctx->cfg.device);
+  if (precision == FVGPU_MIXED && ctx->has_mesh) {
+    char why[256];
+    if (!fv::mixed_supported(ctx->ph, why, sizeof why)) return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
+    if (fv::prepare_mixed(ctx->mixed, ctx->ph, ctx->view(), ctx->level.as<int32_t>(), ctx->stream) != cudaSuccess)
+      return set_err(ctx, FVGPU_ERR_CUDA, "mixed-path setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  ctx->cfg.precision = precision;
+  ctx->drop_graphs();
+  return FVGPU_OK;
+}
+
+int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
+  if (!ctx || !m) return set_err(ctx, FVGPU_ERR_ARG, "null argument");
+  int rc = validate_mesh(ctx, m);
+  if (rc) return rc;
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->drop_graphs();
+  fv::release_mixed(ctx->mixed);
+  ctx->has_mesh = false;
+  const int64_t n = m->ncells, nh = m->nhang;
+  const int neq = ctx->neq;
+  struct Up {
+    DevBuf *buf;
+    const void *src;
+    size_t bytes;
+  } ups[] = {
+      {&ctx->nbr, m->nbr, sizeof(int32_t) * 6 * n},     {&ctx->nbr_face, m->nbr_face, sizeof(int32_t) * 6 * n},
+      {&ctx->area, m->area, sizeof(double) * 6 * n},    {&ctx->dcf, m->dcf, sizeof(double) * 6 * n},
+      {&ctx->dcc, m->dcc, sizeof(double) * 6 * n},      {&ctx->vol, m->vol, sizeof(double) * n},
+      {&ctx->hang_nbr, m->hang_nbr, sizeof(int32_t) * 4 * nh},
+      {&ctx->hang_area, m->hang_area, sizeof(double) * 4 * nh},
+      {&ctx->level, m->level, m->level ? sizeof(int32_t) * n : 0},
+  };
+  for (auto &u : ups) {
+    FV_CUDA(ctx, u.buf->alloc(u.bytes));
+    if (u.src && u.bytes) FV_CUDA(ctx, cudaMemcpy(u.buf->p, u.src, u.bytes, cudaMemcpyHostToDevice));
+  }
+  FV_CUDA(ctx, ctx->S.alloc(sizeof(double) * neq * n));
+  FV_CUDA(ctx, ctx->SN.alloc(sizeof(double) * neq * n));
+  FV_CUDA(ctx, ctx->R.alloc(sizeof(double) * neq * n));
+  FV_CUDA(ctx, ctx->SF.alloc(ctx->cfg.ischeme == 2 ? sizeof(double) * 6 * neq * n : 16));
+  FV_CUDA(ctx, ctx->SG.alloc(ctx->cfg.ns == 1 ? sizeof(double) * (neq + 1) * 3 * n : 16));
+  FV_CUDA(ctx, cudaMemset(ctx->S.p, 0, ctx->S.bytes));
+  FV_CUDA(ctx, cudaMemset(ctx->SN.p, 0, ctx->SN.bytes));
+  FV_CUDA(ctx, cudaMemset(ctx->R.p, 0, ctx->R.bytes));
+  FV_CUDA(ctx, cudaMemset(ctx->SF.p, 0, ctx->SF.bytes));
+  FV_CUDA(ctx, cudaMemset(ctx->SG.p, 0, ctx->SG.bytes));
+  ctx->inner.release();
+  ctx->has_inner = false;
+  ctx->n = n;
+  ctx->nhang = nh;
+  ctx->ph = make_phys(ctx->cfg, neq, m->frames);
+  ctx->lambda_valid = false;
+  if (ctx->cfg.precision == FVGPU_MIXED) {
+    char why[256];
+    if (!fv::mixed_supported(ctx->ph, why, sizeof why)) return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
+    if (fv::prepare_mixed(ctx->mixed, ctx->ph, ctx->view(), ctx->level.as<int32_t>(), ctx->stream) != cudaSuccess)
+      return set_err(ctx, FVGPU_ERR_CUDA, "mixed-path setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  FV_CUDA(ctx, cudaDeviceSynchronize());
+  ctx->has_mesh = true;
+  return FVGPU_OK;
+}
+
+int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->S.p, sizeof(double) * ctx->n, U, sizeof(double) * ld,
+                                 sizeof(double) * ctx->n, ctx->neq, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->lambda_valid = false;
+  return FVGPU_OK;
+}
+
+int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaMemcpy2DAsync(U, sizeof(double) * ld, ctx->S.p, sizeof(double) * ctx->n,
+                                 sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int fvgpu_download(fvgpu_ctx *ctx, int field, double *out) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!out) return set_err(ctx, FVGPU_ERR_ARG, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  const DevBuf *b = nullptr;
+  size_t bytes = 0;
+  const int64_t n = ctx->n;
+  switch (field) {
+    case FVGPU_FIELD_S: b = &ctx->S; bytes = sizeof(double) * ctx->neq * n; break;
+    case FVGPU_FIELD_SN: b = &ctx->SN; bytes = sizeof(double) * ctx->neq * n; break;
+    case FVGPU_FIELD_RHS: b = &ctx->R; bytes = sizeof(double) * ctx->neq * n; break;
+    case FVGPU_FIELD_SF:
+      if (ctx->cfg.ischeme != 2) return set_err(ctx, FVGPU_ERR_STATE, "SF exists only for ischeme 2");
+      b = &ctx->SF; bytes = sizeof(double) * 6 * ctx->neq * n; break;
+    case FVGPU_FIELD_SG:
+      if (ctx->cfg.ns != 1) return set_err(ctx, FVGPU_ERR_STATE, "SG exists only for ns 1");
+      b = &ctx->SG; bytes = sizeof(double) * (ctx->neq + 1) * 3 * n; break;
+    default: return set_err(ctx, FVGPU_ERR_ARG, "unknown field %d", field);
+  }
+  FV_CUDA(ctx, cudaMemcpyAsync(out, b->p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int fvgpu_faceinterp(fvgpu_ctx *ctx) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (ctx->cfg.ischeme != 2) return set_err(ctx, FVGPU_ERR_STATE, "faceinterp needs ischeme 2");
+  cudaSetDevice(ctx->cfg.device);
+  return enqueue_faceinterp(ctx);
+}
+
+int fvgpu_gradcalc(fvgpu_ctx *ctx) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (ctx->cfg.ns != 1) return set_err(ctx, FVGPU_ERR_STATE, "gradcalc needs ns 1");
+  cudaSetDevice(ctx->cfg.device);
+  return enqueue_gradcalc(ctx);
+}
+
+int fvgpu_rhs(fvgpu_ctx *ctx) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  cudaSetDevice(ctx->cfg.device);
+  return enqueue_rhs(ctx, nullptr, 0);
+}
+
+int fvgpu_set_inner(fvgpu_ctx *ctx, const int32_t *inner) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!inner) return set_err(ctx, FVGPU_ERR_ARG, "null inner flags");
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, ctx->inner.alloc(sizeof(int32_t) * ctx->n));
+  FV_CUDA(ctx, cudaMemcpy(ctx->inner.p, inner, sizeof(int32_t) * ctx->n, cudaMemcpyHostToDevice));
+  ctx->has_inner = true;
+  return FVGPU_OK;
+}
+
+int fvgpu_rhs_nb(fvgpu_ctx *ctx, int inner_outer) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!ctx->has_inner) return set_err(ctx, FVGPU_ERR_STATE, "fvgpu_set_inner not called");
+  cudaSetDevice(ctx->cfg.device);
+  return enqueue_rhs(ctx, ctx->inner.as<int32_t>(), inner_outer);
+}
+
+int fvgpu_rk(fvgpu_ctx *ctx, int irk, double dt) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (irk < 0 || irk > 4) return set_err(ctx, FVGPU_ERR_ARG, "irk must lie in 0..4");
+  cudaSetDevice(ctx->cfg.device);
+  k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
+  FV_LAUNCHED(ctx);
+  fv::launch_rk_fp64(irk, ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->SN.as<double>(), ctx->R.as<double>(),
+                     ctx->d_dt(), nullptr, ctx->stream);
+  FV_LAUNCHED(ctx);
+  ctx->lambda_valid = false;
+  return FVGPU_OK;
+}
+
+int fvgpu_compute_dt(fvgpu_ctx *ctx, double cfl, double *dt) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!dt || !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "need cfl > 0 and an output pointer");
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaMemsetAsync(ctx->d_lambda_tmp(), 0, sizeof(double), ctx->stream));
+  fv::launch_lambda_fp64(ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->d_lambda_tmp(), ctx->stream);
+  FV_LAUNCHED(ctx);
+  FV_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scal->lambda_tmp, ctx->d_lambda_tmp(), sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  rc = sync_and_check(ctx);
+  if (rc) return rc;
+  const double lam = ctx->h_scal->lambda_tmp;
+  if (!(lam > 0.0) || !std::isfinite(lam)) return set_err(ctx, FVGPU_ERR_NONFINITE, "spectral radius %g", lam);
+  *dt = cfl / lam;
+  return FVGPU_OK;
+}
+
+int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (scheme < FVGPU_SCHEME_EULER || scheme > FVGPU_SCHEME_SSPRK3 || nsteps < 0)
+    return set_err(ctx, FVGPU_ERR_ARG, "bad scheme or step count");
+  const bool cfl_mode = !(dt > 0.0);
+  if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
+  cudaSetDevice(ctx->cfg.device);
+  if (nsteps == 0) return FVGPU_OK;
+  if (cfl_mode) {
+    rc = ensure_lambda(ctx);
+    if (rc) return rc;
+    k_set_double<<<1, 1, 0, ctx->stream>>>(&ctx->d_scal()->cfl, cfl);
+  } else {
+    k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
+  }
+  FV_LAUNCHED(ctx);
+  const GraphKey key{scheme, cfl_mode ? 1 : 0, ctx->cfg.precision};
+  auto it = ctx->graphs.find(key);
+  if (it == ctx->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    int before = 0;
+    for (int k = 0; k < FVGPU_NKINDS; ++k) before += ctx->marks.counts[k];
+    FV_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_step(ctx, scheme, cfl_mode);
+    int after = 0;
+    for (int k = 0; k < FVGPU_NKINDS; ++k) after += ctx->marks.counts[k];
+    ctx->graph_launches[key] = after - before;
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return set_err(ctx, FVGPU_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    cudaGraphExec_t ge = nullptr;
+    ce = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_err(ctx, FVGPU_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    it = ctx->graphs.emplace(key, ge).first;
+  }
+  for (int s = 0; s < nsteps; ++s) FV_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+  if (!cfl_mode) ctx->lambda_valid = false;
+  return FVGPU_OK;
+}
+
+int fvgpu_profile_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps, double *ms,
+                       int *launches) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!ms || !launches || nsteps <= 0) return set_err(ctx, FVGPU_ERR_ARG, "need outputs and nsteps > 0");
+  if (scheme < FVGPU_SCHEME_EULER || scheme > FVGPU_SCHEME_SSPRK3) return set_err(ctx, FVGPU_ERR_ARG, "bad scheme");
+  const bool cfl_mode = !(dt > 0.0);
+  if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
+  cudaSetDevice(ctx->cfg.device);
+  if (cfl_mode) {
+    rc = ensure_lambda(ctx);
+    if (rc) return rc;
+    k_set_double<<<1, 1, 0, ctx->stream>>>(&ctx->d_scal()->cfl, cfl);
+  } else {
+    k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
+  }
+  FV_LAUNCHED(ctx);
+  const int cap = 64 * nsteps + 2;
+  std::vector<cudaEvent_t> ev(size_t(cap), nullptr);
+  std::vector<int> kinds(size_t(cap), -1);
+  for (auto &e : ev) FV_CUDA(ctx, cudaEventCreate(&e));
+  fv::LaunchMarks &mk = ctx->marks;
+  mk.active = true;
+  mk.stream = ctx->stream;
+  mk.events = ev.data();
+  mk.kinds = kinds.data();
+  mk.capacity = cap - 1;
+  mk.used = 0;
+  for (int s = 0; s < nsteps && rc == 0; ++s) rc = enqueue_step(ctx, scheme, cfl_mode);
+  const int used = mk.used;
+  cudaEventRecord(ev[size_t(used)], ctx->stream);
+  mk.active = false;
+  mk.events = nullptr;
+  mk.kinds = nullptr;
+  if (!rc) rc = sync_and_check(ctx);
+  for (int k = 0; k < FVGPU_NKINDS; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  if (!rc) {
+    for (int i = 0; i < used; ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[size_t(i)], ev[size_t(i) + 1]);
+      ms[kinds[size_t(i)]] += double(t);
+      launches[kinds[size_t(i)]] += 1;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (!cfl_mode) ctx->lambda_valid = false;
+  return rc;
+}
+
+int fvgpu_get_stream(fvgpu_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return FVGPU_ERR_ARG;
+  *stream = (void *)ctx->stream;
+  return FVGPU_OK;
+}
+
+int fvgpu_conservation(fvgpu_ctx *ctx, double *sums) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!sums) return set_err(ctx, FVGPU_ERR_ARG, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  double *part = ctx->partial.as<double>();
+  k_cons_partial<<<kConsBlocks, kConsThreads, 0, ctx->stream>>>(ctx->neq, ctx->n, ctx->S.as<double>(),
+                                                                ctx->vol.as<double>(), part);
+  FV_LAUNCHED(ctx);
+  double *d_sums = part + kConsBlocks * (fv::kNeqMax + 1);  // 8 spare slots after the block rows
+  k_cons_final<<<1, kConsThreads, 0, ctx->stream>>>(ctx->neq, part, d_sums);
+  FV_LAUNCHED(ctx);
+  FV_CUDA(ctx, cudaMemcpyAsync(sums, d_sums, sizeof(double) * (ctx->neq + 1), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  (void)w;
+  (void)dJdU;
+  (void)ld;
+  return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "the residual adjoint is not part of this build");
+}
+
+int fvgpu_synchronize(fvgpu_ctx *ctx) {
+  if (!ctx) return FVGPU_ERR_ARG;
+  cudaSetDevice(ctx->cfg.device);
+  return sync_and_check(ctx);
+}
+
+int fvgpu_last_error(fvgpu_ctx *ctx, int *code, int64_t *cell, char *msg, int msglen) {
+  const std::string &m = ctx ? ctx->last_msg : g_create_error;
+  if (code) *code = ctx ? ctx->last_code : 0;
+  if (cell) *cell = ctx ? ctx->last_cell : -1;
+  if (msg && msglen > 0) {
+    strncpy(msg, m.c_str(), size_t(msglen) - 1);
+    msg[msglen - 1] = 0;
+  }
+  return FVGPU_OK;
+}
+
+}  // extern "C"

@@ -159,6 +159,23 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
 int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld);
 
 /* ---- diagnostics -------------------------------------------------------- */
+/* Kernel kinds reported by fvgpu_profile_step. */
+#define FVGPU_KIND_FACEINTERP 0  /* faceinterp.c */
+#define FVGPU_KIND_GRADCALC 1    /* gradcalc.c */
+#define FVGPU_KIND_RESIDUAL 2    /* residual_faces_AMR.c (+ fused RK stage) */
+#define FVGPU_KIND_RK 3          /* RK.c */
+#define FVGPU_KIND_DT 4          /* CFL spectral radius / time step */
+#define FVGPU_KIND_MIXED_STAGE 5 /* mixed path: fused reconstruction + flux + RK stage */
+#define FVGPU_KIND_MIXED_AUX 6   /* mixed path: auxiliary kernels */
+#define FVGPU_NKINDS 8
+/* Run nsteps steps eagerly (no graph) with a CUDA event recorded on the
+ * context's stream before every kernel and after the last; ms[k] receives the
+ * summed device time of kind k and launches[k] its launch count (arrays of
+ * FVGPU_NKINDS).  Same arguments and results as fvgpu_step. */
+int fvgpu_profile_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps, double *ms,
+                       int *launches);
+/* The CUDA stream (cudaStream_t) all of the context's work is queued on. */
+int fvgpu_get_stream(fvgpu_ctx *ctx, void **stream);
 /* Error of the last failing call: code, offending cell (-1 if none) and text. */
 int fvgpu_last_error(fvgpu_ctx *ctx, int *code, int64_t *cell, char *msg, int msglen);
 /* Number of conserved variables of the configured model (5 or 4). */

@@ -52,7 +52,8 @@ def build_oracle() -> str:
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "liboracle.so")
     src = os.path.join(HERE, "fvoracle.c")
-    _run(["gcc", *CFLAGS, "-shared", "-I", os.path.join(REPO, "include"), src, "-o", out, "-lm"])
+    _run(["gcc", *CFLAGS, "-fopenmp", "-shared", "-I", os.path.join(REPO, "include"), src, "-o", out,
+          "-lm"])
     return out
 
 

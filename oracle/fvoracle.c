@@ -39,11 +39,27 @@ static const int kOpp[6] = {2, 3, 0, 1, 5, 4}; /* fcopp, operatetp.c:481-490 */
 static int64_t g_err_cell = -1;
 static int g_err_code = 0;
 static void set_err(int code, int64_t cell) {
-  if (g_err_code == 0) {
-    g_err_code = code;
-    g_err_cell = cell;
+#pragma omp critical(fvo_err)
+  {
+    if (g_err_code == 0) {
+      g_err_code = code;
+      g_err_cell = cell;
+    }
   }
 }
+
+/* Cells are independent in every per-cell loop below, so running them on
+ * several threads gives the same bits as one thread. */
+#ifdef _OPENMP
+#include <omp.h>
+void fvo_set_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+}
+int fvo_get_threads(void) { return omp_get_max_threads(); }
+#else
+void fvo_set_threads(int n) { (void)n; }
+int fvo_get_threads(void) { return 1; }
+#endif
 int fvo_error(int64_t *cell) {
   if (cell) *cell = g_err_cell;
   return g_err_code;
@@ -378,6 +394,7 @@ static void delta_values(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const
 void fvo_faceinterp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U, double *SF) {
   const int neq = neq_of(cfg);
   const int64_t n = m->ncells;
+#pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < n; ++c) {
     double own[NEQMAX];
     load_cell(U, neq, n, c, own);
@@ -417,6 +434,7 @@ void fvo_faceinterp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const doub
 void fvo_gradcalc(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U, double *SG) {
   const int neq = neq_of(cfg);
   const int64_t n = m->ncells;
+#pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < n; ++c) {
     double g[NEQMAX + 1][3];
     for (int iv = 0; iv <= neq; ++iv) g[iv][0] = g[iv][1] = g[iv][2] = 0.0;
@@ -481,6 +499,7 @@ void fvo_rhs_nb(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *
   const int neq = neq_of(cfg);
   const int64_t n = m->ncells;
   const int muscl = cfg->ischeme == 2;
+#pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < n; ++c) {
     if (inner && inner[c] != inner_outer) continue;
     double rhs[NEQMAX];
@@ -555,6 +574,7 @@ void fvo_rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U, 
 void fvo_rk(int irk, double dt, int neq, const fvgpu_mesh_soa *m, double *S, double *SN,
             const double *RHS) {
   const int64_t n = m->ncells;
+#pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < n; ++c) {
     const double Vol = m->vol[c];
     for (int e = 0; e < neq; ++e) {

@@ -204,6 +204,8 @@ class Oracle:
             L.fvo_error.argtypes = [C.POINTER(C.c_int64)]
             L.fvo_error.restype = C.c_int
             L.fvo_clear_error.argtypes = []
+            L.fvo_set_threads.argtypes = [C.c_int]
+            L.fvo_get_threads.restype = C.c_int
             cls._lib = L
         return cls._lib
 
@@ -221,6 +223,14 @@ class Oracle:
 
     def _c(self):
         return C.byref(self.ccfg)
+
+    @classmethod
+    def set_threads(cls, n: int):
+        cls.lib().fvo_set_threads(int(n))
+
+    @classmethod
+    def threads(cls) -> int:
+        return cls.lib().fvo_get_threads()
 
     def error(self):
         cell = C.c_int64()
