@@ -44,10 +44,12 @@ struct DevBuf {
 
 struct GraphKey {
   int scheme, cfl, precision;
+  const void *state;  // the graph bakes in the state buffer (mixed steps alternate two)
   bool operator<(const GraphKey &o) const {
     if (scheme != o.scheme) return scheme < o.scheme;
     if (cfl != o.cfl) return cfl < o.cfl;
-    return precision < o.precision;
+    if (precision != o.precision) return precision < o.precision;
+    return state < o.state;
   }
 };
 
@@ -81,6 +83,8 @@ struct fvgpu_ctx {
   bool has_inner = false;
   // mixed-precision path resources
   fv::MixedResources mixed;
+  bool mixed_ok = false;
+  std::string mixed_why;
   fv::LaunchMarks marks;
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, int> graph_launches;  // kernels per captured step
@@ -450,13 +454,20 @@ int enqueue_step_fp64(fvgpu_ctx *ctx, int scheme, bool cfl_mode) {
 }
 
 int enqueue_step(fvgpu_ctx *ctx, int scheme, bool cfl_mode) {
-  if (ctx->cfg.precision == FVGPU_MIXED)
-    return fv::enqueue_step_mixed(ctx->mixed, ctx->ph, ctx->view(), scheme, cfl_mode, ctx->S.as<double>(),
-                                  ctx->SN.as<double>(), ctx->d_dt(), ctx->d_lambda(), &ctx->d_scal()->cfl,
-                                  ctx->d_err(), ctx->marks, ctx->stream) == cudaSuccess
-               ? FVGPU_OK
-               : set_err(ctx, FVGPU_ERR_CUDA, "mixed step launch: %s", cudaGetErrorString(cudaGetLastError()));
+  if (ctx->cfg.precision == FVGPU_MIXED) {
+    const cudaError_t e = fv::enqueue_step_mixed(ctx->mixed, ctx->ph, ctx->view(), scheme, cfl_mode,
+                                                 ctx->S.as<double>(), fv::mixed_alt_state(ctx->mixed), ctx->d_dt(),
+                                                 ctx->d_lambda(), &ctx->d_scal()->cfl, ctx->d_err(), ctx->marks,
+                                                 ctx->stream);
+    return e == cudaSuccess ? FVGPU_OK : set_err(ctx, FVGPU_ERR_CUDA, "mixed step launch: %s", cudaGetErrorString(e));
+  }
   return enqueue_step_fp64(ctx, scheme, cfl_mode);
+}
+
+// after a step has been queued: the mixed path wrote the new state into the
+// second buffer, which becomes the current state
+void after_step(fvgpu_ctx *ctx) {
+  if (ctx->cfg.precision == FVGPU_MIXED) fv::mixed_swap_state(ctx->mixed, ctx->S.p);
 }
 
 int ensure_lambda(fvgpu_ctx *ctx) {
@@ -534,11 +545,11 @@ int fvgpu_set_precision(fvgpu_ctx *ctx, int precision) {
     return set_err(ctx, FVGPU_ERR_ARG, "precision must be FVGPU_FP64 or FVGPU_MIXED");
   if (precision == ctx->cfg.precision) return FVGPU_OK;
   cudaSetDevice(ctx->cfg.device);
-  if (precision == FVGPU_MIXED && ctx->has_mesh) {
+  if (precision == FVGPU_MIXED) {
     char why[256];
     if (!fv::mixed_supported(ctx->ph, why, sizeof why)) return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
-    if (fv::prepare_mixed(ctx->mixed, ctx->ph, ctx->view(), ctx->level.as<int32_t>(), ctx->stream) != cudaSuccess)
-      return set_err(ctx, FVGPU_ERR_CUDA, "mixed-path setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (ctx->has_mesh && !ctx->mixed_ok)
+      return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", ctx->mixed_why.c_str());
   }
   ctx->cfg.precision = precision;
   ctx->drop_graphs();
@@ -588,11 +599,12 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   ctx->nhang = nh;
   ctx->ph = make_phys(ctx->cfg, neq, m->frames);
   ctx->lambda_valid = false;
-  if (ctx->cfg.precision == FVGPU_MIXED) {
-    char why[256];
-    if (!fv::mixed_supported(ctx->ph, why, sizeof why)) return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
-    if (fv::prepare_mixed(ctx->mixed, ctx->ph, ctx->view(), ctx->level.as<int32_t>(), ctx->stream) != cudaSuccess)
-      return set_err(ctx, FVGPU_ERR_CUDA, "mixed-path setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+  {
+    char why[256] = {0};
+    ctx->mixed_ok = fv::mixed_prepare_host(ctx->mixed, ctx->ph, m, why, sizeof why) == FVGPU_OK;
+    ctx->mixed_why = why;
+    if (ctx->cfg.precision == FVGPU_MIXED && !ctx->mixed_ok)
+      return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
   }
   FV_CUDA(ctx, cudaDeviceSynchronize());
   ctx->has_mesh = true;
@@ -735,7 +747,8 @@ int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps) {
     k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
   }
   FV_LAUNCHED(ctx);
-  const GraphKey key{scheme, cfl_mode ? 1 : 0, ctx->cfg.precision};
+  for (int s = 0; s < nsteps; ++s) {
+  const GraphKey key{scheme, cfl_mode ? 1 : 0, ctx->cfg.precision, ctx->S.p};
   auto it = ctx->graphs.find(key);
   if (it == ctx->graphs.end()) {
     cudaGraph_t g = nullptr;
@@ -758,7 +771,9 @@ int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps) {
     if (ce != cudaSuccess) return set_err(ctx, FVGPU_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
     it = ctx->graphs.emplace(key, ge).first;
   }
-  for (int s = 0; s < nsteps; ++s) FV_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+  FV_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+  after_step(ctx);
+  }
   if (!cfl_mode) ctx->lambda_valid = false;
   return FVGPU_OK;
 }
@@ -791,7 +806,10 @@ int fvgpu_profile_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int ns
   mk.kinds = kinds.data();
   mk.capacity = cap - 1;
   mk.used = 0;
-  for (int s = 0; s < nsteps && rc == 0; ++s) rc = enqueue_step(ctx, scheme, cfl_mode);
+  for (int s = 0; s < nsteps && rc == 0; ++s) {
+    rc = enqueue_step(ctx, scheme, cfl_mode);
+    if (!rc) after_step(ctx);
+  }
   const int used = mk.used;
   cudaEventRecord(ev[size_t(used)], ctx->stream);
   mk.active = false;

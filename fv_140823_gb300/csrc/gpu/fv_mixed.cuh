@@ -6,22 +6,34 @@
 #include <stdint.h>
 
 #include "fv_kernels.cuh"
+#include "fvgpu.h"
 
 namespace fv {
 
-// Device resources the mixed path derives from the mesh at upload time.
+// Device resources the mixed path derives from the mesh at upload time:
+// packed per-cell geometry codes, per-level geometry tables, the two FP32
+// stage increments and the second FP64 state buffer (ping-pong).
 struct MixedResources {
   void *buf[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t n = 0;
   bool ready = false;
 };
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen);
-cudaError_t prepare_mixed(MixedResources &r, const Phys &ph, const MeshView &m, const int32_t *level,
-                          cudaStream_t st);
+// Builds the mixed-path tables from the host mesh; FVGPU_OK or an error code
+// with the reason in `why`.
+int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen);
 void release_mixed(MixedResources &r);
+// the second FP64 state buffer (steps write into it; the caller swaps)
+double *mixed_alt_state(MixedResources &r);
+// exchange the caller's state buffer with the second buffer after a step
+void mixed_swap_state(MixedResources &r, void *&state);
+cudaError_t enqueue_mixed_lambda(MixedResources &r, const Phys &ph, const MeshView &m, const double *S,
+                                 double *lambda, LaunchMarks &marks, cudaStream_t st);
+// One RK step from FP64 state `in` to `out` (distinct buffers).
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
-                               double *S, double *SN, double *dt, double *lambda, const double *cfl,
+                               const double *in, double *out, double *dt, double *lambda, const double *cfl,
                                unsigned long long *err, LaunchMarks &marks, cudaStream_t st);
 
 }  // namespace fv

@@ -1,0 +1,120 @@
+"""FP32-mixed path against the FP64 path (which is bit-identical to the
+reference).  Tolerance: relative L2 error per conserved field <= 1e-6 after
+the stated number of steps on smooth flows; discontinuous flows (Sod, the
+bubble) are held to 1e-5 because FP32 rounding can flip a minmod branch at a
+shock, which moves that cell's face value by a limiter-sized amount."""
+import numpy as np
+import pytest
+
+from fv_140823_gb300 import abi, cases
+from fv_140823_gb300.abi import SolverConfig
+
+pytestmark = pytest.mark.gpu
+
+
+def solver(t, cfg):
+    from fv_140823_gb300.solver import Solver
+    return Solver(t, cfg)
+
+
+def rel_l2(a, b):
+    return np.array([np.linalg.norm(a[v] - b[v]) / max(np.linalg.norm(b[v]), 1e-300) for v in range(a.shape[0])])
+
+
+def run(case, precision, nsteps, dt):
+    cfg = SolverConfig(**{**case.cfg.__dict__, "precision": precision})
+    with solver(case.tables, cfg) as s:
+        s.set_state(case.U)
+        s.step(case.scheme, dt=dt, nsteps=nsteps)
+        return s.state()
+
+
+def fixed_dt(case):
+    cfg = SolverConfig(**{**case.cfg.__dict__, "precision": abi.FP64})
+    with solver(case.tables, cfg) as s:
+        s.set_state(case.U)
+        return s.compute_dt(case.cfl)
+
+
+@pytest.mark.parametrize("level,nsteps", [(5, 50), (6, 20)])
+def test_periodic_smooth_flow_within_1e6(level, nsteps):
+    c = cases.periodic(level=level)
+    dt = fixed_dt(c)
+    a = run(c, abi.MIXED, nsteps, dt)
+    b = run(c, abi.FP64, nsteps, dt)
+    err = rel_l2(a, b)
+    assert np.all(err <= 1e-6), err
+
+
+def test_sod_within_1e5():
+    c = cases.sod(level=5)
+    dt = fixed_dt(c)
+    err = rel_l2(run(c, abi.MIXED, 20, dt), run(c, abi.FP64, 20, dt))
+    # momentum components normal to the tube stay exactly zero in both paths
+    assert err[0] <= 1e-5 and err[1] <= 1e-5 and err[4] <= 1e-5, err
+
+
+@pytest.mark.parametrize("scheme", ["euler", "ssprk2", "ssprk3"])
+def test_amr_bump_all_schemes(scheme):
+    c = cases.bump(base_level=4, extra_levels=2)
+    c.scheme = scheme
+    dt = fixed_dt(c)
+    err = rel_l2(run(c, abi.MIXED, 10, dt), run(c, abi.FP64, 10, dt))
+    assert np.all(err[[0, 1, 4]] <= 1e-6), err
+
+
+def test_mixture_bubble_model3():
+    c = cases.bubble(base_level=3, extra_levels=2)
+    dt = 2e-7
+    err = rel_l2(run(c, abi.MIXED, 5, dt), run(c, abi.FP64, 5, dt))
+    assert err[0] <= 1e-5 and err[4] <= 1e-5, err
+
+
+def test_mixed_conserves_and_is_deterministic():
+    c = cases.periodic(level=5)
+    cfg = SolverConfig(**{**c.cfg.__dict__, "precision": abi.MIXED})
+    outs = []
+    for _ in range(2):
+        with solver(c.tables, cfg) as s:
+            s.set_state(c.U)
+            before = s.conservation()
+            s.step("ssprk3", cfl=0.5, nsteps=7)
+            after = s.conservation()
+            outs.append(s.state())
+        drift = np.abs(after - before)[[0, 4]] / np.abs(before[[0, 4]])
+        assert np.all(drift <= 1e-9), drift
+    assert np.array_equal(outs[0].view(np.int64), outs[1].view(np.int64))
+
+
+def test_mixed_cfl_dt_tracks_fp64():
+    c = cases.periodic(level=5)
+    dts = {}
+    for prec in (abi.MIXED, abi.FP64):
+        cfg = SolverConfig(**{**c.cfg.__dict__, "precision": prec})
+        with solver(c.tables, cfg) as s:
+            s.set_state(c.U)
+            s.step("ssprk3", cfl=0.5, nsteps=5)
+            dts[prec] = s.compute_dt(0.5)
+    assert abs(dts[abi.MIXED] - dts[abi.FP64]) <= 1e-6 * dts[abi.FP64]
+
+
+def test_precision_switch_keeps_state():
+    c = cases.periodic(level=4)
+    with solver(c.tables, SolverConfig(**{**c.cfg.__dict__, "precision": abi.FP64})) as s:
+        s.set_state(c.U)
+        s.set_precision(abi.MIXED)
+        s.step("ssprk3", cfl=0.5, nsteps=3)   # odd count: the state ends in the second buffer
+        s.set_precision(abi.FP64)
+        s.step("ssprk3", cfl=0.5, nsteps=1)
+        S = s.state()
+    assert np.all(np.isfinite(S))
+    ref = run(c, abi.FP64, 0, 1.0)
+    assert np.array_equal(ref, c.U)
+
+
+def test_mixed_rejects_viscous():
+    from fv_140823_gb300.solver import FvGpuError
+    c = cases.tgv(base_level=3, extra_levels=1)
+    with pytest.raises(FvGpuError) as ei:
+        solver(c.tables, SolverConfig(**{**c.cfg.__dict__, "precision": abi.MIXED}))
+    assert ei.value.code == abi.ERR_UNSUPPORTED
