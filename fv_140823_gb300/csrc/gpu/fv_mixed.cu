@@ -54,7 +54,8 @@ struct GeoTables {
   float face[kGeoEntries * kGeoStride];
   float sub_area[(kMaxLevel + 1) * 6];
   float vol[kMaxLevel + 1];
-  double inv_vol[kMaxLevel + 1];
+  float inv_vol[kMaxLevel + 1];
+  float inv2vol[kMaxLevel + 1];  // 1 / (2 V): CFL radius
 };
 
 __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return ((level * 6 + f) * 4 + rel); }
@@ -62,6 +63,16 @@ __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return 
 // + faces: normals +x (1), +y (2), +z (5); their slot in the flux table
 __host__ __device__ constexpr bool is_plus_face(int f) { return f == 1 || f == 2 || f == 5; }
 __device__ __forceinline__ int plus_slot(int f) { return f == 1 ? 0 : (f == 2 ? 1 : 2); }
+
+// FP32 constants of the mixed path, converted once on the host (FP64 -> FP32
+// conversions inside the kernel would run on GB300's slow FP64 pipe).
+struct MixedConst {
+  float fr[54];      // face frames n, t1, t2 per face index
+  float gamma, pinf, gm1, gpinf;
+  float ylo, yhi;    // mass-fraction clip (facercnstr.c:43-44)
+  float inflow[kNeqMax];
+  int model, neq, ischeme, pad;
+};
 
 struct StageArgs {
   int64_t n;
@@ -93,7 +104,7 @@ struct FS {
   float q[kNeqMax];
 };
 
-__device__ __forceinline__ bool mixed_face_state(const Phys &ph, const float *q, bool clip, FS &s) {
+__device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
   s.r = q[0];
   const float rinv = __frcp_rn(s.r);
   s.u = q[1] * rinv;
@@ -101,22 +112,20 @@ __device__ __forceinline__ bool mixed_face_state(const Phys &ph, const float *q,
   s.w = q[3] * rinv;
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) s.q[v] = q[v];
-  if (ph.model == 1) {
-    const float g = float(ph.gamma), pinf = float(ph.pinf);
+  if (mc.model == 1) {
     s.e = q[4];
     const float ke = fmaf(s.w, s.w, fmaf(s.v, s.v, s.u * s.u));
     const float e_int = fmaf(-0.5f, ke, s.e * rinv);
-    s.p = fmaf(s.r * (g - 1.0f), e_int, -g * pinf);
-    s.c = __fsqrt_rn(g * (s.p + pinf) * rinv);
+    s.p = fmaf(s.r * mc.gm1, e_int, -mc.gpinf);
+    s.c = __fsqrt_rn(mc.gamma * (s.p + mc.pinf) * rinv);
     s.y = 0.0f;
     return true;
   }
   // model 3: mass fraction in FP32, pressure inversion in FP64
   s.y = q[4] * rinv;
   if (clip) {
-    const float lo = float(ph.ymin / 1000.0), hi = float(1.0 - ph.ymin / 1000.0);
-    s.y = s.y < lo ? lo : s.y;
-    s.y = s.y > hi ? hi : s.y;
+    s.y = s.y < mc.ylo ? mc.ylo : s.y;
+    s.y = s.y > mc.yhi ? mc.yhi : s.y;
   }
   double p, c;
   const bool ok = eos_mixture(double(s.r), double(s.y), p, c);
@@ -129,12 +138,12 @@ __device__ __forceinline__ bool mixed_face_state(const Phys &ph, const float *q,
 // Normal flux through a face with unit normal n (frame f): HLLC of
 // hllc_euler.c / compute_wave_speeds.c / star_region_euler.c, contracted
 // with n as residual_faces_AMR.c:145-149 does (F.n + F_HLLC).
-__device__ __forceinline__ bool mixed_hllc_normal(const Phys &ph, int f, int bc, const FS &L, const FS &R,
+__device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, int bc, const FS &L, const FS &R,
                                                   float out[kNeqMax]) {
-  const double *fr = ph.frames + 9 * f;
-  const float nx = float(fr[0]), ny = float(fr[1]), nz = float(fr[2]);
-  const float mx = float(fr[3]), my = float(fr[4]), mz = float(fr[5]);
-  const float lx = float(fr[6]), ly = float(fr[7]), lz = float(fr[8]);
+  const float *fr = mc.fr + 9 * f;
+  const float nx = fr[0], ny = fr[1], nz = fr[2];
+  const float mx = fr[3], my = fr[4], mz = fr[5];
+  const float lx = fr[6], ly = fr[7], lz = fr[8];
   const float uL = fmaf(L.w, nz, fmaf(L.v, ny, L.u * nx));
   const float vL = fmaf(L.w, mz, fmaf(L.v, my, L.u * mx));
   const float wL = fmaf(L.w, lz, fmaf(L.v, ly, L.u * lx));
@@ -167,7 +176,7 @@ __device__ __forceinline__ bool mixed_hllc_normal(const Phys &ph, int f, int bc,
   Fn[1] = fmaf(K.p, nx, K.r * K.u * un);
   Fn[2] = fmaf(K.p, ny, K.r * K.v * un);
   Fn[3] = fmaf(K.p, nz, K.r * K.w * un);
-  if (ph.model == 1)
+  if (mc.model == 1)
     Fn[4] = (K.e + K.p) * un;
   else
     Fn[4] = K.r * K.y * un;
@@ -178,7 +187,7 @@ __device__ __forceinline__ bool mixed_hllc_normal(const Phys &ph, int f, int bc,
     const float us1 = cS * fmaf(wK, ly, fmaf(vK, my, S_S * ny));
     const float us2 = cS * fmaf(wK, lz, fmaf(vK, mz, S_S * nz));
     float us4;
-    if (ph.model == 1)
+    if (mc.model == 1)
       us4 = cS * fmaf(S_S - uK, S_S + __fdividef(K.p, K.r * dK), K.e * __frcp_rn(K.r));
     else
       us4 = cS * K.y;
@@ -195,13 +204,11 @@ __device__ __forceinline__ bool mixed_hllc_normal(const Phys &ph, int f, int bc,
 }
 
 // Boundary ghost (bc.c) from the own face state.
-__device__ __forceinline__ void mixed_ghost(const Phys &ph, int bc, int f, FS &g) {
+__device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
   if (bc == 1) {
-    float q[kNeqMax];
-    for (int v = 0; v < kNeqMax; ++v) q[v] = float(ph.inflow[v]);
-    mixed_face_state(ph, q, false, g);
+    mixed_face_state(mc, mc.inflow, false, g);
   } else if (bc == 3 || bc == 4) {
-    const float nx = float(ph.frames[9 * f]), ny = float(ph.frames[9 * f + 1]), nz = float(ph.frames[9 * f + 2]);
+    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
     if (bc == 3) {
       const float un = g.u * nx + g.v * ny + g.w * nz;
       g.u -= 2.0f * un * nx;
@@ -220,10 +227,10 @@ __device__ __forceinline__ void mixed_ghost(const Phys &ph, int bc, int f, FS &g
 
 struct Ctx {
   const StageArgs &a;
-  const Phys &ph;
+  const MixedConst &ph;
   int64_t c0;
   const float (*st)[kBlock];  // [neq][kBlock] block states
-  __device__ Ctx(const StageArgs &a_, const Phys &ph_, int64_t c0_, const float (*st_)[kBlock])
+  __device__ Ctx(const StageArgs &a_, const MixedConst &ph_, int64_t c0_, const float (*st_)[kBlock])
       : a(a_), ph(ph_), c0(c0_), st(st_) {}
   __device__ __forceinline__ bool in_block(int64_t x) const { return x >= c0 && x < c0 + kBlock; }
   // stage state of any cell: shared memory when in the block, else SN + D
@@ -312,19 +319,39 @@ struct Ctx {
   }
 };
 
-__device__ __forceinline__ void block_max_lambda_f(double lam, double *out) {
-  __shared__ double red[kBlock / 32];
-  for (int o = 16; o > 0; o >>= 1) lam = fmax(lam, __shfl_xor_sync(0xffffffffu, lam, o));
+// Block max of the per-cell FP32 CFL radius, folded into the FP64 maximum
+// with an integer atomicMax on the bit pattern (exact and order-independent).
+__device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
+  __shared__ float red[kBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lam;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double mx = red[0];
-    for (int w = 1; w < kBlock / 32; ++w) mx = fmax(mx, red[w]);
-    if (mx > 0.0 || isnan(mx)) atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(mx));
+    float mx = red[0];
+    for (int w = 1; w < kBlock / 32; ++w) mx = fmaxf(mx, red[w]);
+    const double d = double(mx);
+    if (d > 0.0 || isnan(d)) atomicMax((unsigned long long *)out, (unsigned long long)__double_as_longlong(d));
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_mixed_stage(Phys ph, StageArgs a) {
+// CFL spectral radius of one cell (definition in fvgpu.h), FP32.
+__device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTables *geo, int32_t g,
+                                               const float q[kNeqMax]) {
+  const int lev = level_of(g);
+  FS s;
+  mixed_face_state(mc, q, false, s);
+  float acc = 0.0f;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    const float un = fabsf(fmaf(s.w, mc.fr[9 * f + 2], fmaf(s.v, mc.fr[9 * f + 1], s.u * mc.fr[9 * f])));
+    const int rel = rel_of(g, f);
+    const float A = rel == kRelFiner ? 4.0f * geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
+    acc = fmaf(A, un + s.c, acc);
+  }
+  return acc * geo->inv2vol[lev];
+}
+
+__global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs a) {
   __shared__ float st[kNeqMax][kBlock];
   __shared__ float sf[6][kNeqMax][kBlock];
   __shared__ float fp[3][kNeqMax][kBlock];
@@ -526,7 +553,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(Phys ph, StageArgs a) {
   }
 
   // D: RK stage in increment form, FP64 state at the last stage
-  double lam = 0.0;
+  float lam = 0.0f;
   if (active) {
     bool finite = true;
 #pragma unroll
@@ -534,7 +561,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(Phys ph, StageArgs a) {
       if (v < neq && !isfinite(R[v])) finite = false;
     if (!ok) raise_error(a.err, kErrRegion, c);
     if (!finite) raise_error(a.err, kErrNonFinite, c);
-    const float dtv = __double2float_rn(*a.dt * a.geo->inv_vol[lev]);
+    const float dtv = __double2float_rn(*a.dt) * a.geo->inv_vol[lev];
     float dn[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
@@ -555,22 +582,11 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(Phys ph, StageArgs a) {
         a.SNout[v * n + c] = snew[v];
       }
       if (a.lambda) {
-        // CFL spectral radius of the new state (FP32 per cell, FP64 max)
+        // CFL spectral radius of the new state (FP32 per cell, max folded into FP64)
         float qn[kNeqMax];
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) qn[v] = v < neq ? __double2float_rn(snew[v]) : 0.0f;
-        FS s;
-        mixed_face_state(ph, qn, false, s);
-        float acc = 0.0f;
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-          const float un = fabsf(s.u * float(ph.frames[9 * f]) + s.v * float(ph.frames[9 * f + 1]) +
-                                 s.w * float(ph.frames[9 * f + 2]));
-          const int rel = rel_of(g, f);
-          const float A = rel == kRelFiner ? 4.0f * a.geo->sub_area[lev * 6 + f] : geo_face(a.geo, lev, f, rel)[2];
-          acc += A * (un + s.c);
-        }
-        lam = double(acc) / (2.0 * double(a.geo->vol[lev]));
+        lam = cell_lambda_f(ph, a.geo, g, qn);
       }
     } else {
 #pragma unroll
@@ -582,29 +598,33 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(Phys ph, StageArgs a) {
 }
 
 // CFL radius of an FP64 state with the mixed geometry (first step).
-__global__ void __launch_bounds__(kBlock) k_mixed_lambda(Phys ph, StageArgs a) {
+__global__ void __launch_bounds__(kBlock) k_mixed_lambda(MixedConst ph, StageArgs a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
-  double lam = 0.0;
+  float lam = 0.0f;
   if (c < a.n) {
-    const int32_t g = __ldg(a.geom + c);
-    const int lev = level_of(g);
     float q[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) q[v] = v < ph.neq ? __double2float_rn(a.SN[v * a.n + c]) : 0.0f;
-    FS s;
-    mixed_face_state(ph, q, false, s);
-    float acc = 0.0f;
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      const float un = fabsf(s.u * float(ph.frames[9 * f]) + s.v * float(ph.frames[9 * f + 1]) +
-                             s.w * float(ph.frames[9 * f + 2]));
-      const int rel = rel_of(g, f);
-      const float A = rel == kRelFiner ? 4.0f * a.geo->sub_area[lev * 6 + f] : geo_face(a.geo, lev, f, rel)[2];
-      acc += A * (un + s.c);
-    }
-    lam = double(acc) / (2.0 * double(a.geo->vol[lev]));
+    lam = cell_lambda_f(ph, a.geo, __ldg(a.geom + c), q);
   }
   block_max_lambda_f(lam, a.lambda);
+}
+
+MixedConst make_const(const Phys &ph) {
+  MixedConst mc;
+  memset(&mc, 0, sizeof mc);
+  for (int i = 0; i < 54; ++i) mc.fr[i] = float(ph.frames[i]);
+  mc.gamma = float(ph.gamma);
+  mc.pinf = float(ph.pinf);
+  mc.gm1 = float(ph.gamma - 1.0);
+  mc.gpinf = float(ph.gamma * ph.pinf);
+  mc.ylo = float(ph.ymin / 1000.0);
+  mc.yhi = float(1.0 - ph.ymin / 1000.0);
+  for (int v = 0; v < kNeqMax; ++v) mc.inflow[v] = float(ph.inflow[v]);
+  mc.model = ph.model;
+  mc.neq = ph.neq;
+  mc.ischeme = ph.ischeme;
+  return mc;
 }
 
 // resource slots
@@ -671,8 +691,9 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     if (!seen_vol[lev]) {
       seen_vol[lev] = 1;
       gt.vol[lev] = float(m->vol[c]);
-      gt.inv_vol[lev] = 1.0 / m->vol[c];
-    } else if (double(gt.vol[lev]) != double(float(m->vol[c])) || gt.inv_vol[lev] != 1.0 / m->vol[c]) {
+      gt.inv_vol[lev] = float(1.0 / m->vol[c]);
+      gt.inv2vol[lev] = float(1.0 / (2.0 * m->vol[c]));
+    } else if (gt.vol[lev] != float(m->vol[c]) || gt.inv_vol[lev] != float(1.0 / m->vol[c])) {
       snprintf(why, whylen, "the mixed path needs one volume per level (cell %lld)", (long long)c);
       return FVGPU_ERR_UNSUPPORTED;
     }
@@ -781,7 +802,7 @@ cudaError_t enqueue_mixed_lambda(MixedResources &r, const Phys &ph, const MeshVi
   a.SN = S;
   a.lambda = lambda;
   marks.mark(FVGPU_KIND_DT);
-  k_mixed_lambda<<<unsigned((m.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(ph, a);
+  k_mixed_lambda<<<unsigned((m.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(make_const(ph), a);
   return cudaGetLastError();
 }
 
@@ -796,6 +817,7 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     launch_dt_from_lambda(lambda, lambda, cfl, dt, err, st);
   }
   float *D[2] = {static_cast<float *>(r.buf[kBufD1]), static_cast<float *>(r.buf[kBufD2])};
+  const MixedConst mc = make_const(ph);
   const unsigned grid = unsigned((m.n + kBlock - 1) / kBlock);
   for (int k = 0; k < nst; ++k) {
     StageArgs a = stage_args(r, m);
@@ -809,7 +831,7 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.lambda = (a.last && cfl_mode) ? lambda : nullptr;
     a.err = err;
     marks.mark(FVGPU_KIND_MIXED_STAGE);
-    k_mixed_stage<<<grid, kBlock, 0, st>>>(ph, a);
+    k_mixed_stage<<<grid, kBlock, 0, st>>>(mc, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
