@@ -467,7 +467,18 @@ int enqueue_step(fvgpu_ctx *ctx, int scheme, bool cfl_mode) {
 // after a step has been queued: the mixed path wrote the new state into the
 // second buffer, which becomes the current state
 void after_step(fvgpu_ctx *ctx) {
-  if (ctx->cfg.precision == FVGPU_MIXED) fv::mixed_swap_state(ctx->mixed, ctx->S.p);
+  if (ctx->cfg.precision == FVGPU_MIXED)
+    fv::mixed_swap_state(ctx->mixed, ctx->S.p);
+  else
+    ctx->mixed.snf_valid = false;
+}
+
+// the mixed path reads an FP32 copy of the state; rebuild it when the state
+// changed outside a mixed step
+int ensure_mixed_f32(fvgpu_ctx *ctx) {
+  if (ctx->cfg.precision != FVGPU_MIXED || ctx->mixed.snf_valid) return FVGPU_OK;
+  const cudaError_t e = fv::mixed_refresh_f32(ctx->mixed, ctx->S.as<double>(), ctx->neq, ctx->marks, ctx->stream);
+  return e == cudaSuccess ? FVGPU_OK : set_err(ctx, FVGPU_ERR_CUDA, "state copy: %s", cudaGetErrorString(e));
 }
 
 int ensure_lambda(fvgpu_ctx *ctx) {
@@ -552,6 +563,7 @@ int fvgpu_set_precision(fvgpu_ctx *ctx, int precision) {
       return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", ctx->mixed_why.c_str());
   }
   ctx->cfg.precision = precision;
+  ctx->mixed.snf_valid = false;
   ctx->drop_graphs();
   return FVGPU_OK;
 }
@@ -619,6 +631,7 @@ int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld) {
   FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->S.p, sizeof(double) * ctx->n, U, sizeof(double) * ld,
                                  sizeof(double) * ctx->n, ctx->neq, cudaMemcpyHostToDevice, ctx->stream));
   ctx->lambda_valid = false;
+  ctx->mixed.snf_valid = false;
   return FVGPU_OK;
 }
 
@@ -709,6 +722,7 @@ int fvgpu_rk(fvgpu_ctx *ctx, int irk, double dt) {
                      ctx->d_dt(), nullptr, ctx->stream);
   FV_LAUNCHED(ctx);
   ctx->lambda_valid = false;
+  ctx->mixed.snf_valid = false;
   return FVGPU_OK;
 }
 
@@ -739,6 +753,8 @@ int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps) {
   if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
   cudaSetDevice(ctx->cfg.device);
   if (nsteps == 0) return FVGPU_OK;
+  rc = ensure_mixed_f32(ctx);
+  if (rc) return rc;
   if (cfl_mode) {
     rc = ensure_lambda(ctx);
     if (rc) return rc;
@@ -787,6 +803,8 @@ int fvgpu_profile_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int ns
   const bool cfl_mode = !(dt > 0.0);
   if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
   cudaSetDevice(ctx->cfg.device);
+  rc = ensure_mixed_f32(ctx);
+  if (rc) return rc;
   if (cfl_mode) {
     rc = ensure_lambda(ctx);
     if (rc) return rc;

@@ -4,37 +4,41 @@
 //
 // Arithmetic.  Reconstruction, equation of state and HLLC fluxes run in FP32
 // (the mixture EOS pressure inversion stays FP64).  The state is kept in FP64
-// as the step-start state SN; a stage k carries only the FP32 increment
+// as the step-start state SN; a stage carries only the FP32 increment
 // D_k = S_k - SN, so the RK stage formulas of RK.c become
-//     RK(1): D1 = dt/V R(S0)                      S1 = SN + D1
-//     RK(2): D2 = 1/4 (D1 + dt/V R(S1))           S2 = 3/4 SN + 1/4 S1 + 1/4 dt/V R
-//     RK(3): D3 = 2/3 (D2 + dt/V R(S2))           S3 = 1/3 SN + 2/3 S2 + 2/3 dt/V R
-//     RK(4): D  = 1/2 (D1 + dt/V R(S1))           (SSP-RK2 second stage)
-// and the step ends with one FP64 add per variable, SN <- SN + D_last.  The
-// per-stage increments are small against the state, so their FP32 rounding
-// is ~1e-8 of the state per stage while every add into the state itself is
-// FP64.  On GB300 the FP64 pipe runs at ~1/70 of FP32; this keeps the FP64
-// work to a few operations per cell and step, which is what lets the stage
-// kernel run at the HBM limit.
+//     RK(1): D1 = dt/V R(S0)                  (S1 = SN + dt/V R)
+//     RK(2): D2 = 1/4 (D1 + dt/V R(S1))       (S2 = 3/4 SN + 1/4 S1 + 1/4 dt/V R)
+//     RK(3): D3 = 2/3 (D2 + dt/V R(S2))       (S3 = 1/3 SN + 2/3 S2 + 2/3 dt/V R)
+//     RK(4): D  = 1/2 (D1 + dt/V R(S1))       (SSP-RK2 second stage)
+// and each step ends with one FP64 add per variable, SN <- SN + D_last, plus
+// an FP32 copy SNf of the new state that the next step's stages read.  On
+// GB300 the FP64 pipe (including FP64<->FP32 conversion) runs at ~1/70 of
+// FP32, so the stages touch no FP64 value except at the last one: the
+// per-stage increments are small against the state, their FP32 rounding is
+// ~1e-8 of the state per stage, and every add into the state is FP64.
 //
 // Work decomposition.  One thread per cell, blocks of kBlock consecutive cells
-// (Morton order: an 8x8x4 brick of a uniform octree).  Phases:
-//   A  stage state S = SN + D of the block's cells into shared memory
-//   B  MUSCL/minmod face values of the thread's own 6 faces (faceinterp.c /
+// (Morton order: an 8x8x4 brick of a uniform octree).
+//   A  stage state S = SNf + D of the block's cells into shared memory
+//   B  MUSCL/minmod face values of the thread's 6 faces (faceinterp.c /
 //      reconctruct_V3.c) into shared memory
-//   C  flux of each face computed once, canonically from the face's lower
-//      cell (the one whose +x/+y/+z face it is): threads compute their own
-//      + faces and publish them in shared memory; the upper cell reads it, or
+//   C  each face flux computed once, canonically from the face's lower cell
+//      (the one whose +x/+y/+z face it is): a thread computes its own + faces
+//      and publishes them in shared memory; the upper cell reads them, or
 //      recomputes the same canonical flux bit for bit when the lower cell is
 //      in another block or the face is a 1:4 sub-face.  Equal and opposite
-//      contributions -> exactly conservative and deterministic.
-//   D  residual, RK stage update, (last stage) FP64 state and CFL radius.
+//      contributions -> conservative and deterministic.  The face loop is
+//      rolled with a single flux call site so the kernel fits the
+//      instruction cache.
+//   D  residual, RK stage update, (last stage) FP64 state, FP32 copy and CFL
+//      radius.
+// This translation unit is compiled without automatic multiply-add
+// contraction (explicit fmaf only), so every copy of an expression gives the
+// same bits, which the canonical-flux sharing relies on.
 // Geometry comes from per-level tables (octree-regular meshes): a packed
 // per-cell code (level + face relations) replaces the FP64 face tables.
 #include <cstdio>
 #include <cstring>
-#include <map>
-#include <tuple>
 #include <vector>
 
 #include "fv_mixed.cuh"
@@ -46,8 +50,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kMaxLevel = 18;
 constexpr int kRelSame = 0, kRelFiner = 1, kRelCoarser = 2, kRelBoundary = 3;
-// per (level, face, relation): dcf, 1/dcc, area, pad
-constexpr int kGeoStride = 4;
+constexpr int kGeoStride = 4;  // per (level, face, relation): dcf, 1/dcc, area, pad
 constexpr int kGeoEntries = (kMaxLevel + 1) * 6 * 4;
 
 struct GeoTables {
@@ -59,31 +62,31 @@ struct GeoTables {
 };
 
 __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return ((level * 6 + f) * 4 + rel); }
-
 // + faces: normals +x (1), +y (2), +z (5); their slot in the flux table
 __host__ __device__ constexpr bool is_plus_face(int f) { return f == 1 || f == 2 || f == 5; }
 __device__ __forceinline__ int plus_slot(int f) { return f == 1 ? 0 : (f == 2 ? 1 : 2); }
 
-// FP32 constants of the mixed path, converted once on the host (FP64 -> FP32
-// conversions inside the kernel would run on GB300's slow FP64 pipe).
+// FP32 constants, converted once on the host.
 struct MixedConst {
-  float fr[54];      // face frames n, t1, t2 per face index
+  float fr[54];  // face frames n, t1, t2 per face index
   float gamma, pinf, gm1, gpinf;
-  float ylo, yhi;    // mass-fraction clip (facercnstr.c:43-44)
+  float ylo, yhi;  // mass-fraction clip (facercnstr.c:43-44)
   float inflow[kNeqMax];
   int model, neq, ischeme, pad;
 };
 
 struct StageArgs {
-  int64_t n;
+  int n;
   const int32_t *nbr;       // [6][n]
   const int32_t *geom;      // [n]: level | rel_f << (5 + 2 f)
   const int32_t *hang_nbr;  // [nhang][4]
   const GeoTables *geo;
-  const double *SN;         // [neq][n] step-start state
+  const float *SNf;         // [neq][n] FP32 copy of the step-start state
   const float *Din;         // [neq][n] stage-input increment (null: zero)
   float *Dout;              // [neq][n]
+  const double *SN;         // [neq][n] step-start state (last stage)
   double *SNout;            // [neq][n] last stage: SN + D
+  float *SNfout;            // [neq][n] last stage: FP32 copy of SNout
   const double *dt;
   double *lambda;           // last stage: CFL radius of the new state
   int irk;
@@ -93,20 +96,22 @@ struct StageArgs {
 
 __device__ __forceinline__ int level_of(int32_t g) { return g & 31; }
 __device__ __forceinline__ int rel_of(int32_t g, int f) { return (g >> (5 + 2 * f)) & 3; }
-
 __device__ __forceinline__ const float *geo_face(const GeoTables *G, int level, int f, int rel) {
   return G->face + geo_index(level, f, rel) * kGeoStride;
 }
 
-// FP32 face state (facercnstr.c / facevalues.c with fast reciprocals).
 struct FS {
   float r, u, v, w, e, p, c, y;
   float q[kNeqMax];
 };
 
+__device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float fast_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
+
+// FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
   s.r = q[0];
-  const float rinv = __frcp_rn(s.r);
+  const float rinv = fast_rcp(s.r);
   s.u = q[1] * rinv;
   s.v = q[2] * rinv;
   s.w = q[3] * rinv;
@@ -117,7 +122,7 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
     const float ke = fmaf(s.w, s.w, fmaf(s.v, s.v, s.u * s.u));
     const float e_int = fmaf(-0.5f, ke, s.e * rinv);
     s.p = fmaf(s.r * mc.gm1, e_int, -mc.gpinf);
-    s.c = __fsqrt_rn(mc.gamma * (s.p + mc.pinf) * rinv);
+    s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
     s.y = 0.0f;
     return true;
   }
@@ -135,11 +140,33 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
   return ok;
 }
 
-// Normal flux through a face with unit normal n (frame f): HLLC of
-// hllc_euler.c / compute_wave_speeds.c / star_region_euler.c, contracted
-// with n as residual_faces_AMR.c:145-149 does (F.n + F_HLLC).
+// Boundary ghost (bc.c:19-49) from the own face state.
+__device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
+  if (bc == 1) {
+    mixed_face_state(mc, mc.inflow, false, g);
+  } else if (bc == 3 || bc == 4) {
+    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
+    if (bc == 3) {
+      const float un = fmaf(g.w, nz, fmaf(g.v, ny, g.u * nx));
+      g.u = fmaf(-2.0f * un, nx, g.u);
+      g.v = fmaf(-2.0f * un, ny, g.v);
+      g.w = fmaf(-2.0f * un, nz, g.w);
+    } else {
+      g.u = -g.u;
+      g.v = -g.v;
+      g.w = -g.w;
+    }
+    g.q[1] = g.r * g.u;
+    g.q[2] = g.r * g.v;
+    g.q[3] = g.r * g.w;
+  }
+}
+
+// Normal flux F.n + S_K (U*_K - U_K) through a face of frame f
+// (hllc_euler.c:3-55, compute_wave_speeds.c:3-88, star_region_euler.c:3-40,
+// contracted with n as residual_faces_AMR.c:145-149).
 __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, int bc, const FS &L, const FS &R,
-                                                  float out[kNeqMax]) {
+                                                  float Fn[kNeqMax]) {
   const float *fr = mc.fr + 9 * f;
   const float nx = fr[0], ny = fr[1], nz = fr[2];
   const float mx = fr[3], my = fr[4], mz = fr[5];
@@ -153,7 +180,7 @@ __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, i
   const float SR = fmaxf(uL + L.c, uR + R.c);
   const float SL = fminf(uL - L.c, uR - R.c);
   const float ruL = L.r * uL, ruR = R.r * uR;
-  const float nn = (nx * nx + ny * ny) + nz * nz;  // (R st R^T)[0][0] = p |n|^2
+  const float nn = fmaf(nz, nz, fmaf(ny, ny, nx * nx));  // (R st R^T)[0][0] = p |n|^2
   const float num = fmaf(SR, ruR, fmaf(-SL, ruL, fmaf(ruL, uL, L.p * nn) - fmaf(ruR, uR, R.p * nn)));
   const float den = fmaf(SR, R.r, fmaf(-SL, L.r, ruL - ruR));
   float S_S = __fdividef(num, den);
@@ -169,99 +196,65 @@ __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, i
   const FS &K = left ? L : R;
   const float uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
   const float SK = left ? SL : SR;
-  // physical flux F(U_K) . n
-  const float un = uK;  // u_K . n
-  float Fn[kNeqMax];
-  Fn[0] = K.r * un;
-  Fn[1] = fmaf(K.p, nx, K.r * K.u * un);
-  Fn[2] = fmaf(K.p, ny, K.r * K.v * un);
-  Fn[3] = fmaf(K.p, nz, K.r * K.w * un);
-  if (mc.model == 1)
-    Fn[4] = (K.e + K.p) * un;
-  else
-    Fn[4] = K.r * K.y * un;
+  const float run = K.r * uK;
+  Fn[0] = run;
+  Fn[1] = fmaf(K.p, nx, run * K.u);
+  Fn[2] = fmaf(K.p, ny, run * K.v);
+  Fn[3] = fmaf(K.p, nz, run * K.w);
+  Fn[4] = mc.model == 1 ? (K.e + K.p) * uK : run * K.y;
   if (star) {
     const float dK = SK - uK;
     const float cS = __fdividef(K.r * dK, SK - S_S);
     const float us0 = cS * fmaf(wK, lx, fmaf(vK, mx, S_S * nx));
     const float us1 = cS * fmaf(wK, ly, fmaf(vK, my, S_S * ny));
     const float us2 = cS * fmaf(wK, lz, fmaf(vK, mz, S_S * nz));
-    float us4;
-    if (mc.model == 1)
-      us4 = cS * fmaf(S_S - uK, S_S + __fdividef(K.p, K.r * dK), K.e * __frcp_rn(K.r));
-    else
-      us4 = cS * K.y;
+    const float us4 = mc.model == 1
+                          ? cS * fmaf(S_S - uK, S_S + __fdividef(K.p, K.r * dK), __fdividef(K.e, K.r))
+                          : cS * K.y;
     Fn[0] = fmaf(SK, cS - K.q[0], Fn[0]);
     Fn[1] = fmaf(SK, us0 - K.q[1], Fn[1]);
     Fn[2] = fmaf(SK, us1 - K.q[2], Fn[2]);
     Fn[3] = fmaf(SK, us2 - K.q[3], Fn[3]);
     Fn[4] = fmaf(SK, us4 - K.q[4], Fn[4]);
   }
-  const bool region = r1 || r2 || r3 || r4;
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) out[v] = Fn[v];
-  return ok && region;
+  return ok && (r1 || r2 || r3 || r4);
 }
 
-// Boundary ghost (bc.c) from the own face state.
-__device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
-  if (bc == 1) {
-    mixed_face_state(mc, mc.inflow, false, g);
-  } else if (bc == 3 || bc == 4) {
-    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
-    if (bc == 3) {
-      const float un = g.u * nx + g.v * ny + g.w * nz;
-      g.u -= 2.0f * un * nx;
-      g.v -= 2.0f * un * ny;
-      g.w -= 2.0f * un * nz;
-    } else {
-      g.u = -g.u;
-      g.v = -g.v;
-      g.w = -g.w;
-    }
-    g.q[1] = g.r * g.u;
-    g.q[2] = g.r * g.v;
-    g.q[3] = g.r * g.w;
-  }
-}
-
-struct Ctx {
+struct Block {
   const StageArgs &a;
-  const MixedConst &ph;
-  int64_t c0;
-  const float (*st)[kBlock];  // [neq][kBlock] block states
-  __device__ Ctx(const StageArgs &a_, const MixedConst &ph_, int64_t c0_, const float (*st_)[kBlock])
-      : a(a_), ph(ph_), c0(c0_), st(st_) {}
-  __device__ __forceinline__ bool in_block(int64_t x) const { return x >= c0 && x < c0 + kBlock; }
-  // stage state of any cell: shared memory when in the block, else SN + D
-  __device__ __forceinline__ void state(int64_t x, float q[kNeqMax]) const {
+  const MixedConst &mc;
+  int c0;
+  const float (*st)[kBlock];
+  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, const float (*st_)[kBlock])
+      : a(a_), mc(mc_), c0(c0_), st(st_) {}
+  __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(kBlock); }
+  // stage state of any cell: shared memory when in the block, else SNf + D
+  __device__ __forceinline__ void state(int x, float q[kNeqMax]) const {
     if (in_block(x)) {
-      const int t = int(x - c0);
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) q[v] = v < ph.neq ? st[v][t] : 0.0f;
+      for (int v = 0; v < kNeqMax; ++v) q[v] = st[v][x - c0];
       return;
     }
-    const int64_t n = a.n;
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      if (v < ph.neq) {
-        float s = __double2float_rn(__ldg(a.SN + v * n + x));
-        if (a.Din) s += __ldg(a.Din + v * n + x);
-        q[v] = s;
-      } else {
-        q[v] = 0.0f;
+      float s = 0.0f;
+      if (v < mc.neq) {
+        s = __ldg(a.SNf + v * a.n + x);
+        if (a.Din) s += __ldg(a.Din + v * a.n + x);
       }
+      q[v] = s;
     }
   }
-  // neighbour value seen across face f of cell x (deltavalues.c): single
-  // neighbour, mean of the 4 fine ones, or the boundary ghost
-  __device__ __forceinline__ void across(int64_t x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
+  // value across face f of cell x (deltavalues.c): single neighbour, mean of
+  // the four fine ones, or the boundary ghost
+  __device__ __forceinline__ void across(int x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
     const int32_t code = __ldg(a.nbr + f * a.n + x);
     if (code >= 0) {
       state(code, nb);
     } else if (is_hanging(code)) {
       const int32_t *k = a.hang_nbr + 4 * hang_index(code);
       float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
       for (int s = 0; s < 4; ++s) {
         float q[kNeqMax];
         state(__ldg(k + s), q);
@@ -276,36 +269,34 @@ struct Ctx {
       for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
       if (bc == 1 || bc == 3 || bc == 4) {
         FS g;
-        mixed_face_state(ph, own, false, g);
-        mixed_ghost(ph, bc, f, g);
+        mixed_face_state(mc, own, false, g);
+        mixed_ghost(mc, bc, f, g);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
       }
     }
   }
-  // MUSCL/minmod face value of face f of cell x (reconctruct_V3.c)
-  __device__ __forceinline__ void recon_face(int64_t x, int32_t gx, int f, const float qx[kNeqMax],
-                                             const float d0[kNeqMax], const float d1[kNeqMax],
-                                             float out[kNeqMax]) const {
+  // minmod face value of face f (reconctruct_V3.c:17-43) from the deltas
+  __device__ __forceinline__ void recon(int32_t gx, int f, const float qx[kNeqMax], const float d0[kNeqMax],
+                                        const float d1[kNeqMax], float out[kNeqMax]) const {
     const int lev = level_of(gx);
     const int rf = rel_of(gx, f), ro = rel_of(gx, opp_face(f));
     const float *gf = geo_face(a.geo, lev, f, rf);
-    const float dcf = gf[0], inv_dcc_p = gf[1];
-    const float inv_dcc_m = geo_face(a.geo, lev, opp_face(f), ro)[1];
+    const float dcf = gf[0], inv_p = gf[1];
+    const float inv_m = geo_face(a.geo, lev, opp_face(f), ro)[1];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
       float grad = 0.0f;
       if (rf != kRelBoundary && fabsf(d0[v]) > 1e-10f) {
-        const float sp = d0[v] * inv_dcc_p;
-        const float sm = -d1[v] * inv_dcc_m;
+        const float sp = d0[v] * inv_p;
+        const float sm = -d1[v] * inv_m;
         if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
       }
       out[v] = fmaf(dcf, grad, qx[v]);
     }
-    (void)x;
   }
-  // face value of face f of a cell outside the thread's own work (any cell)
-  __device__ __forceinline__ void recon_any(int64_t x, int f, float out[kNeqMax]) const {
+  // face value of face f of any cell (used across block edges)
+  __device__ __forceinline__ void recon_any(int x, int f, float out[kNeqMax]) const {
     float qx[kNeqMax], nbp[kNeqMax], nbm[kNeqMax], d0[kNeqMax], d1[kNeqMax];
     state(x, qx);
     across(x, f, qx, nbp);
@@ -315,12 +306,10 @@ struct Ctx {
       d0[v] = nbp[v] - qx[v];
       d1[v] = nbm[v] - qx[v];
     }
-    recon_face(x, __ldg(a.geom + x), f, qx, d0, d1, out);
+    recon(__ldg(a.geom + x), f, qx, d0, d1, out);
   }
 };
 
-// Block max of the per-cell FP32 CFL radius, folded into the FP64 maximum
-// with an integer atomicMax on the bit pattern (exact and order-independent).
 __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
   __shared__ float red[kBlock / 32];
   for (int o = 16; o > 0; o >>= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o));
@@ -351,44 +340,38 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
   return acc * geo->inv2vol[lev];
 }
 
-__global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs a) {
+__global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs a) {
   __shared__ float st[kNeqMax][kBlock];
   __shared__ float sf[6][kNeqMax][kBlock];
   __shared__ float fp[3][kNeqMax][kBlock];
+  __shared__ float s_dt;
   const int t = threadIdx.x;
-  const int64_t c0 = int64_t(blockIdx.x) * kBlock;
-  const int64_t c = c0 + t;
-  const int64_t n = a.n;
+  const int c0 = int(blockIdx.x) * kBlock;
+  const int c = c0 + t;
+  const int n = a.n;
   const bool active = c < n;
-  const int neq = ph.neq;
-  const bool muscl = ph.ischeme == 2;
-  Ctx cx(a, ph, c0, st);
+  const int neq = mc.neq;
+  const bool muscl = mc.ischeme == 2;
+  Block blk(a, mc, c0, st);
 
   // A: own stage state
-  double sn[kNeqMax];
   float din[kNeqMax], q[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
-    sn[v] = 0.0;
     din[v] = 0.0f;
     q[v] = 0.0f;
     if (active && v < neq) {
-      sn[v] = __ldg(a.SN + v * n + c);
       din[v] = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-      q[v] = __double2float_rn(sn[v]) + din[v];
+      q[v] = __ldg(a.SNf + v * n + c) + din[v];
     }
     st[v][t] = q[v];
   }
   int32_t nb[6];
   int32_t g = 0;
-  if (active) {
-    g = __ldg(a.geom + c);
 #pragma unroll
-    for (int f = 0; f < 6; ++f) nb[f] = __ldg(a.nbr + f * n + c);
-  } else {
-#pragma unroll
-    for (int f = 0; f < 6; ++f) nb[f] = -3;
-  }
+  for (int f = 0; f < 6; ++f) nb[f] = active ? __ldg(a.nbr + f * n + c) : -3;
+  if (active) g = __ldg(a.geom + c);
+  if (t == 0) s_dt = __double2float_rn(*a.dt);
   __syncthreads();
 
   // B: own face values
@@ -398,14 +381,14 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         float nbv[kNeqMax];
-        cx.across(c, f, q, nbv);
+        blk.across(c, f, q, nbv);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) dl[f][v] = nbv[v] - q[v];
       }
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         float o[kNeqMax];
-        cx.recon_face(c, g, f, q, dl[f], dl[opp_face(f)], o);
+        blk.recon(g, f, q, dl[f], dl[opp_face(f)], o);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = o[v];
       }
@@ -418,141 +401,82 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs
   }
   __syncthreads();
 
-  // face value of face f of cell x: shared memory when in the block
-  auto face_value = [&](int64_t x, int f, float out[kNeqMax]) {
-    if (cx.in_block(x)) {
-      const int tx = int(x - c0);
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) out[v] = sf[f][v][tx];
-    } else if (muscl) {
-      cx.recon_any(x, f, out);
-    } else {
-      cx.state(x, out);
-    }
-  };
-
-  // C: fluxes
+  // C: fluxes.  Order: + faces 1, 2, 5 (publish), barrier, - faces 3, 0, 4.
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   bool ok = true;
   const int lev = level_of(g);
-  if (active) {
-    // + faces: canonical lower cell is this one
+#pragma unroll 1
+  for (int it = 0; it < 6; ++it) {
+    if (it == 3) __syncthreads();
+    if (!active) continue;
+    const int f = it == 0 ? 1 : it == 1 ? 2 : it == 2 ? 5 : it == 3 ? 3 : it == 4 ? 0 : 4;
+    const bool plus = it < 3;
+    const int fo = opp_face(f);
+    const int32_t code = nb[f];
+    const bool boundary = is_boundary(code);
+    const bool hanging = is_hanging(code);
+    const int rel = rel_of(g, f);
+    const int nsub = hanging ? 4 : 1;
+    const int32_t *hk = hanging ? a.hang_nbr + 4 * hang_index(code) : nullptr;
+    const float A = hanging ? a.geo->sub_area[lev * 6 + f] : geo_face(a.geo, lev, f, rel)[2];
+#pragma unroll 1
+    for (int s = 0; s < nsub; ++s) {
+      const int other = boundary ? -1 : (hanging ? __ldg(hk + s) : code);
+      float Fn[kNeqMax];
+      // the - side reads a published flux when the lower cell is in the block
+      // and its + face carries a single neighbour (this cell)
+      const bool published = !plus && !boundary && (hanging || rel == kRelSame) && blk.in_block(other);
+      if (published) {
+        const int tl = other - c0;
 #pragma unroll
-    for (int f = 1; f < 6; ++f) {
-      if (!is_plus_face(f)) continue;
-      const int32_t code = nb[f];
-      float own[kNeqMax];
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) own[v] = sf[f][v][t];
-      FS L;
-      ok &= mixed_face_state(ph, own, muscl, L);
-      if (code >= 0 || is_boundary(code)) {
-        FS Rs;
-        int bc = 0;
-        if (code >= 0) {
-          float other[kNeqMax];
-          face_value(code, opp_face(f), other);
-          ok &= mixed_face_state(ph, other, muscl, Rs);
-        } else {
-          bc = -1 - code;
-          Rs = L;
-          mixed_ghost(ph, bc, f, Rs);
-        }
-        float Fn[kNeqMax];
-        ok &= mixed_hllc_normal(ph, f, bc, L, Rs, Fn);
-        const float A = geo_face(a.geo, lev, f, rel_of(g, f))[2];
+        for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
+      } else {
+        float own[kNeqMax], oth[kNeqMax];
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) {
-          if (code >= 0) fp[plus_slot(f)][v][t] = Fn[v];
-          R[v] -= A * Fn[v];
+          own[v] = sf[f][v][t];
+          oth[v] = own[v];
         }
-      } else {  // 1:4 face: four sub-faces
-        const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-        const float As = a.geo->sub_area[lev * 6 + f];
-        for (int s = 0; s < 4; ++s) {
-          float other[kNeqMax];
-          face_value(__ldg(k + s), opp_face(f), other);
-          FS Rs;
-          ok &= mixed_face_state(ph, other, muscl, Rs);
-          float Fn[kNeqMax];
-          ok &= mixed_hllc_normal(ph, f, 0, L, Rs, Fn);
+        if (!boundary) {
+          if (blk.in_block(other)) {
 #pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) R[v] -= As * Fn[v];
-        }
-      }
-    }
-  }
-  __syncthreads();
-  if (active) {
-    // - faces: canonical lower cell is the neighbour (or this cell at a boundary)
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      if (is_plus_face(f)) continue;
-      const int32_t code = nb[f];
-      const int fo = opp_face(f);
-      float own[kNeqMax];
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) own[v] = sf[f][v][t];
-      if (is_boundary(code)) {
-        FS Ls, Rs;
-        ok &= mixed_face_state(ph, own, muscl, Ls);
-        const int bc = -1 - code;
-        Rs = Ls;
-        mixed_ghost(ph, bc, f, Rs);
-        float Fn[kNeqMax];
-        ok &= mixed_hllc_normal(ph, f, bc, Ls, Rs, Fn);
-        const float A = geo_face(a.geo, lev, f, kRelBoundary)[2];
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) R[v] -= A * Fn[v];
-        continue;
-      }
-      const int rel = rel_of(g, f);
-      if (code >= 0) {
-        float Fn[kNeqMax];
-        if (rel == kRelSame && cx.in_block(code)) {
-          const int tl = int(code - c0);
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
-        } else {
-          // neighbour in another block, or coarser (its + face is a 1:4 face):
-          // recompute the neighbour's canonical flux
-          float lowv[kNeqMax];
-          face_value(code, fo, lowv);
-          FS Ls, Rs;
-          ok &= mixed_face_state(ph, lowv, muscl, Ls);
-          ok &= mixed_face_state(ph, own, muscl, Rs);
-          ok &= mixed_hllc_normal(ph, fo, 0, Ls, Rs, Fn);
-        }
-        const float A = geo_face(a.geo, lev, f, rel)[2];
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) R[v] += A * Fn[v];
-      } else {  // this cell is the coarse side of a 1:4 face on its - side
-        const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-        const float As = a.geo->sub_area[lev * 6 + f];
-        FS Rs;
-        ok &= mixed_face_state(ph, own, muscl, Rs);
-        for (int s = 0; s < 4; ++s) {
-          const int64_t ks = __ldg(k + s);
-          float Fn[kNeqMax];
-          if (cx.in_block(ks)) {
-            const int tl = int(ks - c0);
-#pragma unroll
-            for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
+            for (int v = 0; v < kNeqMax; ++v) oth[v] = sf[fo][v][other - c0];
+          } else if (muscl) {
+            blk.recon_any(other, fo, oth);
           } else {
-            float lowv[kNeqMax];
-            face_value(ks, fo, lowv);
-            FS Ls;
-            ok &= mixed_face_state(ph, lowv, muscl, Ls);
-            ok &= mixed_hllc_normal(ph, fo, 0, Ls, Rs, Fn);
+            blk.state(other, oth);
           }
+        }
+        // canonical orientation: lower side first, frame of the lower cell's + face
+        const bool own_low = plus || boundary;
+        float lo[kNeqMax], hi[kNeqMax];
 #pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) R[v] += As * Fn[v];
+        for (int v = 0; v < kNeqMax; ++v) {
+          lo[v] = own_low ? own[v] : oth[v];
+          hi[v] = own_low ? oth[v] : own[v];
+        }
+        FS Ls, Rs;
+        ok &= mixed_face_state(mc, lo, muscl, Ls);
+        const int bc = boundary ? -1 - code : 0;
+        if (boundary) {
+          Rs = Ls;
+          mixed_ghost(mc, bc, f, Rs);
+        } else {
+          ok &= mixed_face_state(mc, hi, muscl, Rs);
+        }
+        ok &= mixed_hllc_normal(mc, own_low ? f : fo, bc, Ls, Rs, Fn);
+        if (plus && !boundary && !hanging) {
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
         }
       }
+      const float sA = (plus || boundary) ? -A : A;
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, Fn[v], R[v]);
     }
   }
 
-  // D: RK stage in increment form, FP64 state at the last stage
+  // D: RK stage in increment form; FP64 state and FP32 copy at the last stage
   float lam = 0.0f;
   if (active) {
     bool finite = true;
@@ -561,7 +485,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs
       if (v < neq && !isfinite(R[v])) finite = false;
     if (!ok) raise_error(a.err, kErrRegion, c);
     if (!finite) raise_error(a.err, kErrNonFinite, c);
-    const float dtv = __double2float_rn(*a.dt) * a.geo->inv_vol[lev];
+    const float dtv = s_dt * a.geo->inv_vol[lev];
     float dn[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
@@ -574,20 +498,16 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs
       }
     }
     if (a.last) {
-      double snew[kNeqMax];
+      float qn[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) {
         if (v >= neq) break;
-        snew[v] = sn[v] + double(dn[v]);
-        a.SNout[v * n + c] = snew[v];
+        const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
+        a.SNout[v * n + c] = snew;
+        qn[v] = __double2float_rn(snew);
+        a.SNfout[v * n + c] = qn[v];
       }
-      if (a.lambda) {
-        // CFL spectral radius of the new state (FP32 per cell, max folded into FP64)
-        float qn[kNeqMax];
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) qn[v] = v < neq ? __double2float_rn(snew[v]) : 0.0f;
-        lam = cell_lambda_f(ph, a.geo, g, qn);
-      }
+      if (a.lambda) lam = cell_lambda_f(mc, a.geo, g, qn);
     } else {
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v)
@@ -597,17 +517,10 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst ph, StageArgs
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
-// CFL radius of an FP64 state with the mixed geometry (first step).
-__global__ void __launch_bounds__(kBlock) k_mixed_lambda(MixedConst ph, StageArgs a) {
-  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
-  float lam = 0.0f;
-  if (c < a.n) {
-    float q[kNeqMax];
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) q[v] = v < ph.neq ? __double2float_rn(a.SN[v * a.n + c]) : 0.0f;
-    lam = cell_lambda_f(ph, a.geo, __ldg(a.geom + c), q);
-  }
-  block_max_lambda_f(lam, a.lambda);
+// FP32 copy of an FP64 state (after an upload or an FP64-path step).
+__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
+    Sf[i] = __double2float_rn(S[i]);
 }
 
 MixedConst make_const(const Phys &ph) {
@@ -628,7 +541,7 @@ MixedConst make_const(const Phys &ph) {
 }
 
 // resource slots
-enum { kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4 };
+enum { kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6 };
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
   if (r.buf[slot]) cudaFree(r.buf[slot]);
@@ -637,6 +550,16 @@ cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
   cudaError_t e = cudaMalloc(&r.buf[slot], bytes ? bytes : 16);
   if (e == cudaSuccess) r.bytes[slot] = bytes;
   return e;
+}
+
+StageArgs stage_args(MixedResources &r, const MeshView &m) {
+  StageArgs a{};
+  a.n = int(m.n);
+  a.nbr = m.nbr;
+  a.geom = static_cast<const int32_t *>(r.buf[kBufGeom]);
+  a.hang_nbr = m.hang_nbr;
+  a.geo = static_cast<const GeoTables *>(r.buf[kBufTables]);
+  return a;
 }
 
 }  // namespace
@@ -655,6 +578,7 @@ bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
 
 int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen) {
   r.ready = false;
+  r.snf_valid = false;
   char tmp[256];
   if (!mixed_supported(ph, tmp, sizeof tmp)) {
     snprintf(why, whylen, "%s", tmp);
@@ -720,6 +644,10 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
           snprintf(why, whylen, "the mixed path needs one sub-face area per level and face");
           return FVGPU_ERR_UNSUPPORTED;
         }
+        if (m->nbr_face[i] != opp_face(f)) {
+          snprintf(why, whylen, "the mixed path needs neighbour face = opposite face");
+          return FVGPU_ERR_UNSUPPORTED;
+        }
       } else {
         const int nl = m->level[nc];
         if (nl == lev)
@@ -760,7 +688,9 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       (e = cudaMemcpy(r.buf[kBufTables], &gt, sizeof gt, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess) {
+      (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
   }
@@ -776,16 +706,7 @@ void release_mixed(MixedResources &r) {
     r.bytes[i] = 0;
   }
   r.ready = false;
-}
-
-static StageArgs stage_args(MixedResources &r, const MeshView &m) {
-  StageArgs a{};
-  a.n = m.n;
-  a.nbr = m.nbr;
-  a.geom = static_cast<const int32_t *>(r.buf[kBufGeom]);
-  a.hang_nbr = m.hang_nbr;
-  a.geo = static_cast<const GeoTables *>(r.buf[kBufTables]);
-  return a;
+  r.snf_valid = false;
 }
 
 double *mixed_alt_state(MixedResources &r) { return static_cast<double *>(r.buf[kBufAlt]); }
@@ -794,19 +715,20 @@ void mixed_swap_state(MixedResources &r, void *&state) {
   void *t = state;
   state = r.buf[kBufAlt];
   r.buf[kBufAlt] = t;
+  t = r.buf[kBufSNf];
+  r.buf[kBufSNf] = r.buf[kBufSNfAlt];
+  r.buf[kBufSNfAlt] = t;
 }
 
-cudaError_t enqueue_mixed_lambda(MixedResources &r, const Phys &ph, const MeshView &m, const double *S,
-                                 double *lambda, LaunchMarks &marks, cudaStream_t st) {
-  StageArgs a = stage_args(r, m);
-  a.SN = S;
-  a.lambda = lambda;
-  marks.mark(FVGPU_KIND_DT);
-  k_mixed_lambda<<<unsigned((m.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(make_const(ph), a);
-  return cudaGetLastError();
+cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
+  marks.mark(FVGPU_KIND_MIXED_AUX);
+  k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) r.snf_valid = true;
+  return e;
 }
 
-// One RK step from state `in` to state `out` (out != in).
+// One RK step from FP64 state `in` (and its FP32 copy) to `out`.
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,
                                unsigned long long *err, LaunchMarks &marks, cudaStream_t st) {
@@ -821,10 +743,12 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
   const unsigned grid = unsigned((m.n + kBlock - 1) / kBlock);
   for (int k = 0; k < nst; ++k) {
     StageArgs a = stage_args(r, m);
-    a.SN = in;
+    a.SNf = static_cast<const float *>(r.buf[kBufSNf]);
     a.Din = k == 0 ? nullptr : D[(k - 1) & 1];
     a.Dout = D[k & 1];
+    a.SN = in;
     a.SNout = out;
+    a.SNfout = static_cast<float *>(r.buf[kBufSNfAlt]);
     a.dt = dt;
     a.irk = kStages[scheme][k];
     a.last = k == nst - 1;

@@ -18,6 +18,7 @@ struct MixedResources {
   size_t bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t n = 0;
   bool ready = false;
+  bool snf_valid = false;  // FP32 copy of the current state is up to date
 };
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen);
@@ -29,8 +30,8 @@ void release_mixed(MixedResources &r);
 double *mixed_alt_state(MixedResources &r);
 // exchange the caller's state buffer with the second buffer after a step
 void mixed_swap_state(MixedResources &r, void *&state);
-cudaError_t enqueue_mixed_lambda(MixedResources &r, const Phys &ph, const MeshView &m, const double *S,
-                                 double *lambda, LaunchMarks &marks, cudaStream_t st);
+// rebuild the FP32 copy of the FP64 state S (after uploads / FP64-path updates)
+cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st);
 // One RK step from FP64 state `in` to `out` (distinct buffers).
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,
