@@ -74,6 +74,8 @@ _GPU_SIGS = {
     "fvgpu_profile_step": ([C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
                            C.c_int),
     "fvgpu_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+    "fvgpu_conservation_noalloc": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p],
+                                   C.c_int),
 }
 
 

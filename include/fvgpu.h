@@ -153,6 +153,23 @@ int fvgpu_compute_dt(fvgpu_ctx *ctx, double cfl, double *dt);
  * (conservationcalc.c:19-34), FP64, fixed reduction order. */
 int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
 
+/* Conservation sums for callers that cannot allocate device memory (no
+ * counterpart in the reference).  Some host codes reserve all their device
+ * memory up front and allow no allocation inside the time loop, or run under
+ * a device-memory cap that is already fully committed; they cannot give
+ * fvgpu_conservation the context-owned scratch it allocates.  This variant
+ * takes DEVICE pointers the caller owns -- S [neq][ncells], vol [ncells] and
+ * sums [neq+1] -- and keeps its scratch in a fixed 48 KiB device array of the
+ * library (every GPU that loads the library holds it until exit).  Limits:
+ * 1 <= neq <= 5, 1 <= ncells < 2^31, else FVGPU_ERR_ARG.  It allocates
+ * nothing.  The first call on a device looks up the array's device address
+ * (make it before any stream capture on that device).  All calls share the
+ * array: calls that overlap on the GPU race, so order them.  Work is queued on
+ * `stream` (a cudaStream_t, NULL = default stream); sums are ready when that
+ * stream reaches this point. */
+int fvgpu_conservation_noalloc(const double *S, const double *vol, int64_t ncells, int neq, double *sums,
+                               void *stream);
+
 /* ---- adjoint ----------------------------------------------------------- */
 /* dJdU = (dR/dU)^T w for the residual R(U) of the current state (FP64),
  * w and dJdU host arrays [neq][ld]. */
