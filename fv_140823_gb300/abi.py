@@ -26,6 +26,7 @@ ERROR_NAMES = {
 
 FP64 = 0
 MIXED = 1
+FLAG_NO_BRICKS = 1
 SCHEME_EULER = 1
 SCHEME_SSPRK2 = 2
 SCHEME_SSPRK3 = 3
@@ -45,7 +46,7 @@ NKINDS = 8
 class FvConfig(C.Structure):
     _fields_ = [("model", C.c_int), ("ns", C.c_int), ("ischeme", C.c_int), ("iprimtv", C.c_int),
                 ("eos", C.c_int), ("precision", C.c_int), ("device", C.c_int),
-                ("reserved0", C.c_int), ("gamma", C.c_double), ("pinf", C.c_double),
+                ("flags", C.c_int), ("gamma", C.c_double), ("pinf", C.c_double),
                 ("visc", C.c_double), ("ymin", C.c_double), ("inflow", C.c_double * 8),
                 ("reserved", C.c_double * 4)]
 
@@ -67,6 +68,7 @@ class SolverConfig:
     eos: int = 0
     precision: int = FP64
     device: int = 0
+    flags: int = 0
     gamma: float = 1.4
     pinf: float = 0.0
     visc: float = 0.0
@@ -79,7 +81,7 @@ class SolverConfig:
 
     def to_c(self) -> FvConfig:
         c = FvConfig()
-        for n in ("model", "ns", "ischeme", "iprimtv", "eos", "precision", "device"):
+        for n in ("model", "ns", "ischeme", "iprimtv", "eos", "precision", "device", "flags"):
             setattr(c, n, int(getattr(self, n)))
         for n in ("gamma", "pinf", "visc", "ymin"):
             setattr(c, n, float(getattr(self, n)))

@@ -613,6 +613,7 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   ctx->lambda_valid = false;
   {
     char why[256] = {0};
+    ctx->mixed.force_general = (ctx->cfg.flags & FVGPU_FLAG_NO_BRICKS) != 0;
     ctx->mixed_ok = fv::mixed_prepare_host(ctx->mixed, ctx->ph, m, why, sizeof why) == FVGPU_OK;
     ctx->mixed_why = why;
     if (ctx->cfg.precision == FVGPU_MIXED && !ctx->mixed_ok)

@@ -1,6 +1,6 @@
 // fvbuild: -fmad=false
 //
-// FP32-mixed path: one fused kernel per RK stage.
+// FP32-mixed path: fused kernels per RK stage.
 //
 // Arithmetic.  Reconstruction, equation of state and HLLC fluxes run in FP32
 // (the mixture EOS pressure inversion stays FP64).  The state is kept in FP64
@@ -17,26 +17,31 @@
 // per-stage increments are small against the state, their FP32 rounding is
 // ~1e-8 of the state per stage, and every add into the state is FP64.
 //
-// Work decomposition.  One thread per cell, blocks of kBlock consecutive cells
-// (Morton order: an 8x8x4 brick of a uniform octree).
-//   A  stage state S = SNf + D of the block's cells into shared memory
-//   B  MUSCL/minmod face values of the thread's 6 faces (faceinterp.c /
-//      reconctruct_V3.c) into shared memory
-//   C  each face flux computed once, canonically from the face's lower cell
-//      (the one whose +x/+y/+z face it is): a thread computes its own + faces
-//      and publishes them in shared memory; the upper cell reads them, or
-//      recomputes the same canonical flux bit for bit when the lower cell is
-//      in another block or the face is a 1:4 sub-face.  Equal and opposite
-//      contributions -> conservative and deterministic.  The face loop is
-//      rolled with a single flux call site so the kernel fits the
-//      instruction cache.
-//   D  residual, RK stage update, (last stage) FP64 state, FP32 copy and CFL
-//      radius.
-// This translation unit is compiled without automatic multiply-add
-// contraction (explicit fmaf only), so every copy of an expression gives the
-// same bits, which the canonical-flux sharing relies on.
+// Canonical face fluxes.  Every face flux is defined from the face's lower
+// cell (the one whose +x/+y/+z face it is), with that face's frame; the
+// lower cell's residual gets -A F and the upper cell's +A F.  Whoever
+// evaluates a face gets the same bits (this translation unit is compiled
+// without automatic multiply-add contraction, explicit fmaf only), so the
+// scheme is conservative and deterministic however the work is split.
+//
+// Two kernels share that definition:
+//   k_mixed_brick    a Morton-aligned 8x8x4 brick of same-level cells whose
+//                    six sides are same-level bricks or domain boundaries:
+//                    brick + 2-deep face halo staged in shared memory, the
+//                    896 faces of the brick evaluated once each by dense
+//                    per-thread face tasks, no neighbour tables read;
+//   k_mixed_general  any other run of up to 256 consecutive cells (AMR
+//                    interfaces, 1:4 faces): table-driven, each thread
+//                    computes its + faces and publishes them, the upper cell
+//                    reuses them or recomputes the canonical flux across
+//                    block edges and 1:4 sub-faces.
+// A cell's residual is accumulated in the same face order with the same
+// operations in both kernels, so its result does not depend on which kernel
+// handled it (tests compare the two bit for bit).
+//
 // Geometry comes from per-level tables (octree-regular meshes): a packed
 // per-cell code (level + face relations) replaces the FP64 face tables.
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -53,6 +58,16 @@ constexpr int kRelSame = 0, kRelFiner = 1, kRelCoarser = 2, kRelBoundary = 3;
 constexpr int kGeoStride = 4;  // per (level, face, relation): dcf, 1/dcc, area, pad
 constexpr int kGeoEntries = (kMaxLevel + 1) * 6 * 4;
 
+// brick geometry: 8 x 8 x 4 cells in local Morton order, 2-deep face halo
+constexpr int BX = 8, BY = 8, BZ = 4;
+constexpr int TX = BX + 4, TY = BY + 4, TZ = BZ + 4;
+constexpr int kTile = TX * TY * TZ;
+constexpr int kFacesX = (BX + 1) * BY * BZ;  // 288
+constexpr int kFacesY = BX * (BY + 1) * BZ;  // 288
+constexpr int kFacesZ = BX * BY * (BZ + 1);  // 320
+constexpr int kFaces = kFacesX + kFacesY + kFacesZ;
+constexpr int kHalo = 2 * (2 * BY * BZ + 2 * BX * BZ + 2 * BX * BY);  // 512
+
 struct GeoTables {
   float face[kGeoEntries * kGeoStride];
   float sub_area[(kMaxLevel + 1) * 6];
@@ -65,6 +80,10 @@ __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return 
 // + faces: normals +x (1), +y (2), +z (5); their slot in the flux table
 __host__ __device__ constexpr bool is_plus_face(int f) { return f == 1 || f == 2 || f == 5; }
 __device__ __forceinline__ int plus_slot(int f) { return f == 1 ? 0 : (f == 2 ? 1 : 2); }
+// residual accumulation order (both kernels): +x, +y, +z, -x, -y, -z
+__device__ __forceinline__ int face_of_iter(int it) {
+  return it == 0 ? 1 : it == 1 ? 2 : it == 2 ? 5 : it == 3 ? 3 : it == 4 ? 0 : 4;
+}
 
 // FP32 constants, converted once on the host.
 struct MixedConst {
@@ -75,12 +94,22 @@ struct MixedConst {
   int model, neq, ischeme, pad;
 };
 
+// A block of work: a brick (type 0) or a general run (type 1).
+struct BlockDesc {
+  int start;    // first cell
+  int count;    // cells (256 for a brick)
+  int level;    // brick level
+  int side[6];  // brick side per face index: >= 0 first cell of the neighbour brick, < 0: -1 - bc
+  int pad;
+};
+
 struct StageArgs {
   int n;
   const int32_t *nbr;       // [6][n]
   const int32_t *geom;      // [n]: level | rel_f << (5 + 2 f)
   const int32_t *hang_nbr;  // [nhang][4]
   const GeoTables *geo;
+  const BlockDesc *blocks;
   const float *SNf;         // [neq][n] FP32 copy of the step-start state
   const float *Din;         // [neq][n] stage-input increment (null: zero)
   float *Dout;              // [neq][n]
@@ -106,7 +135,7 @@ struct FS {
 };
 
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ float fast_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
+__device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
 
 // FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
@@ -159,6 +188,20 @@ __device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f,
     g.q[1] = g.r * g.u;
     g.q[2] = g.r * g.v;
     g.q[3] = g.r * g.w;
+  }
+}
+
+// value across a boundary face: the own state, or its ghost (deltavalues.c:9-14)
+__device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float own[kNeqMax],
+                                               float nb[kNeqMax]) {
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
+  if (bc == 1 || bc == 3 || bc == 4) {
+    FS g;
+    mixed_face_state(mc, own, false, g);
+    mixed_ghost(mc, bc, f, g);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
   }
 }
 
@@ -220,95 +263,45 @@ __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, i
   return ok && (r1 || r2 || r3 || r4);
 }
 
-struct Block {
-  const StageArgs &a;
-  const MixedConst &mc;
-  int c0;
-  const float (*st)[kBlock];
-  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, const float (*st_)[kBlock])
-      : a(a_), mc(mc_), c0(c0_), st(st_) {}
-  __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(kBlock); }
-  // stage state of any cell: shared memory when in the block, else SNf + D
-  __device__ __forceinline__ void state(int x, float q[kNeqMax]) const {
-    if (in_block(x)) {
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) q[v] = st[v][x - c0];
-      return;
-    }
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      float s = 0.0f;
-      if (v < mc.neq) {
-        s = __ldg(a.SNf + v * a.n + x);
-        if (a.Din) s += __ldg(a.Din + v * a.n + x);
-      }
-      q[v] = s;
-    }
+// Canonical flux of a face from the lower / upper face values (bc > 0: a
+// domain-boundary face, the upper side is the ghost of the lower one).
+__device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int bc, bool clip,
+                                               const float lo[kNeqMax], const float hi[kNeqMax],
+                                               float Fn[kNeqMax]) {
+  FS Ls, Rs;
+  bool ok = mixed_face_state(mc, lo, clip, Ls);
+  if (bc > 0) {
+    Rs = Ls;
+    mixed_ghost(mc, bc, f, Rs);
+  } else {
+    ok &= mixed_face_state(mc, hi, clip, Rs);
   }
-  // value across face f of cell x (deltavalues.c): single neighbour, mean of
-  // the four fine ones, or the boundary ghost
-  __device__ __forceinline__ void across(int x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
-    const int32_t code = __ldg(a.nbr + f * a.n + x);
-    if (code >= 0) {
-      state(code, nb);
-    } else if (is_hanging(code)) {
-      const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-      float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-      for (int s = 0; s < 4; ++s) {
-        float q[kNeqMax];
-        state(__ldg(k + s), q);
+  ok &= mixed_hllc_normal(mc, f, bc, Ls, Rs, Fn);
+  return ok;
+}
+
+// Minmod face value of face f of a cell with geometry code gx from its state
+// and the deltas across f (d0) and across the opposite face (d1)
+// (reconctruct_V3.c:17-43, slopes divided by dist_cc as multiplications).
+__device__ __forceinline__ void recon_face(const GeoTables *geo, int32_t gx, int f, const float qx[kNeqMax],
+                                           const float d0[kNeqMax], const float d1[kNeqMax],
+                                           float out[kNeqMax]) {
+  const int lev = level_of(gx);
+  const int rf = rel_of(gx, f), ro = rel_of(gx, opp_face(f));
+  const float *gf = geo_face(geo, lev, f, rf);
+  const float dcf = gf[0], inv_p = gf[1];
+  const float inv_m = geo_face(geo, lev, opp_face(f), ro)[1];
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
-      }
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
-    } else {
-      const int bc = -1 - code;
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
-      if (bc == 1 || bc == 3 || bc == 4) {
-        FS g;
-        mixed_face_state(mc, own, false, g);
-        mixed_ghost(mc, bc, f, g);
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
-      }
+  for (int v = 0; v < kNeqMax; ++v) {
+    float grad = 0.0f;
+    if (rf != kRelBoundary && fabsf(d0[v]) > 1e-10f) {
+      const float sp = d0[v] * inv_p;
+      const float sm = -d1[v] * inv_m;
+      if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
     }
+    out[v] = fmaf(dcf, grad, qx[v]);
   }
-  // minmod face value of face f (reconctruct_V3.c:17-43) from the deltas
-  __device__ __forceinline__ void recon(int32_t gx, int f, const float qx[kNeqMax], const float d0[kNeqMax],
-                                        const float d1[kNeqMax], float out[kNeqMax]) const {
-    const int lev = level_of(gx);
-    const int rf = rel_of(gx, f), ro = rel_of(gx, opp_face(f));
-    const float *gf = geo_face(a.geo, lev, f, rf);
-    const float dcf = gf[0], inv_p = gf[1];
-    const float inv_m = geo_face(a.geo, lev, opp_face(f), ro)[1];
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      float grad = 0.0f;
-      if (rf != kRelBoundary && fabsf(d0[v]) > 1e-10f) {
-        const float sp = d0[v] * inv_p;
-        const float sm = -d1[v] * inv_m;
-        if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
-      }
-      out[v] = fmaf(dcf, grad, qx[v]);
-    }
-  }
-  // face value of face f of any cell (used across block edges)
-  __device__ __forceinline__ void recon_any(int x, int f, float out[kNeqMax]) const {
-    float qx[kNeqMax], nbp[kNeqMax], nbm[kNeqMax], d0[kNeqMax], d1[kNeqMax];
-    state(x, qx);
-    across(x, f, qx, nbp);
-    across(x, opp_face(f), qx, nbm);
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      d0[v] = nbp[v] - qx[v];
-      d1[v] = nbm[v] - qx[v];
-    }
-    recon(__ldg(a.geom + x), f, qx, d0, d1, out);
-  }
-};
+}
 
 __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
   __shared__ float red[kBlock / 32];
@@ -340,19 +333,129 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
   return acc * geo->inv2vol[lev];
 }
 
-__global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs a) {
+// RK stage update of one cell in increment form; FP64 state, FP32 copy and
+// CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
+__device__ __forceinline__ float stage_update(const MixedConst &mc, const StageArgs &a, int c, int32_t g,
+                                              const float R[kNeqMax], const float din[kNeqMax], float dt, bool ok) {
+  const int n = a.n, neq = mc.neq;
+  bool finite = true;
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v)
+    if (v < neq && !isfinite(R[v])) finite = false;
+  if (!ok) raise_error(a.err, kErrRegion, c);
+  if (!finite) raise_error(a.err, kErrNonFinite, c);
+  const float dtv = dt * a.geo->inv_vol[level_of(g)];
+  float dn[kNeqMax];
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) {
+    const float incr = dtv * R[v];
+    switch (a.irk) {
+      case 1: dn[v] = incr; break;
+      case 2: dn[v] = 0.25f * (din[v] + incr); break;
+      case 3: dn[v] = (2.0f / 3.0f) * (din[v] + incr); break;
+      default: dn[v] = 0.5f * (din[v] + incr); break;
+    }
+  }
+  if (a.last) {
+    float qn[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) {
+      if (v >= neq) break;
+      const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
+      a.SNout[v * n + c] = snew;
+      qn[v] = __double2float_rn(snew);
+      a.SNfout[v * n + c] = qn[v];
+    }
+    return a.lambda ? cell_lambda_f(mc, a.geo, g, qn) : 0.0f;
+  }
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v)
+    if (v < neq) a.Dout[v * n + c] = dn[v];
+  return 0.0f;
+}
+
+// stage state of any cell from global memory: SNf + D
+__device__ __forceinline__ void global_state(const MixedConst &mc, const StageArgs &a, int x, float q[kNeqMax]) {
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) {
+    float s = 0.0f;
+    if (v < mc.neq) {
+      s = __ldg(a.SNf + v * a.n + x);
+      if (a.Din) s += __ldg(a.Din + v * a.n + x);
+    }
+    q[v] = s;
+  }
+}
+
+// ============================ general kernel ================================
+
+struct Block {
+  const StageArgs &a;
+  const MixedConst &mc;
+  int c0, cnt;
+  const float (*st)[kBlock];
+  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock])
+      : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_) {}
+  __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(cnt); }
+  __device__ __forceinline__ void state(int x, float q[kNeqMax]) const {
+    if (in_block(x)) {
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) q[v] = st[v][x - c0];
+      return;
+    }
+    global_state(mc, a, x, q);
+  }
+  // value across face f of cell x (deltavalues.c): single neighbour, mean of
+  // the four fine ones, or the boundary ghost
+  __device__ __forceinline__ void across(int x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
+    const int32_t code = __ldg(a.nbr + f * a.n + x);
+    if (code >= 0) {
+      state(code, nb);
+    } else if (is_hanging(code)) {
+      const int32_t *k = a.hang_nbr + 4 * hang_index(code);
+      float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+      for (int s = 0; s < 4; ++s) {
+        float q[kNeqMax];
+        state(__ldg(k + s), q);
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
+      }
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
+    } else {
+      boundary_value(mc, -1 - code, f, own, nb);
+    }
+  }
+  // face value of face f of any cell (used across block edges)
+  __device__ __forceinline__ void recon_any(int x, int f, float out[kNeqMax]) const {
+    float qx[kNeqMax], nbp[kNeqMax], nbm[kNeqMax], d0[kNeqMax], d1[kNeqMax];
+    state(x, qx);
+    across(x, f, qx, nbp);
+    across(x, opp_face(f), qx, nbm);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) {
+      d0[v] = nbp[v] - qx[v];
+      d1[v] = nbm[v] - qx[v];
+    }
+    recon_face(a.geo, __ldg(a.geom + x), f, qx, d0, d1, out);
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageArgs a) {
   __shared__ float st[kNeqMax][kBlock];
   __shared__ float sf[6][kNeqMax][kBlock];
   __shared__ float fp[3][kNeqMax][kBlock];
   __shared__ float s_dt;
+  const BlockDesc bd = a.blocks[blockIdx.x];
   const int t = threadIdx.x;
-  const int c0 = int(blockIdx.x) * kBlock;
+  const int c0 = bd.start;
   const int c = c0 + t;
   const int n = a.n;
-  const bool active = c < n;
+  const bool active = t < bd.count;
   const int neq = mc.neq;
   const bool muscl = mc.ischeme == 2;
-  Block blk(a, mc, c0, st);
+  Block blk(a, mc, c0, bd.count, st);
 
   // A: own stage state
   float din[kNeqMax], q[kNeqMax];
@@ -388,7 +491,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         float o[kNeqMax];
-        blk.recon(g, f, q, dl[f], dl[opp_face(f)], o);
+        recon_face(a.geo, g, f, q, dl[f], dl[opp_face(f)], o);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = o[v];
       }
@@ -401,7 +504,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs
   }
   __syncthreads();
 
-  // C: fluxes.  Order: + faces 1, 2, 5 (publish), barrier, - faces 3, 0, 4.
+  // C: fluxes, + faces (publish), barrier, - faces
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   bool ok = true;
   const int lev = level_of(g);
@@ -409,7 +512,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs
   for (int it = 0; it < 6; ++it) {
     if (it == 3) __syncthreads();
     if (!active) continue;
-    const int f = it == 0 ? 1 : it == 1 ? 2 : it == 2 ? 5 : it == 3 ? 3 : it == 4 ? 0 : 4;
+    const int f = face_of_iter(it);
     const bool plus = it < 3;
     const int fo = opp_face(f);
     const int32_t code = nb[f];
@@ -455,16 +558,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs
           lo[v] = own_low ? own[v] : oth[v];
           hi[v] = own_low ? oth[v] : own[v];
         }
-        FS Ls, Rs;
-        ok &= mixed_face_state(mc, lo, muscl, Ls);
-        const int bc = boundary ? -1 - code : 0;
-        if (boundary) {
-          Rs = Ls;
-          mixed_ghost(mc, bc, f, Rs);
-        } else {
-          ok &= mixed_face_state(mc, hi, muscl, Rs);
-        }
-        ok &= mixed_hllc_normal(mc, own_low ? f : fo, bc, Ls, Rs, Fn);
+        ok &= canonical_flux(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
         if (plus && !boundary && !hanging) {
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
@@ -476,44 +570,257 @@ __global__ void __launch_bounds__(kBlock) k_mixed_stage(MixedConst mc, StageArgs
     }
   }
 
-  // D: RK stage in increment form; FP64 state and FP32 copy at the last stage
   float lam = 0.0f;
-  if (active) {
-    bool finite = true;
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v)
-      if (v < neq && !isfinite(R[v])) finite = false;
-    if (!ok) raise_error(a.err, kErrRegion, c);
-    if (!finite) raise_error(a.err, kErrNonFinite, c);
-    const float dtv = s_dt * a.geo->inv_vol[lev];
-    float dn[kNeqMax];
+  if (active) lam = stage_update(mc, a, c, g, R, din, s_dt, ok);
+  if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
+}
+
+// ============================= brick kernel =================================
+
+__device__ __forceinline__ int tile_index(int x, int y, int z) { return ((z + 2) * TY + (y + 2)) * TX + (x + 2); }
+__device__ __forceinline__ int morton_local(int x, int y, int z) {
+  return (x & 1) | ((y & 1) << 1) | ((z & 1) << 2) | (((x >> 1) & 1) << 3) | (((y >> 1) & 1) << 4) |
+         (((z >> 1) & 1) << 5) | (((x >> 2) & 1) << 6) | (((y >> 2) & 1) << 7);
+}
+__device__ __forceinline__ void morton_decode(int t, int &x, int &y, int &z) {
+  x = (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2);
+  y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
+  z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
+}
+
+// halo cell h (0..511) of the brick: its tile coordinates, the side (face
+// index) it belongs to, its layer (1 = adjacent, 2 = second) and its local
+// coordinates inside the neighbour brick
+__device__ __forceinline__ void halo_cell(int h, int &x, int &y, int &z, int &side, int &layer, int &lx, int &ly,
+                                          int &lz) {
+  if (h < 4 * BY * BZ) {  // x sides: 2 sides x 2 layers x BY x BZ
+    const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ);
+    layer = 1 + r / (BY * BZ);
+    const int rr = r % (BY * BZ);
+    y = rr % BY;
+    z = rr / BY;
+    side = s == 0 ? 3 : 1;
+    x = s == 0 ? -layer : BX - 1 + layer;
+    lx = s == 0 ? BX - layer : layer - 1;
+    ly = y;
+    lz = z;
+  } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
+    const int hh = h - 4 * BY * BZ;
+    const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ);
+    layer = 1 + r / (BX * BZ);
+    const int rr = r % (BX * BZ);
+    x = rr % BX;
+    z = rr / BX;
+    side = s == 0 ? 0 : 2;
+    y = s == 0 ? -layer : BY - 1 + layer;
+    ly = s == 0 ? BY - layer : layer - 1;
+    lx = x;
+    lz = z;
+  } else {
+    const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
+    const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY);
+    layer = 1 + r / (BX * BY);
+    const int rr = r % (BX * BY);
+    x = rr % BX;
+    y = rr / BX;
+    side = s == 0 ? 4 : 5;
+    z = s == 0 ? -layer : BZ - 1 + layer;
+    lz = s == 0 ? BZ - layer : layer - 1;
+    lx = x;
+    ly = y;
+  }
+}
+
+// geometry code of a brick-tile cell: same level, boundary relation on the
+// faces that lie on a domain-boundary side of the brick
+__device__ __forceinline__ int32_t brick_geom(const BlockDesc &bd, int x, int y, int z) {
+  int32_t g = bd.level;
+  if (x == 0 && bd.side[3] < 0) g |= kRelBoundary << (5 + 2 * 3);
+  if (x == BX - 1 && bd.side[1] < 0) g |= kRelBoundary << (5 + 2 * 1);
+  if (y == 0 && bd.side[0] < 0) g |= kRelBoundary << (5 + 2 * 0);
+  if (y == BY - 1 && bd.side[2] < 0) g |= kRelBoundary << (5 + 2 * 2);
+  if (z == 0 && bd.side[4] < 0) g |= kRelBoundary << (5 + 2 * 4);
+  if (z == BZ - 1 && bd.side[5] < 0) g |= kRelBoundary << (5 + 2 * 5);
+  return g;
+}
+
+__device__ __forceinline__ bool in_brick(int x, int y, int z) {
+  return unsigned(x) < unsigned(BX) && unsigned(y) < unsigned(BY) && unsigned(z) < unsigned(BZ);
+}
+
+// unit step of face f in tile coordinates
+__device__ __forceinline__ void face_step(int f, int &dx, int &dy, int &dz) {
+  dx = f == 1 ? 1 : (f == 3 ? -1 : 0);
+  dy = f == 2 ? 1 : (f == 0 ? -1 : 0);
+  dz = f == 5 ? 1 : (f == 4 ? -1 : 0);
+}
+
+__global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs a) {
+  __shared__ float tile[kNeqMax][kTile];
+  __shared__ float flux[kNeqMax][kFaces];
+  __shared__ float s_dt;
+  const BlockDesc bd = a.blocks[blockIdx.x];
+  const int t = threadIdx.x;
+  const int n = a.n;
+  const int neq = mc.neq;
+  const bool muscl = mc.ischeme == 2;
+  const int c = bd.start + t;
+
+  // A1: the brick's cells and the halo of same-level neighbour bricks
+  int x, y, z;
+  morton_decode(t, x, y, z);
+  float din[kNeqMax];
+  {
+    const int ti = tile_index(x, y, z);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      const float incr = dtv * R[v];
-      switch (a.irk) {
-        case 1: dn[v] = incr; break;
-        case 2: dn[v] = 0.25f * (din[v] + incr); break;
-        case 3: dn[v] = (2.0f / 3.0f) * (din[v] + incr); break;
-        default: dn[v] = 0.5f * (din[v] + incr); break;
+      din[v] = 0.0f;
+      float s = 0.0f;
+      if (v < neq) {
+        din[v] = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
+        s = __ldg(a.SNf + v * n + c) + din[v];
       }
-    }
-    if (a.last) {
-      float qn[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) {
-        if (v >= neq) break;
-        const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
-        a.SNout[v * n + c] = snew;
-        qn[v] = __double2float_rn(snew);
-        a.SNfout[v * n + c] = qn[v];
-      }
-      if (a.lambda) lam = cell_lambda_f(mc, a.geo, g, qn);
-    } else {
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v)
-        if (v < neq) a.Dout[v * n + c] = dn[v];
+      tile[v][ti] = s;
     }
   }
+#pragma unroll 1
+  for (int h = t; h < kHalo; h += kBlock) {
+    int hx, hy, hz, side, layer, lx, ly, lz;
+    halo_cell(h, hx, hy, hz, side, layer, lx, ly, lz);
+    const int base = bd.side[side];
+    if (base >= 0) {
+      float q[kNeqMax];
+      global_state(mc, a, base + morton_local(lx, ly, lz), q);
+      const int ti = tile_index(hx, hy, hz);
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = q[v];
+    }
+  }
+  if (t == 0) s_dt = __double2float_rn(*a.dt);
+  __syncthreads();
+  // A2: ghost values beyond domain-boundary sides (deltavalues.c:9-14)
+#pragma unroll 1
+  for (int h = t; h < kHalo; h += kBlock) {
+    int hx, hy, hz, side, layer, lx, ly, lz;
+    halo_cell(h, hx, hy, hz, side, layer, lx, ly, lz);
+    const int base = bd.side[side];
+    if (base < 0) {
+      int dx, dy, dz;
+      face_step(side, dx, dy, dz);
+      // the brick cell this ghost stands next to
+      const int ix = hx - layer * dx, iy = hy - layer * dy, iz = hz - layer * dz;
+      float own[kNeqMax], gv[kNeqMax];
+      const int ti_own = tile_index(ix, iy, iz);
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
+      boundary_value(mc, -1 - base, side, own, gv);
+      const int ti = tile_index(hx, hy, hz);
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = gv[v];
+    }
+  }
+  __syncthreads();
+
+  // B: face tasks -- each face of the brick once
+  bool ok = true;
+#pragma unroll 1
+  for (int task = t; task < kFaces; task += kBlock) {
+    int f, lx, ly, lz;  // lower cell (tile coords) and its + face
+    if (task < kFacesX) {
+      f = 1;
+      lx = task % (BX + 1) - 1;
+      ly = (task / (BX + 1)) % BY;
+      lz = task / ((BX + 1) * BY);
+    } else if (task < kFacesX + kFacesY) {
+      const int r = task - kFacesX;
+      f = 2;
+      lx = r % BX;
+      ly = (r / BX) % (BY + 1) - 1;
+      lz = r / (BX * (BY + 1));
+    } else {
+      const int r = task - kFacesX - kFacesY;
+      f = 5;
+      lx = r % BX;
+      ly = (r / BX) % BY;
+      lz = r / (BX * BY) - 1;
+    }
+    int dx, dy, dz;
+    face_step(f, dx, dy, dz);
+    const int ux = lx + dx, uy = ly + dy, uz = lz + dz;
+    const bool low_in = in_brick(lx, ly, lz), up_in = in_brick(ux, uy, uz);
+    const int fo = opp_face(f);
+    // a face on a domain-boundary side: only the brick cell's side exists
+    const int bside = low_in ? bd.side[f] : bd.side[fo];
+    const bool dom_boundary = !(low_in && up_in) && bside < 0;
+    float Fn[kNeqMax];
+    // face value of (cell P, face g): state and the two values across
+    auto recon_tile = [&](int px, int py, int pz, int g, float out[kNeqMax]) {
+      int gx, gy, gz;
+      face_step(g, gx, gy, gz);
+      const int ip = tile_index(px, py, pz), ia = tile_index(px + gx, py + gy, pz + gz),
+                ib = tile_index(px - gx, py - gy, pz - gz);
+      float qp[kNeqMax], d0[kNeqMax], d1[kNeqMax];
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) {
+        qp[v] = tile[v][ip];
+        d0[v] = tile[v][ia] - qp[v];
+        d1[v] = tile[v][ib] - qp[v];
+      }
+      if (!muscl) {
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) out[v] = qp[v];
+        return;
+      }
+      const int32_t gp = in_brick(px, py, pz) ? brick_geom(bd, px, py, pz) : bd.level;
+      recon_face(a.geo, gp, g, qp, d0, d1, out);
+    };
+    if (dom_boundary) {
+      // the brick cell's own boundary face, own frame (residual_faces_AMR.c:196-209)
+      const int bf = low_in ? f : fo;
+      float own[kNeqMax], dummy[kNeqMax];
+      if (low_in)
+        recon_tile(lx, ly, lz, f, own);
+      else
+        recon_tile(ux, uy, uz, fo, own);
+      const bool fok = canonical_flux(mc, bf, -1 - bside, muscl, own, dummy, Fn);
+      ok &= fok;
+      if (!low_in) {  // stored as the canonical +-face flux of the missing lower cell
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
+      }
+    } else {
+      float lo[kNeqMax], hi[kNeqMax];
+      recon_tile(lx, ly, lz, f, lo);
+      recon_tile(ux, uy, uz, fo, hi);
+      ok &= canonical_flux(mc, f, 0, muscl, lo, hi, Fn);
+    }
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
+  }
+  __syncthreads();
+
+  // C: gather in the fixed face order, RK stage update
+  const int32_t g = brick_geom(bd, x, y, z);
+  const int lev = bd.level;
+  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int it = 0; it < 6; ++it) {
+    const int f = face_of_iter(it);
+    const bool plus = it < 3;
+    const float A = geo_face(a.geo, lev, f, rel_of(g, f))[2];
+    // index of the face task holding this face (lower cell = this cell for + faces)
+    int task;
+    if (f == 1 || f == 3)
+      task = z * (BX + 1) * BY + y * (BX + 1) + (x + (f == 1 ? 1 : 0));
+    else if (f == 2 || f == 0)
+      task = kFacesX + z * BX * (BY + 1) + (y + (f == 2 ? 1 : 0)) * BX + x;
+    else
+      task = kFacesX + kFacesY + (z + (f == 5 ? 1 : 0)) * BX * BY + y * BX + x;
+    const float sA = plus ? -A : A;
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, flux[v][task], R[v]);
+  }
+  const float lam = stage_update(mc, a, c, g, R, din, s_dt, ok);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
@@ -541,7 +848,7 @@ MixedConst make_const(const Phys &ph) {
 }
 
 // resource slots
-enum { kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6 };
+enum { kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6, kBufBlocks = 7 };
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
   if (r.buf[slot]) cudaFree(r.buf[slot]);
@@ -560,6 +867,74 @@ StageArgs stage_args(MixedResources &r, const MeshView &m) {
   a.hang_nbr = m.hang_nbr;
   a.geo = static_cast<const GeoTables *>(r.buf[kBufTables]);
   return a;
+}
+
+// ---- host: brick detection ---------------------------------------------------
+
+int host_morton_local(int x, int y, int z) {
+  return (x & 1) | ((y & 1) << 1) | ((z & 1) << 2) | (((x >> 1) & 1) << 3) | (((y >> 1) & 1) << 4) |
+         (((z >> 1) & 1) << 5) | (((x >> 2) & 1) << 6) | (((y >> 2) & 1) << 7);
+}
+void host_morton_decode(int t, int &x, int &y, int &z) {
+  x = (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2);
+  y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
+  z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
+}
+constexpr int kStepX[6] = {0, 1, 0, -1, 0, 0}, kStepY[6] = {-1, 0, 1, 0, 0, 0}, kStepZ[6] = {0, 0, 0, 0, -1, 1};
+
+// cells i..i+255 form an 8x8x4 same-level brick in local Morton order whose
+// internal face links are the brick's own
+bool brick_interior(const fvgpu_mesh_soa *m, int64_t i) {
+  const int64_t n = m->ncells;
+  if (i + kBlock > n) return false;
+  const int lev = m->level[i];
+  // quick rejects: the corner cell's +x/+y/+z neighbours
+  if (m->nbr[1 * n + i] != i + 1 || m->nbr[2 * n + i] != i + 2 || m->nbr[5 * n + i] != i + 4) return false;
+  for (int t = 0; t < kBlock; ++t) {
+    if (m->level[i + t] != lev) return false;
+    int x, y, z;
+    host_morton_decode(t, x, y, z);
+    for (int f = 0; f < 6; ++f) {
+      const int nx = x + kStepX[f], ny = y + kStepY[f], nz = z + kStepZ[f];
+      if (nx < 0 || nx >= BX || ny < 0 || ny >= BY || nz < 0 || nz >= BZ) continue;
+      if (m->nbr[int64_t(f) * n + i + t] != i + host_morton_local(nx, ny, nz)) return false;
+    }
+  }
+  return true;
+}
+
+// side f of brick i: the first cell of a same-level brick that supplies all
+// its neighbours, -1-bc for a uniform domain boundary, or INT_MIN
+int brick_side(const fvgpu_mesh_soa *m, int64_t i, int f, const std::vector<char> &is_brick) {
+  const int64_t n = m->ncells;
+  int result = 0;
+  bool first = true;
+  for (int t = 0; t < kBlock; ++t) {
+    int x, y, z;
+    host_morton_decode(t, x, y, z);
+    const int nx = x + kStepX[f], ny = y + kStepY[f], nz = z + kStepZ[f];
+    if (nx >= 0 && nx < BX && ny >= 0 && ny < BY && nz >= 0 && nz < BZ) continue;  // interior face
+    const int32_t code = m->nbr[int64_t(f) * n + i + t];
+    int value;
+    if (code < 0 && code > FVGPU_HANG0) {
+      value = code;  // boundary -1 - bc
+    } else if (code >= 0) {
+      const int wx = (nx + BX) % BX, wy = (ny + BY) % BY, wz = (nz + BZ) % BZ;
+      const int64_t base = int64_t(code) - host_morton_local(wx, wy, wz);
+      if (base < 0 || base + kBlock > n || !is_brick[size_t(base)]) return INT32_MIN;
+      if (m->level[code] != m->level[i]) return INT32_MIN;
+      value = int(base);
+    } else {
+      return INT32_MIN;  // 1:4 face
+    }
+    if (first) {
+      result = value;
+      first = false;
+    } else if (value != result) {
+      return INT32_MIN;
+    }
+  }
+  return result;
 }
 
 }  // namespace
@@ -681,11 +1056,65 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     }
     geom[size_t(c)] = code;
   }
+  // bricks: candidate starts, then keep those whose six sides resolve
+  std::vector<char> is_brick(size_t(n), 0);
+  if (!r.force_general) {
+    for (int64_t i = 0; i + kBlock <= n;) {
+      if (brick_interior(m, i)) {
+        is_brick[size_t(i)] = 1;
+        i += kBlock;
+      } else {
+        ++i;
+      }
+    }
+  }
+  std::vector<BlockDesc> bricks, general;
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (int64_t i = 0; i < n; ++i) {
+      if (!is_brick[size_t(i)]) continue;
+      for (int f = 0; f < 6; ++f) {
+        if (brick_side(m, i, f, is_brick) == INT32_MIN) {
+          is_brick[size_t(i)] = 0;
+          changed = true;
+          break;
+        }
+      }
+    }
+  }
+  for (int64_t i = 0; i < n;) {
+    if (is_brick[size_t(i)]) {
+      BlockDesc d;
+      memset(&d, 0, sizeof d);
+      d.start = int(i);
+      d.count = kBlock;
+      d.level = m->level[i];
+      for (int f = 0; f < 6; ++f) d.side[f] = brick_side(m, i, f, is_brick);
+      bricks.push_back(d);
+      i += kBlock;
+      continue;
+    }
+    BlockDesc d;
+    memset(&d, 0, sizeof d);
+    d.start = int(i);
+    int cnt = 0;
+    while (i < n && cnt < kBlock && !is_brick[size_t(i)]) {
+      ++i;
+      ++cnt;
+    }
+    d.count = cnt;
+    general.push_back(d);
+  }
+  std::vector<BlockDesc> all(bricks);
+  all.insert(all.end(), general.begin(), general.end());
   cudaError_t e;
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = alloc_slot(r, kBufTables, sizeof(GeoTables))) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufTables], &gt, sizeof gt, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufBlocks, sizeof(BlockDesc) * (all.size() + 1))) != cudaSuccess ||
+      (e = cudaMemcpy(r.buf[kBufBlocks], all.data(), sizeof(BlockDesc) * all.size(), cudaMemcpyHostToDevice)) !=
+          cudaSuccess ||
       (e = alloc_slot(r, kBufD1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
@@ -695,6 +1124,8 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
   }
   r.n = n;
+  r.nbricks = int64_t(bricks.size());
+  r.ngeneral = int64_t(general.size());
   r.ready = true;
   return FVGPU_OK;
 }
@@ -707,6 +1138,7 @@ void release_mixed(MixedResources &r) {
   }
   r.ready = false;
   r.snf_valid = false;
+  r.nbricks = r.ngeneral = 0;
 }
 
 double *mixed_alt_state(MixedResources &r) { return static_cast<double *>(r.buf[kBufAlt]); }
@@ -740,7 +1172,7 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
   }
   float *D[2] = {static_cast<float *>(r.buf[kBufD1]), static_cast<float *>(r.buf[kBufD2])};
   const MixedConst mc = make_const(ph);
-  const unsigned grid = unsigned((m.n + kBlock - 1) / kBlock);
+  const BlockDesc *blocks = static_cast<const BlockDesc *>(r.buf[kBufBlocks]);
   for (int k = 0; k < nst; ++k) {
     StageArgs a = stage_args(r, m);
     a.SNf = static_cast<const float *>(r.buf[kBufSNf]);
@@ -754,10 +1186,20 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.last = k == nst - 1;
     a.lambda = (a.last && cfl_mode) ? lambda : nullptr;
     a.err = err;
-    marks.mark(FVGPU_KIND_MIXED_STAGE);
-    k_mixed_stage<<<grid, kBlock, 0, st>>>(mc, a);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (r.nbricks > 0) {
+      a.blocks = blocks;
+      marks.mark(FVGPU_KIND_MIXED_STAGE);
+      k_mixed_brick<<<unsigned(r.nbricks), kBlock, 0, st>>>(mc, a);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (r.ngeneral > 0) {
+      a.blocks = blocks + r.nbricks;
+      marks.mark(FVGPU_KIND_MIXED_STAGE);
+      k_mixed_general<<<unsigned(r.ngeneral), kBlock, 0, st>>>(mc, a);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }

@@ -17,6 +17,9 @@ struct MixedResources {
   void *buf[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t n = 0;
+  int64_t nbricks = 0;     // brick blocks (structured fast path)
+  int64_t ngeneral = 0;    // general blocks
+  bool force_general = false;  // FVGPU_FLAG_NO_BRICKS
   bool ready = false;
   bool snf_valid = false;  // FP32 copy of the current state is up to date
 };

@@ -56,6 +56,11 @@ extern "C" {
 #define FVGPU_MIXED 1  /* reconstruction, EOS and fluxes in FP32; residual
                           accumulation, RK update, sums and dt in FP64 */
 
+/* fvgpu_config.flags */
+#define FVGPU_FLAG_NO_BRICKS 1  /* mixed path: run every cell through the general
+                                   (table-driven) kernel instead of the brick
+                                   kernel; results are bit-identical */
+
 /* RK schemes = stage lists of RK(irk) (RK.c:16-47) */
 #define FVGPU_SCHEME_EULER 1   /* RK(0), RK(1) */
 #define FVGPU_SCHEME_SSPRK2 2  /* RK(0), RK(1), RK(4) */
@@ -83,7 +88,7 @@ typedef struct fvgpu_config {
   int eos;         /* 1 = viscous work term in the energy flux (flux_viscous.c:227) */
   int precision;   /* FVGPU_FP64 or FVGPU_MIXED */
   int device;      /* CUDA device ordinal */
-  int reserved0;
+  int flags;       /* FVGPU_FLAG_* */
   double gamma;    /* PAR.matergama[0] */
   double pinf;     /* PAR.materpinf[0] */
   double visc;     /* PAR.matervisc[0] */
