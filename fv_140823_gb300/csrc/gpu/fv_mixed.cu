@@ -333,6 +333,33 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
   return acc * geo->inv2vol[lev];
 }
 
+// Exact FP32 -> FP64 and round-to-nearest FP64 -> FP32 conversions on the
+// integer pipe (the hardware conversions run on GB300's slow FP64 pipe);
+// zero, subnormal, infinite and NaN values take the hardware path.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u)
+    return __longlong_as_double(static_cast<long long>((uint64_t(b & 0x80000000u) << 32) |
+                                                       (uint64_t(e + 896u) << 52) | (uint64_t(b & 0x7fffffu) << 29)));
+  if ((b << 1) == 0u) return __longlong_as_double(static_cast<long long>(uint64_t(b) << 32));
+  return double(x);
+}
+__device__ __forceinline__ float d2f_rn(double x) {
+  const uint64_t d = static_cast<uint64_t>(__double_as_longlong(x));
+  const uint32_t hi = uint32_t(d >> 32), lo = uint32_t(d);
+  const int e = int((hi >> 20) & 0x7ffu) - 896;
+  if (e >= 1 && e <= 254) {
+    const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    uint32_t r = (hi & 0x80000000u) | (uint32_t(e) << 23) | m;
+    const uint32_t rem = lo & 0x1fffffffu, half = 0x10000000u;
+    if (rem > half || (rem == half && (m & 1u))) r += 1u;
+    return __uint_as_float(r);
+  }
+  if ((d << 1) == 0u) return __uint_as_float(hi);
+  return __double2float_rn(x);
+}
+
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
 // CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
 __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageArgs &a, int c, int32_t g,
@@ -361,9 +388,9 @@ __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageA
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
       if (v >= neq) break;
-      const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
+      const double snew = __ldg(a.SN + v * n + c) + f2d_exact(dn[v]);
       a.SNout[v * n + c] = snew;
-      qn[v] = __double2float_rn(snew);
+      qn[v] = d2f_rn(snew);
       a.SNfout[v * n + c] = qn[v];
     }
     return a.lambda ? cell_lambda_f(mc, a.geo, g, qn) : 0.0f;
@@ -577,7 +604,10 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
 
 // ============================= brick kernel =================================
 
-__device__ __forceinline__ int tile_index(int x, int y, int z) { return ((z + 2) * TY + (y + 2)) * TX + (x + 2); }
+__host__ __device__ constexpr int tile_index(int x, int y, int z) { return ((z + 2) * TY + (y + 2)) * TX + (x + 2); }
+__host__ __device__ constexpr bool in_brick(int x, int y, int z) {
+  return x >= 0 && x < BX && y >= 0 && y < BY && z >= 0 && z < BZ;
+}
 __device__ __forceinline__ int morton_local(int x, int y, int z) {
   return (x & 1) | ((y & 1) << 1) | ((z & 1) << 2) | (((x >> 1) & 1) << 3) | (((y >> 1) & 1) << 4) |
          (((z >> 1) & 1) << 5) | (((x >> 2) & 1) << 6) | (((y >> 2) & 1) << 7);
@@ -587,77 +617,63 @@ __device__ __forceinline__ void morton_decode(int t, int &x, int &y, int &z) {
   y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
   z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
 }
+// bit f set when a brick cell lies on the brick's face-f side (0 for halo cells)
+__host__ __device__ constexpr uint32_t edge_mask(int x, int y, int z) {
+  if (!in_brick(x, y, z)) return 0u;
+  return (y == 0 ? 1u : 0u) | (x == BX - 1 ? 2u : 0u) | (y == BY - 1 ? 4u : 0u) | (x == 0 ? 8u : 0u) |
+         (z == 0 ? 16u : 0u) | (z == BZ - 1 ? 32u : 0u);
+}
 
-// halo cell h (0..511) of the brick: its tile coordinates, the side (face
-// index) it belongs to, its layer (1 = adjacent, 2 = second) and its local
-// coordinates inside the neighbour brick
-__device__ __forceinline__ void halo_cell(int h, int &x, int &y, int &z, int &side, int &layer, int &lx, int &ly,
-                                          int &lz) {
-  if (h < 4 * BY * BZ) {  // x sides: 2 sides x 2 layers x BY x BZ
-    const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ);
-    layer = 1 + r / (BY * BZ);
-    const int rr = r % (BY * BZ);
-    y = rr % BY;
-    z = rr / BY;
-    side = s == 0 ? 3 : 1;
-    x = s == 0 ? -layer : BX - 1 + layer;
-    lx = s == 0 ? BX - layer : layer - 1;
-    ly = y;
-    lz = z;
-  } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
-    const int hh = h - 4 * BY * BZ;
-    const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ);
-    layer = 1 + r / (BX * BZ);
-    const int rr = r % (BX * BZ);
-    x = rr % BX;
-    z = rr / BX;
-    side = s == 0 ? 0 : 2;
-    y = s == 0 ? -layer : BY - 1 + layer;
-    ly = s == 0 ? BY - layer : layer - 1;
-    lx = x;
-    lz = z;
-  } else {
-    const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
-    const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY);
-    layer = 1 + r / (BX * BY);
-    const int rr = r % (BX * BY);
-    x = rr % BX;
-    y = rr / BX;
-    side = s == 0 ? 4 : 5;
-    z = s == 0 ? -layer : BZ - 1 + layer;
-    lz = s == 0 ? BZ - layer : layer - 1;
-    lx = x;
-    ly = y;
+// Face tasks of a brick: x faces (lower x = -1..7), then y, then z.  Packed:
+// tile index of the lower cell (11 bits), axis (2), lower / upper cell inside
+// the brick (1 + 1), edge masks of the lower and upper cells (6 + 6).
+struct BrickTasks {
+  uint32_t task[kFaces];
+};
+constexpr BrickTasks make_brick_tasks() {
+  BrickTasks T{};
+  for (int task = 0; task < kFaces; ++task) {
+    int axis = 0, lx = 0, ly = 0, lz = 0;
+    if (task < kFacesX) {
+      lx = task % (BX + 1) - 1;
+      ly = (task / (BX + 1)) % BY;
+      lz = task / ((BX + 1) * BY);
+    } else if (task < kFacesX + kFacesY) {
+      const int r = task - kFacesX;
+      axis = 1;
+      lx = r % BX;
+      ly = (r / BX) % (BY + 1) - 1;
+      lz = r / (BX * (BY + 1));
+    } else {
+      const int r = task - kFacesX - kFacesY;
+      axis = 2;
+      lx = r % BX;
+      ly = (r / BX) % BY;
+      lz = r / (BX * BY) - 1;
+    }
+    const int ux = lx + (axis == 0), uy = ly + (axis == 1), uz = lz + (axis == 2);
+    T.task[task] = uint32_t(tile_index(lx, ly, lz)) | (uint32_t(axis) << 11) |
+                   (uint32_t(in_brick(lx, ly, lz)) << 13) | (uint32_t(in_brick(ux, uy, uz)) << 14) |
+                   (edge_mask(lx, ly, lz) << 15) | (edge_mask(ux, uy, uz) << 21);
   }
+  return T;
 }
+__device__ const BrickTasks g_brick_tasks = make_brick_tasks();
 
-// geometry code of a brick-tile cell: same level, boundary relation on the
-// faces that lie on a domain-boundary side of the brick
-__device__ __forceinline__ int32_t brick_geom(const BlockDesc &bd, int x, int y, int z) {
-  int32_t g = bd.level;
-  if (x == 0 && bd.side[3] < 0) g |= kRelBoundary << (5 + 2 * 3);
-  if (x == BX - 1 && bd.side[1] < 0) g |= kRelBoundary << (5 + 2 * 1);
-  if (y == 0 && bd.side[0] < 0) g |= kRelBoundary << (5 + 2 * 0);
-  if (y == BY - 1 && bd.side[2] < 0) g |= kRelBoundary << (5 + 2 * 2);
-  if (z == 0 && bd.side[4] < 0) g |= kRelBoundary << (5 + 2 * 4);
-  if (z == BZ - 1 && bd.side[5] < 0) g |= kRelBoundary << (5 + 2 * 5);
+// geometry code of a brick cell: its level, boundary relation on the faces
+// where it touches a domain-boundary side of the brick
+__device__ __forceinline__ int32_t brick_geom(int level, uint32_t bnd_edges) {
+  int32_t g = level;
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+    if ((bnd_edges >> f) & 1u) g |= kRelBoundary << (5 + 2 * f);
   return g;
-}
-
-__device__ __forceinline__ bool in_brick(int x, int y, int z) {
-  return unsigned(x) < unsigned(BX) && unsigned(y) < unsigned(BY) && unsigned(z) < unsigned(BZ);
-}
-
-// unit step of face f in tile coordinates
-__device__ __forceinline__ void face_step(int f, int &dx, int &dy, int &dz) {
-  dx = f == 1 ? 1 : (f == 3 ? -1 : 0);
-  dy = f == 2 ? 1 : (f == 0 ? -1 : 0);
-  dz = f == 5 ? 1 : (f == 4 ? -1 : 0);
 }
 
 __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs a) {
   __shared__ float tile[kNeqMax][kTile];
   __shared__ float flux[kNeqMax][kFaces];
+  __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
   __shared__ float s_dt;
   const BlockDesc bd = a.blocks[blockIdx.x];
   const int t = threadIdx.x;
@@ -665,8 +681,20 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
   const int neq = mc.neq;
   const bool muscl = mc.ischeme == 2;
   const int c = bd.start + t;
+  uint32_t bmask = 0;  // sides of the brick on the domain boundary
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+    if (bd.side[f] < 0) bmask |= 1u << f;
+  if (t < 12) {
+    const int f = t >> 1, r = t & 1;
+    const float *gf = geo_face(a.geo, bd.level, f, r ? kRelBoundary : kRelSame);
+    s_geo[f][r][0] = gf[0];
+    s_geo[f][r][1] = gf[1];
+    s_geo[f][r][2] = gf[2];
+  }
+  if (t == 0) s_dt = __double2float_rn(*a.dt);
 
-  // A1: the brick's cells and the halo of same-level neighbour bricks
+  // A1: the brick's cells and the halo from the six neighbour bricks
   int x, y, z;
   morton_decode(t, x, y, z);
   float din[kNeqMax];
@@ -685,8 +713,32 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
   }
 #pragma unroll 1
   for (int h = t; h < kHalo; h += kBlock) {
-    int hx, hy, hz, side, layer, lx, ly, lz;
-    halo_cell(h, hx, hy, hz, side, layer, lx, ly, lz);
+    // halo cell h: side, layer and position (x sides, y sides, z sides)
+    int hx, hy, hz, side, lx, ly, lz;
+    if (h < 4 * BY * BZ) {
+      const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ), layer = 1 + r / (BY * BZ), rr = r % (BY * BZ);
+      hy = ly = rr % BY;
+      hz = lz = rr / BY;
+      side = s == 0 ? 3 : 1;
+      hx = s == 0 ? -layer : BX - 1 + layer;
+      lx = s == 0 ? BX - layer : layer - 1;
+    } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
+      const int hh = h - 4 * BY * BZ;
+      const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ), layer = 1 + r / (BX * BZ), rr = r % (BX * BZ);
+      hx = lx = rr % BX;
+      hz = lz = rr / BX;
+      side = s == 0 ? 0 : 2;
+      hy = s == 0 ? -layer : BY - 1 + layer;
+      ly = s == 0 ? BY - layer : layer - 1;
+    } else {
+      const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
+      const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY), layer = 1 + r / (BX * BY), rr = r % (BX * BY);
+      hx = lx = rr % BX;
+      hy = ly = rr / BX;
+      side = s == 0 ? 4 : 5;
+      hz = s == 0 ? -layer : BZ - 1 + layer;
+      lz = s == 0 ? BZ - layer : layer - 1;
+    }
     const int base = bd.side[side];
     if (base >= 0) {
       float q[kNeqMax];
@@ -696,103 +748,113 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
       for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = q[v];
     }
   }
-  if (t == 0) s_dt = __double2float_rn(*a.dt);
   __syncthreads();
-  // A2: ghost values beyond domain-boundary sides (deltavalues.c:9-14)
+  // A2: ghost values beyond domain-boundary sides (deltavalues.c:9-14): the
+  // ghost of the brick cell next to it, in both halo layers
+  if (bmask) {
 #pragma unroll 1
-  for (int h = t; h < kHalo; h += kBlock) {
-    int hx, hy, hz, side, layer, lx, ly, lz;
-    halo_cell(h, hx, hy, hz, side, layer, lx, ly, lz);
-    const int base = bd.side[side];
-    if (base < 0) {
-      int dx, dy, dz;
-      face_step(side, dx, dy, dz);
-      // the brick cell this ghost stands next to
-      const int ix = hx - layer * dx, iy = hy - layer * dy, iz = hz - layer * dz;
-      float own[kNeqMax], gv[kNeqMax];
-      const int ti_own = tile_index(ix, iy, iz);
+    for (int h = t; h < 2 * (BY * BZ + BX * BZ + BX * BY); h += kBlock) {
+      int side, bx, by, bz, sx = 0, sy = 0, sz = 0;
+      if (h < 2 * BY * BZ) {
+        side = h < BY * BZ ? 3 : 1;
+        const int rr = h % (BY * BZ);
+        by = rr % BY;
+        bz = rr / BY;
+        bx = side == 3 ? 0 : BX - 1;
+        sx = side == 3 ? -1 : 1;
+      } else if (h < 2 * BY * BZ + 2 * BX * BZ) {
+        const int hh = h - 2 * BY * BZ;
+        side = hh < BX * BZ ? 0 : 2;
+        const int rr = hh % (BX * BZ);
+        bx = rr % BX;
+        bz = rr / BX;
+        by = side == 0 ? 0 : BY - 1;
+        sy = side == 0 ? -1 : 1;
+      } else {
+        const int hh = h - 2 * BY * BZ - 2 * BX * BZ;
+        side = hh < BX * BY ? 4 : 5;
+        const int rr = hh % (BX * BY);
+        bx = rr % BX;
+        by = rr / BX;
+        bz = side == 4 ? 0 : BZ - 1;
+        sz = side == 4 ? -1 : 1;
+      }
+      if ((bmask >> side) & 1u) {
+        float own[kNeqMax], gv[kNeqMax];
+        const int ti_own = tile_index(bx, by, bz);
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
-      boundary_value(mc, -1 - base, side, own, gv);
-      const int ti = tile_index(hx, hy, hz);
+        for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
+        boundary_value(mc, -1 - bd.side[side], side, own, gv);
+        const int t1 = tile_index(bx + sx, by + sy, bz + sz), t2 = tile_index(bx + 2 * sx, by + 2 * sy, bz + 2 * sz);
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = gv[v];
+        for (int v = 0; v < kNeqMax; ++v) {
+          tile[v][t1] = gv[v];
+          tile[v][t2] = gv[v];
+        }
+      }
     }
   }
   __syncthreads();
+
+  // face value of the face g of the tile cell at ti (edge mask e), with the
+  // values across g at ti + dg and across the opposite face at ti - dg
+  auto recon_tile = [&](int ti, uint32_t e, int g, int dg, float out[kNeqMax]) {
+    float qp[kNeqMax];
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) qp[v] = tile[v][ti];
+    if (!muscl) {
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) out[v] = qp[v];
+      return;
+    }
+    const uint32_t be = e & bmask;
+    const int rg = (be >> g) & 1u, ro = (be >> opp_face(g)) & 1u;
+    const float dcf = s_geo[g][rg][0], inv_p = s_geo[g][rg][1], inv_m = s_geo[opp_face(g)][ro][1];
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) {
+      const float d0 = tile[v][ti + dg] - qp[v];
+      const float d1 = tile[v][ti - dg] - qp[v];
+      float grad = 0.0f;
+      if (!rg && fabsf(d0) > 1e-10f) {
+        const float sp = d0 * inv_p;
+        const float sm = -d1 * inv_m;
+        if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
+      }
+      out[v] = fmaf(dcf, grad, qp[v]);
+    }
+  };
 
   // B: face tasks -- each face of the brick once
   bool ok = true;
 #pragma unroll 1
   for (int task = t; task < kFaces; task += kBlock) {
-    int f, lx, ly, lz;  // lower cell (tile coords) and its + face
-    if (task < kFacesX) {
-      f = 1;
-      lx = task % (BX + 1) - 1;
-      ly = (task / (BX + 1)) % BY;
-      lz = task / ((BX + 1) * BY);
-    } else if (task < kFacesX + kFacesY) {
-      const int r = task - kFacesX;
-      f = 2;
-      lx = r % BX;
-      ly = (r / BX) % (BY + 1) - 1;
-      lz = r / (BX * (BY + 1));
-    } else {
-      const int r = task - kFacesX - kFacesY;
-      f = 5;
-      lx = r % BX;
-      ly = (r / BX) % BY;
-      lz = r / (BX * BY) - 1;
-    }
-    int dx, dy, dz;
-    face_step(f, dx, dy, dz);
-    const int ux = lx + dx, uy = ly + dy, uz = lz + dz;
-    const bool low_in = in_brick(lx, ly, lz), up_in = in_brick(ux, uy, uz);
-    const int fo = opp_face(f);
-    // a face on a domain-boundary side: only the brick cell's side exists
-    const int bside = low_in ? bd.side[f] : bd.side[fo];
-    const bool dom_boundary = !(low_in && up_in) && bside < 0;
+    const uint32_t e = __ldg(&g_brick_tasks.task[task]);
+    const int ti = int(e & 2047u);
+    const int axis = int((e >> 11) & 3u);
+    const bool low_in = (e >> 13) & 1u, up_in = (e >> 14) & 1u;
+    const uint32_t elo = (e >> 15) & 63u, eup = (e >> 21) & 63u;
+    const int st = axis == 0 ? 1 : (axis == 1 ? TX : TX * TY);
+    const int fp = axis == 0 ? 1 : (axis == 1 ? 2 : 5);
+    const int fm = opp_face(fp);
     float Fn[kNeqMax];
-    // face value of (cell P, face g): state and the two values across
-    auto recon_tile = [&](int px, int py, int pz, int g, float out[kNeqMax]) {
-      int gx, gy, gz;
-      face_step(g, gx, gy, gz);
-      const int ip = tile_index(px, py, pz), ia = tile_index(px + gx, py + gy, pz + gz),
-                ib = tile_index(px - gx, py - gy, pz - gz);
-      float qp[kNeqMax], d0[kNeqMax], d1[kNeqMax];
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) {
-        qp[v] = tile[v][ip];
-        d0[v] = tile[v][ia] - qp[v];
-        d1[v] = tile[v][ib] - qp[v];
-      }
-      if (!muscl) {
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) out[v] = qp[v];
-        return;
-      }
-      const int32_t gp = in_brick(px, py, pz) ? brick_geom(bd, px, py, pz) : bd.level;
-      recon_face(a.geo, gp, g, qp, d0, d1, out);
-    };
-    if (dom_boundary) {
-      // the brick cell's own boundary face, own frame (residual_faces_AMR.c:196-209)
-      const int bf = low_in ? f : fo;
-      float own[kNeqMax], dummy[kNeqMax];
+    const int bside = low_in ? fp : fm;
+    if (!(low_in && up_in) && bd.side[bside] < 0) {
+      // the brick cell's own domain-boundary face, own frame (residual_faces_AMR.c:196-209)
+      float own[kNeqMax];
       if (low_in)
-        recon_tile(lx, ly, lz, f, own);
+        recon_tile(ti, elo, fp, st, own);
       else
-        recon_tile(ux, uy, uz, fo, own);
-      const bool fok = canonical_flux(mc, bf, -1 - bside, muscl, own, dummy, Fn);
-      ok &= fok;
-      if (!low_in) {  // stored as the canonical +-face flux of the missing lower cell
+        recon_tile(ti + st, eup, fm, -st, own);
+      ok &= canonical_flux(mc, bside, -1 - bd.side[bside], muscl, own, own, Fn);
+      if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
       }
     } else {
       float lo[kNeqMax], hi[kNeqMax];
-      recon_tile(lx, ly, lz, f, lo);
-      recon_tile(ux, uy, uz, fo, hi);
-      ok &= canonical_flux(mc, f, 0, muscl, lo, hi, Fn);
+      recon_tile(ti, elo, fp, st, lo);
+      recon_tile(ti + st, eup, fm, -st, hi);
+      ok &= canonical_flux(mc, fp, 0, muscl, lo, hi, Fn);
     }
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
@@ -800,27 +862,22 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
   __syncthreads();
 
   // C: gather in the fixed face order, RK stage update
-  const int32_t g = brick_geom(bd, x, y, z);
-  const int lev = bd.level;
+  const uint32_t be = edge_mask(x, y, z) & bmask;
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
+  const int ty_p = kFacesX + z * BX * (BY + 1) + (y + 1) * BX + x;
+  const int tz_p = kFacesX + kFacesY + (z + 1) * BX * BY + y * BX + x;
+  const int task_of[6] = {ty_p - BX, tx_p, ty_p, tx_p - 1, tz_p - BX * BY, tz_p};
 #pragma unroll
   for (int it = 0; it < 6; ++it) {
     const int f = face_of_iter(it);
-    const bool plus = it < 3;
-    const float A = geo_face(a.geo, lev, f, rel_of(g, f))[2];
-    // index of the face task holding this face (lower cell = this cell for + faces)
-    int task;
-    if (f == 1 || f == 3)
-      task = z * (BX + 1) * BY + y * (BX + 1) + (x + (f == 1 ? 1 : 0));
-    else if (f == 2 || f == 0)
-      task = kFacesX + z * BX * (BY + 1) + (y + (f == 2 ? 1 : 0)) * BX + x;
-    else
-      task = kFacesX + kFacesY + (z + (f == 5 ? 1 : 0)) * BX * BY + y * BX + x;
-    const float sA = plus ? -A : A;
+    const float A = s_geo[f][(be >> f) & 1u][2];
+    const float sA = it < 3 ? -A : A;
+    const int task = task_of[f];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, flux[v][task], R[v]);
   }
-  const float lam = stage_update(mc, a, c, g, R, din, s_dt, ok);
+  const float lam = stage_update(mc, a, c, brick_geom(bd.level, be), R, din, s_dt, ok);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
