@@ -236,29 +236,34 @@ __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, i
   const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
   const bool left = r1 || r2;
   const bool star = r2 || r3;
-  const FS &K = left ? L : R;
+  // upwind side K, selected field by field (no reference to either struct)
+  const float Kr = left ? L.r : R.r, Ku = left ? L.u : R.u, Kv = left ? L.v : R.v, Kw = left ? L.w : R.w;
+  const float Ke = left ? L.e : R.e, Kp = left ? L.p : R.p, Ky = left ? L.y : R.y;
+  float Kq[kNeqMax];
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) Kq[v] = left ? L.q[v] : R.q[v];
   const float uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
   const float SK = left ? SL : SR;
-  const float run = K.r * uK;
+  const float run = Kr * uK;
   Fn[0] = run;
-  Fn[1] = fmaf(K.p, nx, run * K.u);
-  Fn[2] = fmaf(K.p, ny, run * K.v);
-  Fn[3] = fmaf(K.p, nz, run * K.w);
-  Fn[4] = mc.model == 1 ? (K.e + K.p) * uK : run * K.y;
+  Fn[1] = fmaf(Kp, nx, run * Ku);
+  Fn[2] = fmaf(Kp, ny, run * Kv);
+  Fn[3] = fmaf(Kp, nz, run * Kw);
+  Fn[4] = mc.model == 1 ? (Ke + Kp) * uK : run * Ky;
   if (star) {
     const float dK = SK - uK;
-    const float cS = __fdividef(K.r * dK, SK - S_S);
+    const float cS = __fdividef(Kr * dK, SK - S_S);
     const float us0 = cS * fmaf(wK, lx, fmaf(vK, mx, S_S * nx));
     const float us1 = cS * fmaf(wK, ly, fmaf(vK, my, S_S * ny));
     const float us2 = cS * fmaf(wK, lz, fmaf(vK, mz, S_S * nz));
     const float us4 = mc.model == 1
-                          ? cS * fmaf(S_S - uK, S_S + __fdividef(K.p, K.r * dK), __fdividef(K.e, K.r))
-                          : cS * K.y;
-    Fn[0] = fmaf(SK, cS - K.q[0], Fn[0]);
-    Fn[1] = fmaf(SK, us0 - K.q[1], Fn[1]);
-    Fn[2] = fmaf(SK, us1 - K.q[2], Fn[2]);
-    Fn[3] = fmaf(SK, us2 - K.q[3], Fn[3]);
-    Fn[4] = fmaf(SK, us4 - K.q[4], Fn[4]);
+                          ? cS * fmaf(S_S - uK, S_S + __fdividef(Kp, Kr * dK), __fdividef(Ke, Kr))
+                          : cS * Ky;
+    Fn[0] = fmaf(SK, cS - Kq[0], Fn[0]);
+    Fn[1] = fmaf(SK, us0 - Kq[1], Fn[1]);
+    Fn[2] = fmaf(SK, us1 - Kq[2], Fn[2]);
+    Fn[3] = fmaf(SK, us2 - Kq[3], Fn[3]);
+    Fn[4] = fmaf(SK, us4 - Kq[4], Fn[4]);
   }
   return ok && (r1 || r2 || r3 || r4);
 }
@@ -675,19 +680,22 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
   __shared__ float flux[kNeqMax][kFaces];
   __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
   __shared__ float s_dt;
-  const BlockDesc bd = a.blocks[blockIdx.x];
+  __shared__ int s_side[6];  // brick sides (indexed at run time: kept out of local memory)
+  const BlockDesc *bdp = a.blocks + blockIdx.x;
   const int t = threadIdx.x;
   const int n = a.n;
   const int neq = mc.neq;
   const bool muscl = mc.ischeme == 2;
-  const int c = bd.start + t;
+  const int start = __ldg(&bdp->start), level = __ldg(&bdp->level);
+  const int c = start + t;
   uint32_t bmask = 0;  // sides of the brick on the domain boundary
 #pragma unroll
   for (int f = 0; f < 6; ++f)
-    if (bd.side[f] < 0) bmask |= 1u << f;
+    if (__ldg(&bdp->side[f]) < 0) bmask |= 1u << f;
+  if (t < 6) s_side[t] = __ldg(&bdp->side[t]);
   if (t < 12) {
     const int f = t >> 1, r = t & 1;
-    const float *gf = geo_face(a.geo, bd.level, f, r ? kRelBoundary : kRelSame);
+    const float *gf = geo_face(a.geo, level, f, r ? kRelBoundary : kRelSame);
     s_geo[f][r][0] = gf[0];
     s_geo[f][r][1] = gf[1];
     s_geo[f][r][2] = gf[2];
@@ -739,7 +747,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
       hz = s == 0 ? -layer : BZ - 1 + layer;
       lz = s == 0 ? BZ - layer : layer - 1;
     }
-    const int base = bd.side[side];
+    const int base = __ldg(&bdp->side[side]);
     if (base >= 0) {
       float q[kNeqMax];
       global_state(mc, a, base + morton_local(lx, ly, lz), q);
@@ -784,7 +792,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
         const int ti_own = tile_index(bx, by, bz);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
-        boundary_value(mc, -1 - bd.side[side], side, own, gv);
+        boundary_value(mc, -1 - s_side[side], side, own, gv);
         const int t1 = tile_index(bx + sx, by + sy, bz + sz), t2 = tile_index(bx + 2 * sx, by + 2 * sy, bz + 2 * sz);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) {
@@ -838,14 +846,14 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
     const int fm = opp_face(fp);
     float Fn[kNeqMax];
     const int bside = low_in ? fp : fm;
-    if (!(low_in && up_in) && bd.side[bside] < 0) {
+    if (!(low_in && up_in) && s_side[bside] < 0) {
       // the brick cell's own domain-boundary face, own frame (residual_faces_AMR.c:196-209)
       float own[kNeqMax];
       if (low_in)
         recon_tile(ti, elo, fp, st, own);
       else
         recon_tile(ti + st, eup, fm, -st, own);
-      ok &= canonical_flux(mc, bside, -1 - bd.side[bside], muscl, own, own, Fn);
+      ok &= canonical_flux(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
       if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
@@ -867,17 +875,20 @@ __global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs
   const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
   const int ty_p = kFacesX + z * BX * (BY + 1) + (y + 1) * BX + x;
   const int tz_p = kFacesX + kFacesY + (z + 1) * BX * BY + y * BX + x;
-  const int task_of[6] = {ty_p - BX, tx_p, ty_p, tx_p - 1, tz_p - BX * BY, tz_p};
-#pragma unroll
-  for (int it = 0; it < 6; ++it) {
-    const int f = face_of_iter(it);
+  // order +x, +y, +z, -x, -y, -z as in the general kernel
+  auto add_face = [&](int f, int task, bool plus) {
     const float A = s_geo[f][(be >> f) & 1u][2];
-    const float sA = it < 3 ? -A : A;
-    const int task = task_of[f];
+    const float sA = plus ? -A : A;
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, flux[v][task], R[v]);
-  }
-  const float lam = stage_update(mc, a, c, brick_geom(bd.level, be), R, din, s_dt, ok);
+  };
+  add_face(1, tx_p, true);
+  add_face(2, ty_p, true);
+  add_face(5, tz_p, true);
+  add_face(3, tx_p - 1, false);
+  add_face(0, ty_p - BX, false);
+  add_face(4, tz_p - BX * BY, false);
+  const float lam = stage_update(mc, a, c, brick_geom(level, be), R, din, s_dt, ok);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
