@@ -675,7 +675,10 @@ __device__ __forceinline__ int32_t brick_geom(int level, uint32_t bnd_edges) {
   return g;
 }
 
-__global__ void __launch_bounds__(kBlock) k_mixed_brick(MixedConst mc, StageArgs a) {
+#ifndef FV_BRICK_MIN_BLOCKS
+#define FV_BRICK_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(MixedConst mc, StageArgs a) {
   __shared__ float tile[kNeqMax][kTile];
   __shared__ float flux[kNeqMax][kFaces];
   __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
