@@ -57,6 +57,17 @@ def build_oracle() -> str:
     return out
 
 
+def build_oracle_ad() -> str:
+    """Compile the scalar-templated restatement (exact JVPs) into
+    oracle/_build/liboracle_ad.so."""
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "liboracle_ad.so")
+    _run(["g++", "-O2", "-std=c++17", "-fno-fast-math", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+          os.path.join(REPO, "include"), os.path.join(HERE, "fvoracle_ad.cpp"), "-o", out])
+    return out
+
+
 def build_ref(ref_root: str = DEFAULT_REF_ROOT) -> str | None:
     """Compile the reference's hot path + harness into oracle/_ref/libfvref.so.
 
@@ -86,6 +97,7 @@ def main(argv: list[str] | None = None) -> int:
     ap.add_argument("--ref-root", default=DEFAULT_REF_ROOT)
     a = ap.parse_args(argv)
     print(build_oracle())
+    print(build_oracle_ad())
     print(build_ref(a.ref_root))
     return 0
 

@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libfvref.so")
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
+ORACLE_AD_LIB = os.path.join(HERE, "_build", "liboracle_ad.so")
 
 # stage lists of the reference's RK(irk) cases (RK.c:16-47)
 SCHEMES = {"ssprk3": (1, 2, 3), "ssprk2": (1, 4), "euler": (1,)}
@@ -297,3 +298,56 @@ class Oracle:
 
     def cfl_dt(self, U, cfl):
         return cfl / self.max_lambda(U)
+
+
+class OracleAD:
+    """Forward-mode (dual number) restatement: exact JVPs of the residual and
+    of RK steps (oracle/fvoracle_ad.cpp), model 1, inviscid."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            if not os.path.isfile(ORACLE_AD_LIB):
+                raise RuntimeError("oracle/_build/liboracle_ad.so is not built")
+            L = C.CDLL(ORACLE_AD_LIB)
+            vp = C.c_void_p
+            L.fvo_ad_residual.argtypes = [vp, vp, vp, vp]
+            L.fvo_ad_jvp.argtypes = [vp, vp, vp, vp, vp, vp]
+            L.fvo_ad_steps_jvp.argtypes = [vp, vp, vp, C.c_int, C.c_double, C.c_int, vp, vp, vp, vp]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, tables, cfg):
+        from fv_140823_gb300.abi import MeshSoaHolder
+        self.L = self.lib()
+        self.cfg = cfg
+        self.ccfg = cfg.to_c()
+        self.mesh = MeshSoaHolder(tables)
+        self.n = tables.ncells
+
+    def residual(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        R = np.empty_like(U)
+        assert self.L.fvo_ad_residual(C.byref(self.ccfg), C.byref(self.mesh.soa), _ptr(U), _ptr(R)) == 0
+        return R
+
+    def jvp(self, U, V):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        R = np.empty_like(U)
+        JV = np.empty_like(U)
+        assert self.L.fvo_ad_jvp(C.byref(self.ccfg), C.byref(self.mesh.soa), _ptr(U), _ptr(V), _ptr(R),
+                                 _ptr(JV)) == 0
+        return R, JV
+
+    def steps_jvp(self, U, V, dt, scheme="ssprk3", nsteps=1):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        S = np.empty_like(U)
+        JV = np.empty_like(U)
+        st = (C.c_int * len(SCHEMES[scheme]))(*SCHEMES[scheme])
+        assert self.L.fvo_ad_steps_jvp(C.byref(self.ccfg), C.byref(self.mesh.soa), st, len(SCHEMES[scheme]),
+                                       float(dt), int(nsteps), _ptr(U), _ptr(V), _ptr(S), _ptr(JV)) == 0
+        return S, JV

@@ -1,0 +1,58 @@
+"""The dual-number restatement (oracle/fvoracle_ad.cpp) against the reference.
+
+With T = double it must reproduce the reference's golden residuals and RK
+steps bit for bit; its tangents must agree with central differences of the
+oracle.  This pins the CPU reference gradient the GPU adjoint is tested
+against.
+"""
+import numpy as np
+import pytest
+
+from fvtest import bits_equal, load_golden
+from pyoracle import Oracle, OracleAD
+
+AD_CASES = ["amr_periodic_first", "amr_periodic_muscl", "inflow_l3", "sod_l3"]
+
+
+@pytest.mark.parametrize("name", AD_CASES)
+def test_ad_residual_and_steps_match_reference_golden(name):
+    t, cfg, z = load_golden(name)
+    ad = OracleAD(t, cfg)
+    U = z["U"]
+    assert bits_equal(ad.residual(U), z["R"])
+    S, JV = ad.steps_jvp(U, np.zeros_like(U), float(z["dt"]), str(z["scheme"]), int(z["nsteps"]))
+    assert bits_equal(S, z["S_out"])
+    assert not np.any(JV)
+
+
+# Sod's piecewise-constant state sits on the minmod kink everywhere (a zero
+# jump takes the |d0| <= 1e-10 branch; any perturbation leaves it), so the
+# residual has no derivative there and central differences are meaningless.
+@pytest.mark.parametrize("name", [c for c in AD_CASES if c != "sod_l3"])
+def test_ad_jvp_matches_central_differences(name):
+    t, cfg, z = load_golden(name)
+    ad, orc = OracleAD(t, cfg), Oracle(t, cfg)
+    U = z["U"]
+    rng = np.random.default_rng(7)
+    V = rng.standard_normal(U.shape) * np.abs(U).mean(axis=1, keepdims=True)
+    R, JV = ad.jvp(U, V)
+    assert bits_equal(R, z["R"])
+    eps = 1e-6
+    fd = (orc.residual(U + eps * V) - orc.residual(U - eps * V)) / (2 * eps)
+    err = np.linalg.norm(JV - fd) / np.linalg.norm(fd)
+    assert err <= 1e-6, err
+
+
+def test_ad_step_tangent_matches_central_differences():
+    t, cfg, z = load_golden("amr_periodic_muscl")
+    ad, orc = OracleAD(t, cfg), Oracle(t, cfg)
+    U, dt = z["U"], float(z["dt"])
+    rng = np.random.default_rng(11)
+    V = rng.standard_normal(U.shape) * np.abs(U).mean(axis=1, keepdims=True)
+    # two steps: in the third a minmod branch of one cell flips within
+    # U +- 1e-6 V, and a difference across a kink is no derivative
+    _, JV = ad.steps_jvp(U, V, dt, "ssprk3", 2)
+    eps = 1e-6
+    fd = (orc.step(U + eps * V, dt, "ssprk3", 2) - orc.step(U - eps * V, dt, "ssprk3", 2)) / (2 * eps)
+    err = np.linalg.norm(JV - fd) / np.linalg.norm(fd)
+    assert err <= 1e-6, err
