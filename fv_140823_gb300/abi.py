@@ -39,7 +39,7 @@ FIELD_RHS = 2
 FIELD_SF = 3
 FIELD_SG = 4
 HANG0 = -16
-KIND_NAMES = ("faceinterp", "gradcalc", "residual", "rk", "dt", "mixed_stage", "mixed_aux", "unused")
+KIND_NAMES = ("faceinterp", "gradcalc", "residual", "rk", "dt", "mixed_stage", "mixed_aux", "adjoint")
 NKINDS = 8
 
 

@@ -1,0 +1,487 @@
+// fvbuild: -fmad=false
+//
+// Adjoint (vector-Jacobian product) of the FP64 residual:  g = (dR/dU)^T w.
+//
+// The residual of cell c is a sum over its faces f and sub-faces s of
+//   -A_{f,s} Phi(SF_c[f], SF_k[nf]; frame f)          (residual_faces_AMR.c)
+// with Phi the HLLC normal flux (hllc_euler.c / compute_wave_speeds.c /
+// star_region_euler.c / flux_adv.c) and SF the minmod face values
+// (faceinterp.c / reconctruct_V3.c).  The transpose is taken by hand, in
+// three gather passes (one thread per cell, fixed order: deterministic, no
+// atomics):
+//   1. k_adj_flux   reverse of every flux evaluation the cell makes: the
+//                   adjoint of its own face value is summed into gL, the one
+//                   of the neighbour's face value is stored per evaluation
+//                   (gR for a single neighbour, gRh for a 1:4 sub-face);
+//   2. k_adj_gsf    adjoint of each face value SF_c[f] = gL + the neighbour
+//                   evaluations that read it;
+//   3. k_adj_recon  reverse of the reconstruction: own face values and the
+//                   face values of the neighbours whose stencil holds c.
+// Forward quantities (states, wave speeds, HLLC region, limiter branch) are
+// recomputed with the same expressions as the forward kernels, so branch
+// decisions match the forward residual exactly.  Scope: model 1, inviscid,
+// first order or MUSCL/minmod, boundary codes other than the walls 3 and 4
+// (inflow 1, transmissive 2), 1:4 faces, periodic meshes.
+#include "fv_adjoint.cuh"
+
+#include <cstdio>
+
+namespace fv {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int NV = 5;
+
+struct St {
+  double r, ux, uy, uz, e, eint, p, c;
+};
+
+// forward face state, model 1 (facevalues.c / facercnstr.c)
+__device__ __forceinline__ void fwd_state(const Phys &ph, const double q[NV], St &s) {
+  s.r = q[0];
+  s.ux = q[1] / s.r;
+  s.uy = q[2] / s.r;
+  s.uz = q[3] / s.r;
+  s.e = q[4];
+  s.eint = (s.e / s.r) - 0.5 * (s.ux * s.ux + s.uy * s.uy + s.uz * s.uz);
+  s.p = s.r * (ph.gamma - 1.0) * s.eint - ph.gamma * ph.pinf;
+  s.c = sqrt(ph.gamma * (s.p + ph.pinf) / s.r);
+}
+
+// reverse of fwd_state: (rb, uxb, uyb, uzb, eb, pb, cb) -> qb (accumulated)
+__device__ __forceinline__ void rev_state(const Phys &ph, const double q[NV], const St &s, double rb, double uxb,
+                                          double uyb, double uzb, double eb, double pb, double cb, double qb[NV]) {
+  // c = sqrt(X), X = gamma (p + pinf) / r
+  const double X = ph.gamma * (s.p + ph.pinf) / s.r;
+  const double Xb = cb / (2.0 * s.c);
+  pb += Xb * ph.gamma / s.r;
+  rb -= Xb * X / s.r;
+  // p = r (gamma - 1) eint - gamma pinf
+  rb += pb * (ph.gamma - 1.0) * s.eint;
+  const double eintb = pb * s.r * (ph.gamma - 1.0);
+  // eint = e / r - 0.5 |u|^2
+  eb += eintb / s.r;
+  rb -= eintb * s.e / (s.r * s.r);
+  uxb -= eintb * s.ux;
+  uyb -= eintb * s.uy;
+  uzb -= eintb * s.uz;
+  // u = q / r
+  qb[1] += uxb / s.r;
+  qb[2] += uyb / s.r;
+  qb[3] += uzb / s.r;
+  rb -= (uxb * s.ux + uyb * s.uy + uzb * s.uz) / s.r;
+  qb[0] += rb;
+  qb[4] += eb;
+  (void)q;
+}
+
+// Reverse of the HLLC normal flux Phi = F(U_K).n + S_K (U*_K - U_K) of face
+// frame f: given Phib, accumulate qLb and qRb.
+__device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], const double qR[NV],
+                         const double Phib[NV], double qLb[NV], double qRb[NV]) {
+  const double *fr = ph.frames + 9 * f;
+  const double nx = fr[0], ny = fr[1], nz = fr[2], mx = fr[3], my = fr[4], mz = fr[5], lx = fr[6], ly = fr[7],
+               lz = fr[8];
+  St L, R;
+  fwd_state(ph, qL, L);
+  fwd_state(ph, qR, R);
+  const double uL = L.ux * nx + L.uy * ny + L.uz * nz;
+  const double vL = L.ux * mx + L.uy * my + L.uz * mz;
+  const double wL = L.ux * lx + L.uy * ly + L.uz * lz;
+  const double uR = R.ux * nx + R.uy * ny + R.uz * nz;
+  const double vR = R.ux * mx + R.uy * my + R.uz * mz;
+  const double wR = R.ux * lx + R.uy * ly + R.uz * lz;
+  const double ruL = L.r * uL, ruR = R.r * uR;
+  const double a1 = uL + L.c, a2 = uR + R.c, b1 = uL - L.c, b2 = uR - R.c;
+  const bool sr_left = a1 > a2, sl_left = b1 < b2;  // max / min of compute_wave_speeds.c:53-54
+  const double SR = sr_left ? a1 : a2;
+  const double SL = sl_left ? b1 : b2;
+  const double nn = rotate_s11(nx, ny, nz, 1.0);  // d s11 / d p
+  const double s11L = rotate_s11(nx, ny, nz, L.p), s11R = rotate_s11(nx, ny, nz, R.p);
+  const double num = (L.r * (uL * uL) + s11L) - (R.r * (uR * uR) + s11R) - (SL * ruL) + (SR * ruR);
+  const double den = ruL - ruR - (SL * L.r) + (SR * R.r);
+  double SS = num / den;
+  const bool ss_const = bc == 3;
+  if (ss_const) SS = 0.0;
+  const bool r1 = 0.0 <= SL;
+  const bool r2 = !r1 && (SL <= 0.0) && (0.0 <= SS);
+  const bool r3 = !r1 && !r2 && (SS <= 0.0) && (0.0 <= SR);
+  const bool left = r1 || r2, star = r2 || r3;
+  const St &K = left ? L : R;
+  const double *qK = left ? qL : qR;
+  const double uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
+  const double SK = left ? SL : SR;
+
+  // bars of K-side quantities
+  double rKb = 0, uxKb = 0, uyKb = 0, uzKb = 0, eKb = 0, pKb = 0, uKb = 0, vKb = 0, wKb = 0, SKb = 0, SSb = 0;
+  double qKb[NV] = {0, 0, 0, 0, 0};
+  // F(U_K).n: [r uK, r ux uK + p nx, r uy uK + p ny, r uz uK + p nz, uK (e + p)]
+  {
+    const double run = K.r * uK;
+    const double runb = Phib[0] + Phib[1] * K.ux + Phib[2] * K.uy + Phib[3] * K.uz;
+    uxKb += Phib[1] * run;
+    uyKb += Phib[2] * run;
+    uzKb += Phib[3] * run;
+    pKb += Phib[1] * nx + Phib[2] * ny + Phib[3] * nz + Phib[4] * uK;
+    uKb += Phib[4] * (K.e + K.p);
+    eKb += Phib[4] * uK;
+    rKb += runb * uK;
+    uKb += runb * K.r;
+  }
+  if (star) {
+    const double dK = SK - uK, G = SK - SS;
+    const double Cs = K.r * dK / G;
+    const double T1 = SS * nx + vK * mx + wK * lx, T2 = SS * ny + vK * my + wK * ly,
+                 T3 = SS * nz + vK * mz + wK * lz;
+    const double Z = K.p / (K.r * dK);
+    const double X = SS - uK, Y = SS + Z;
+    const double E = (K.e / K.r) + X * Y;
+    const double Us[NV] = {Cs, Cs * T1, Cs * T2, Cs * T3, Cs * E};
+    double Usb[NV];
+    for (int i = 0; i < NV; ++i) {  // FH = SK (Us - qK)
+      SKb += Phib[i] * (Us[i] - qK[i]);
+      Usb[i] = SK * Phib[i];
+      qKb[i] -= SK * Phib[i];
+    }
+    double Cb = Usb[0] + Usb[1] * T1 + Usb[2] * T2 + Usb[3] * T3 + Usb[4] * E;
+    const double T1b = Cs * Usb[1], T2b = Cs * Usb[2], T3b = Cs * Usb[3];
+    SSb += T1b * nx + T2b * ny + T3b * nz;
+    vKb += T1b * mx + T2b * my + T3b * mz;
+    wKb += T1b * lx + T2b * ly + T3b * lz;
+    const double Eb = Cs * Usb[4];
+    eKb += Eb / K.r;
+    rKb -= Eb * K.e / (K.r * K.r);
+    const double Xb = Eb * Y, Yb = Eb * X;
+    SSb += Xb + Yb;
+    uKb -= Xb;
+    const double Zb = Yb;
+    pKb += Zb / (K.r * dK);
+    rKb -= Zb * Z / K.r;
+    double dKb = -Zb * Z / dK;
+    // Cs = r dK / G
+    rKb += Cb * dK / G;
+    dKb += Cb * K.r / G;
+    const double Gb = -Cb * Cs / G;
+    SKb += Gb;
+    SSb -= Gb;
+    SKb += dKb;
+    uKb -= dKb;
+  }
+  // map the K-side bars to L / R
+  double rLb = 0, uxLb = 0, uyLb = 0, uzLb = 0, eLb = 0, pLb = 0, cLb = 0;
+  double rRb = 0, uxRb = 0, uyRb = 0, uzRb = 0, eRb = 0, pRb = 0, cRb = 0;
+  double uLb = 0, vLb = 0, wLb = 0, uRb = 0, vRb = 0, wRb = 0, SLb = 0, SRb = 0;
+  if (left) {
+    rLb += rKb; uxLb += uxKb; uyLb += uyKb; uzLb += uzKb; eLb += eKb; pLb += pKb;
+    uLb += uKb; vLb += vKb; wLb += wKb; SLb += SKb;
+    for (int i = 0; i < NV; ++i) qLb[i] += qKb[i];
+  } else {
+    rRb += rKb; uxRb += uxKb; uyRb += uyKb; uzRb += uzKb; eRb += eKb; pRb += pKb;
+    uRb += uKb; vRb += vKb; wRb += wKb; SRb += SKb;
+    for (int i = 0; i < NV; ++i) qRb[i] += qKb[i];
+  }
+  // S* = num / den (a constant on a slip face)
+  if (!ss_const) {
+    const double numb = SSb / den, denb = -SSb * num / (den * den);
+    // num = (rL uL^2 + s11L) - (rR uR^2 + s11R) - SL ruL + SR ruR
+    rLb += numb * uL * uL;
+    uLb += numb * 2.0 * L.r * uL;
+    pLb += numb * nn;
+    rRb -= numb * uR * uR;
+    uRb -= numb * 2.0 * R.r * uR;
+    pRb -= numb * nn;
+    SLb -= numb * ruL;
+    SRb += numb * ruR;
+    double ruLb = -numb * SL, ruRb = numb * SR;
+    // den = ruL - ruR - SL rL + SR rR
+    ruLb += denb;
+    ruRb -= denb;
+    SLb -= denb * L.r;
+    rLb -= denb * SL;
+    SRb += denb * R.r;
+    rRb += denb * SR;
+    rLb += ruLb * uL;
+    uLb += ruLb * L.r;
+    rRb += ruRb * uR;
+    uRb += ruRb * R.r;
+  }
+  // SL = min(uL - cL, uR - cR), SR = max(uL + cL, uR + cR)
+  if (sl_left) { uLb += SLb; cLb -= SLb; } else { uRb += SLb; cRb -= SLb; }
+  if (sr_left) { uLb += SRb; cLb += SRb; } else { uRb += SRb; cRb += SRb; }
+  // frame rotations
+  uxLb += uLb * nx + vLb * mx + wLb * lx;
+  uyLb += uLb * ny + vLb * my + wLb * ly;
+  uzLb += uLb * nz + vLb * mz + wLb * lz;
+  uxRb += uRb * nx + vRb * mx + wRb * lx;
+  uyRb += uRb * ny + vRb * my + wRb * ly;
+  uzRb += uRb * nz + vRb * mz + wRb * lz;
+  rev_state(ph, qL, L, rLb, uxLb, uyLb, uzLb, eLb, pLb, cLb, qLb);
+  rev_state(ph, qR, R, rRb, uxRb, uyRb, uzRb, eRb, pRb, cRb, qRb);
+}
+
+__device__ __forceinline__ void load5(const double *__restrict__ A, int64_t n, int64_t c, double q[NV]) {
+#pragma unroll
+  for (int v = 0; v < NV; ++v) q[v] = A[v * n + c];
+}
+
+// value across face f of cell x (deltavalues.c), as the forward computes it
+__device__ __forceinline__ void across(const Phys &ph, const MeshView &m, const double *__restrict__ U, int64_t x,
+                                       int f, const double own[NV], double nb[NV]) {
+  const int64_t n = m.n;
+  const int32_t code = m.nbr[f * n + x];
+  if (code >= 0) {
+    load5(U, n, code, nb);
+  } else if (is_hanging(code)) {
+    const int32_t *k = m.hang_nbr + 4 * hang_index(code);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nb[v] = 0.0;
+    for (int s = 0; s < 4; ++s) {
+      const int64_t ks = k[s];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) nb[v] += U[v * n + ks] / ((double)4);
+    }
+  } else if (-1 - code == 1) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nb[v] = ph.inflow[v];
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nb[v] = own[v];
+  }
+}
+
+// Derivatives of the minmod face value SF = q + dcf grad of face g with
+// respect to q, the value across g (a) and the value across the opposite face
+// (b), per variable (reconctruct_V3.c:17-43).
+__device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g, const double q[NV],
+                                            const double na[NV], const double nb[NV], double dq[NV], double da[NV],
+                                            double db[NV]) {
+  const int64_t n = m.n;
+  const int go = opp_face(g);
+  const double dcf = m.dcf[g * n + x], dcc_p = m.dcc[g * n + x], dcc_m = m.dcc[go * n + x];
+  const bool bcf = is_boundary(m.nbr[g * n + x]);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    dq[v] = 1.0;
+    da[v] = 0.0;
+    db[v] = 0.0;
+    if (bcf) continue;
+    const double d0 = na[v] - q[v], d1 = nb[v] - q[v];
+    if (!(fabs(d0) > 1e-10)) continue;
+    const double product = (-d1 / dcc_m) * (d0 / dcc_p);
+    if (!(product > 0.0)) continue;
+    if (fabs(-d1 / dcc_m) > fabs(d0 / dcc_p)) {  // grad = d0 / dcc_p
+      dq[v] -= dcf / dcc_p;
+      da[v] = dcf / dcc_p;
+    } else {  // grad = -d1 / dcc_m
+      dq[v] += dcf / dcc_m;
+      db[v] = -dcf / dcc_m;
+    }
+  }
+}
+
+// 1. reverse of every flux evaluation of cell c
+__global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArgs a) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const int64_t n = m.n;
+  const bool muscl = ph.ischeme == 2;
+  double w[NV];
+  load5(a.w, n, c, w);
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = m.nbr[f * n + c];
+    const bool boundary = is_boundary(code);
+    const int nsub = is_hanging(code) ? 4 : 1;
+    double qL[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) qL[v] = muscl ? a.SF[(f * NV + v) * n + c] : a.U[v * n + c];
+    double gl[NV] = {0, 0, 0, 0, 0};
+    const int nf = m.nbr_face[f * n + c];
+    for (int s = 0; s < nsub; ++s) {
+      double qR[NV], A;
+      int64_t k = -1;
+      if (boundary) {
+        const int bc = -1 - code;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) qR[v] = bc == 1 ? ph.inflow[v] : qL[v];
+        A = m.area[f * n + c];
+      } else {
+        if (code >= 0) {
+          k = code;
+          A = m.area[f * n + c];
+        } else {
+          const int64_t r = hang_index(code);
+          k = m.hang_nbr[4 * r + s];
+          A = m.hang_area[4 * r + s];
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) qR[v] = muscl ? a.SF[(nf * NV + v) * n + k] : a.U[v * n + k];
+      }
+      double Phib[NV], gr[NV] = {0, 0, 0, 0, 0};
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Phib[v] = -(A)*w[v];
+      hllc_vjp(ph, f, boundary ? -1 - code : 0, qL, qR, Phib, gl, gr);
+      if (boundary) {
+        if (-1 - code != 1)  // every supported code but inflow: ghost = own face value
+#pragma unroll
+          for (int v = 0; v < NV; ++v) gl[v] += gr[v];
+      } else if (code >= 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a.gR[(f * NV + v) * n + c] = gr[v];
+      } else {
+        const int64_t r = hang_index(code);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a.gRh[(r * 4 + s) * NV + v] = gr[v];
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.gL[(f * NV + v) * n + c] = gl[v];
+  }
+}
+
+// 2. adjoint of every face value: own evaluations + neighbour evaluations
+__global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs a) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const int64_t n = m.n;
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = m.nbr[f * n + c];
+    double g[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) g[v] = a.gL[(f * NV + v) * n + c];
+    if (!is_boundary(code)) {
+      const int nf = m.nbr_face[f * n + c];
+      if (code >= 0) {
+        const int32_t back = m.nbr[nf * n + code];
+        if (back >= 0) {  // 1:1 face: the neighbour's single evaluation
+#pragma unroll
+          for (int v = 0; v < NV; ++v) g[v] += a.gR[(nf * NV + v) * n + code];
+        } else {  // the coarse neighbour's 1:4 face: its sub-face that is this cell
+          const int64_t r = hang_index(back);
+          int sub = 0;
+          for (int s = 0; s < 4; ++s)
+            if (m.hang_nbr[4 * r + s] == c) sub = s;
+#pragma unroll
+          for (int v = 0; v < NV; ++v) g[v] += a.gRh[(r * 4 + sub) * NV + v];
+        }
+      } else {  // this cell's 1:4 face: each fine neighbour's evaluation
+        const int32_t *k = m.hang_nbr + 4 * hang_index(code);
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+          for (int v = 0; v < NV; ++v) g[v] += a.gR[(nf * NV + v) * n + k[s]];
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.gSF[(f * NV + v) * n + c] = g[v];
+  }
+  (void)ph;
+}
+
+// 3. reverse of the reconstruction
+__global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjArgs a) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const int64_t n = m.n;
+  double gu[NV] = {0, 0, 0, 0, 0};
+  if (ph.ischeme != 2) {  // first order: every face value is the cell state
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) gu[v] += a.gSF[(f * NV + v) * n + c];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.out[v * n + c] = gu[v];
+    return;
+  }
+  double q[NV];
+  load5(a.U, n, c, q);
+  double acr[6][NV];
+  for (int f = 0; f < 6; ++f) across(ph, m, a.U, c, f, q, acr[f]);
+  // own face values
+  for (int g = 0; g < 6; ++g) {
+    const int go = opp_face(g);
+    double dq[NV], da[NV], db[NV];
+    recon_deriv(m, c, g, q, acr[g], acr[go], dq, da, db);
+    // across a boundary face whose ghost is the cell's own state (every
+    // supported code but inflow) the neighbour value is this cell
+    const bool bnd_a = is_boundary(m.nbr[g * n + c]) && -1 - m.nbr[g * n + c] != 1;
+    const bool bnd_b = is_boundary(m.nbr[go * n + c]) && -1 - m.nbr[go * n + c] != 1;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double gs = a.gSF[(g * NV + v) * n + c];
+      gu[v] += gs * dq[v];
+      if (bnd_a) gu[v] += gs * da[v];  // transmissive ghost across g is this cell
+      if (bnd_b) gu[v] += gs * db[v];
+    }
+  }
+  // face values of neighbours whose stencil holds this cell
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = m.nbr[f * n + c];
+    if (is_boundary(code)) continue;
+    const int gk = m.nbr_face[f * n + c];  // the neighbour's face toward this cell
+    const int nk = is_hanging(code) ? 4 : 1;
+    for (int s = 0; s < nk; ++s) {
+      const int64_t k = is_hanging(code) ? int64_t(m.hang_nbr[4 * hang_index(code) + s]) : int64_t(code);
+      // this cell counts 1/4 when the neighbour's face is a 1:4 face
+      const double wgt = is_hanging(m.nbr[gk * n + k]) ? 0.25 : 1.0;
+      double qk[NV], ak[NV], bk[NV];
+      load5(a.U, n, k, qk);
+      across(ph, m, a.U, k, gk, qk, ak);
+      across(ph, m, a.U, k, opp_face(gk), qk, bk);
+      double dq[NV], da[NV], db[NV];
+      // SF_k[gk]: this cell is across gk (the "a" side)
+      recon_deriv(m, k, gk, qk, ak, bk, dq, da, db);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) gu[v] += wgt * a.gSF[(gk * NV + v) * n + k] * da[v];
+      // SF_k[opp gk]: this cell is across the opposite face (the "b" side)
+      recon_deriv(m, k, opp_face(gk), qk, bk, ak, dq, da, db);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) gu[v] += wgt * a.gSF[(opp_face(gk) * NV + v) * n + k] * db[v];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.out[v * n + c] = gu[v];
+}
+
+// w = coef * dt / V * g (the residual weight of a stage's adjoint)
+__global__ void k_adj_scale(MeshView m, const double *__restrict__ g, const double *__restrict__ dt, double coef,
+                            double *__restrict__ w) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const double s = coef * *dt / m.vol[c];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) w[v * m.n + c] = s * g[v * m.n + c];
+}
+
+// y = alpha * x + beta * y (all variables)
+__global__ void k_adj_axpby(int64_t count, double alpha, const double *__restrict__ x, double beta,
+                            double *__restrict__ y) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = alpha * x[i] + beta * y[i];
+}
+
+unsigned grid_of(int64_t n) { return unsigned((n + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+bool adjoint_supported(const Phys &ph, char *why, size_t whylen) {
+  if (ph.model != 1 || ph.ns != 0) {
+    snprintf(why, whylen, "the adjoint implements model 1 without viscous fluxes");
+    return false;
+  }
+  return true;
+}
+
+void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStream_t st) {
+  k_adj_flux<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_gsf<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_recon<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+}
+
+void launch_adj_scale(const MeshView &m, const double *g, const double *dt, double coef, double *w, cudaStream_t st) {
+  k_adj_scale<<<grid_of(m.n), kBlock, 0, st>>>(m, g, dt, coef, w);
+}
+
+void launch_axpby(int64_t count, double alpha, const double *x, double beta, double *y, cudaStream_t st) {
+  k_adj_axpby<<<1024, 256, 0, st>>>(count, alpha, x, beta, y);
+}
+
+}  // namespace fv

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "fv_adjoint.cuh"
 #include "fv_kernels.cuh"
 #include "fv_mixed.cuh"
 #include "fvgpu.h"
@@ -85,6 +86,11 @@ struct fvgpu_ctx {
   fv::MixedResources mixed;
   bool mixed_ok = false;
   std::string mixed_why;
+  // adjoint work arrays (allocated by the first adjoint call)
+  unsigned bc_mask = 0;  // bit b set when boundary code b occurs in the mesh
+  DevBuf adjL, adjR, adjRh, adjW, adjG, adjAcc, adjOut, adjY1, adjY2, adjSN, adjCK;
+  int64_t adj_ck_steps = 0;
+  bool adj_ready = false;
   fv::LaunchMarks marks;
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, int> graph_launches;  // kernels per captured step
@@ -491,6 +497,108 @@ int ensure_lambda(fvgpu_ctx *ctx) {
   return FVGPU_OK;
 }
 
+// ---- adjoint ---------------------------------------------------------------
+
+int ensure_adjoint(fvgpu_ctx *ctx) {
+  char why[256] = {0};
+  if (!fv::adjoint_supported(ctx->ph, why, sizeof why)) return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "%s", why);
+  if (ctx->bc_mask & ((1u << 3) | (1u << 4)))
+    return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "the adjoint does not implement the wall boundary codes 3 and 4");
+  if (ctx->adj_ready) return FVGPU_OK;
+  const size_t cell = sizeof(double) * size_t(ctx->neq) * size_t(ctx->n);
+  FV_CUDA(ctx, ctx->adjL.alloc(6 * cell));
+  FV_CUDA(ctx, ctx->adjR.alloc(6 * cell));
+  FV_CUDA(ctx, ctx->adjRh.alloc(sizeof(double) * 4 * size_t(ctx->neq) * size_t(ctx->nhang)));
+  for (DevBuf *b : {&ctx->adjW, &ctx->adjG, &ctx->adjAcc, &ctx->adjOut, &ctx->adjY1, &ctx->adjY2, &ctx->adjSN})
+    FV_CUDA(ctx, b->alloc(cell));
+  ctx->adj_ready = true;
+  return FVGPU_OK;
+}
+
+// out = (dR/dU)^T w at U (all device arrays [neq][n]); overwrites SF
+int enqueue_vjp(fvgpu_ctx *ctx, const double *U, const double *w, double *out) {
+  const fv::MeshView mv = ctx->view();
+  if (ctx->cfg.ischeme == 2) {
+    ctx->marks.mark(FVGPU_KIND_FACEINTERP);
+    fv::launch_faceinterp_fp64(ctx->ph, mv, U, ctx->SF.as<double>(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  fv::AdjArgs a{};
+  a.U = U;
+  a.SF = ctx->SF.as<double>();
+  a.w = w;
+  a.gL = ctx->adjL.as<double>();
+  a.gR = ctx->adjR.as<double>();
+  a.gRh = ctx->adjRh.as<double>();
+  a.gSF = ctx->adjL.as<double>();  // each face's total replaces its own-evaluation part in place
+  a.out = out;
+  ctx->marks.mark(FVGPU_KIND_ADJOINT);
+  fv::launch_adjoint(ctx->ph, mv, a, ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+// RK stage coefficients: S_out = a SN + b S_in + b dt / V R(S_in) (RK.c:16-47)
+void stage_coef(int irk, double &a, double &b) {
+  switch (irk) {
+    case 2: a = 3.0 / 4.0; b = 1.0 / 4.0; break;
+    case 3: a = 1.0 / 3.0; b = 2.0 / 3.0; break;
+    case 4: a = 1.0 / 2.0; b = 1.0 / 2.0; break;
+    default: a = 0.0; b = 1.0; break;
+  }
+}
+
+const int kSchemeStages[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 4, 0}, {1, 2, 3}};
+
+// forward stage irk from S_in into S_out (out of place), SN in ctx->adjSN
+int enqueue_stage_out_of_place(fvgpu_ctx *ctx, int irk, const double *S_in, double *S_out) {
+  if (ctx->cfg.ischeme == 2) {
+    ctx->marks.mark(FVGPU_KIND_FACEINTERP);
+    fv::launch_faceinterp_fp64(ctx->ph, ctx->view(), S_in, ctx->SF.as<double>(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  fv::ResidualArgs a = residual_args(ctx);
+  a.U = S_in;
+  a.R = nullptr;
+  a.S_out = S_out;
+  a.SN = ctx->adjSN.as<double>();
+  a.irk = irk;
+  ctx->marks.mark(FVGPU_KIND_RESIDUAL);
+  fv::launch_residual_fp64(ctx->ph, ctx->view(), a, ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+// G <- (dS_out/dS_in)^T G for one step from the checkpoint X0 (device, [neq][n])
+int enqueue_step_adjoint(fvgpu_ctx *ctx, int scheme, const double *X0) {
+  const int ns = scheme;  // stages per step: 1, 2, 3
+  const int64_t count = int64_t(ctx->neq) * ctx->n;
+  const double *X[3] = {X0, ctx->adjY1.as<double>(), ctx->adjY2.as<double>()};
+  double *G = ctx->adjG.as<double>(), *Acc = ctx->adjAcc.as<double>();
+  for (int j = 0; j + 1 < ns; ++j) {
+    int rc = enqueue_stage_out_of_place(ctx, kSchemeStages[scheme][j], X[j], const_cast<double *>(X[j + 1]));
+    if (rc) return rc;
+  }
+  FV_CUDA(ctx, cudaMemsetAsync(Acc, 0, sizeof(double) * size_t(count), ctx->stream));
+  for (int j = ns - 1; j >= 0; --j) {
+    double a, b;
+    stage_coef(kSchemeStages[scheme][j], a, b);
+    if (a != 0.0) {
+      fv::launch_axpby(count, a, G, 1.0, Acc, ctx->stream);
+      FV_LAUNCHED(ctx);
+    }
+    fv::launch_adj_scale(ctx->view(), G, ctx->d_dt(), b, ctx->adjW.as<double>(), ctx->stream);
+    FV_LAUNCHED(ctx);
+    int rc = enqueue_vjp(ctx, X[j], ctx->adjW.as<double>(), ctx->adjOut.as<double>());
+    if (rc) return rc;
+    fv::launch_axpby(count, 1.0, ctx->adjOut.as<double>(), b, G, ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  fv::launch_axpby(count, 1.0, Acc, 1.0, G, ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
 }  // namespace
 
 namespace fv {
@@ -607,6 +715,16 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   FV_CUDA(ctx, cudaMemset(ctx->SG.p, 0, ctx->SG.bytes));
   ctx->inner.release();
   ctx->has_inner = false;
+  for (DevBuf *b : {&ctx->adjL, &ctx->adjR, &ctx->adjRh, &ctx->adjW, &ctx->adjG, &ctx->adjAcc, &ctx->adjOut,
+                    &ctx->adjY1, &ctx->adjY2, &ctx->adjSN, &ctx->adjCK})
+    b->release();
+  ctx->adj_ck_steps = 0;
+  ctx->adj_ready = false;
+  ctx->bc_mask = 0;
+  for (int64_t i = 0; i < 6 * n; ++i) {
+    const int32_t code = m->nbr[i];
+    if (code < 0 && code > FVGPU_HANG0) ctx->bc_mask |= 1u << (-1 - code);
+  }
   ctx->n = n;
   ctx->nhang = nh;
   ctx->ph = make_phys(ctx->cfg, neq, m->frames);
@@ -878,10 +996,106 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums) {
 int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld) {
   int rc = ensure_state(ctx);
   if (rc) return rc;
-  (void)w;
-  (void)dJdU;
-  (void)ld;
-  return set_err(ctx, FVGPU_ERR_UNSUPPORTED, "the residual adjoint is not part of this build");
+  if (!w || !dJdU || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad array pointer or leading dimension");
+  cudaSetDevice(ctx->cfg.device);
+  rc = ensure_adjoint(ctx);
+  if (rc) return rc;
+  const size_t row = sizeof(double) * size_t(ctx->n);
+  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjW.p, row, w, sizeof(double) * ld, row, ctx->neq, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  rc = enqueue_vjp(ctx, ctx->S.as<double>(), ctx->adjW.as<double>(), ctx->adjG.as<double>());
+  if (rc) return rc;
+  FV_CUDA(ctx, cudaMemcpy2DAsync(dJdU, sizeof(double) * ld, ctx->adjG.p, row, row, ctx->neq,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int fvgpu_residual_vjp_device(fvgpu_ctx *ctx, const double *w, double *dJdU) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!w || !dJdU) return set_err(ctx, FVGPU_ERR_ARG, "null array");
+  cudaSetDevice(ctx->cfg.device);
+  rc = ensure_adjoint(ctx);
+  if (rc) return rc;
+  return enqueue_vjp(ctx, ctx->S.as<double>(), w, dJdU);
+}
+
+int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const double *gN, double *g0,
+                        int64_t ld) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (scheme < FVGPU_SCHEME_EULER || scheme > FVGPU_SCHEME_SSPRK3 || nsteps < 0 || !(dt > 0.0) ||
+      !std::isfinite(dt))
+    return set_err(ctx, FVGPU_ERR_ARG, "need a scheme, nsteps >= 0 and a finite dt > 0");
+  if (!gN || !g0 || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad array pointer or leading dimension");
+  cudaSetDevice(ctx->cfg.device);
+  rc = ensure_adjoint(ctx);
+  if (rc) return rc;
+  const size_t row = sizeof(double) * size_t(ctx->n);
+  const size_t cell = row * size_t(ctx->neq);
+  if (ctx->adj_ck_steps < nsteps) {
+    FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FV_CUDA(ctx, ctx->adjCK.alloc(cell * size_t(nsteps)));
+    ctx->adj_ck_steps = nsteps;
+  }
+  k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
+  FV_LAUNCHED(ctx);
+  // forward sweep: checkpoint, then the step itself (the FP64 sequence fvgpu_step runs)
+  char *ck = static_cast<char *>(ctx->adjCK.p);
+  for (int k = 0; k < nsteps; ++k) {
+    FV_CUDA(ctx, cudaMemcpyAsync(ck + cell * size_t(k), ctx->S.p, cell, cudaMemcpyDeviceToDevice, ctx->stream));
+    rc = enqueue_step_fp64(ctx, scheme, false);
+    if (rc) return rc;
+  }
+  ctx->mixed.snf_valid = false;
+  ctx->lambda_valid = false;
+  // reverse sweep
+  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjG.p, row, gN, sizeof(double) * ld, row, ctx->neq, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  for (int k = nsteps - 1; k >= 0; --k) {
+    rc = enqueue_step_adjoint(ctx, scheme, reinterpret_cast<const double *>(ck + cell * size_t(k)));
+    if (rc) return rc;
+  }
+  FV_CUDA(ctx, cudaMemcpy2DAsync(g0, sizeof(double) * ld, ctx->adjG.p, row, row, ctx->neq, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int fvgpu_profile_adjoint(fvgpu_ctx *ctx, int reps, double *ms_residual, double *ms_vjp) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (reps <= 0 || !ms_residual || !ms_vjp) return set_err(ctx, FVGPU_ERR_ARG, "need reps > 0 and outputs");
+  cudaSetDevice(ctx->cfg.device);
+  rc = ensure_adjoint(ctx);
+  if (rc) return rc;
+  const size_t cell = sizeof(double) * size_t(ctx->neq) * size_t(ctx->n);
+  // residual weights: the state itself (any dense field exercises every path)
+  FV_CUDA(ctx, cudaMemcpyAsync(ctx->adjW.p, ctx->S.p, cell, cudaMemcpyDeviceToDevice, ctx->stream));
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  for (auto &e : ev) FV_CUDA(ctx, cudaEventCreate(&e));
+  for (int pass = 0; pass < 2 && rc == 0; ++pass) {
+    const int n = pass == 0 ? 1 : reps;
+    if (pass == 1) cudaEventRecord(ev[0], ctx->stream);
+    for (int i = 0; i < n && rc == 0; ++i) {
+      if (ctx->cfg.ischeme == 2) rc = enqueue_faceinterp(ctx);
+      if (!rc && ctx->cfg.ns == 1) rc = enqueue_gradcalc(ctx);
+      if (!rc) rc = enqueue_rhs(ctx, nullptr, 0);
+    }
+    if (pass == 1) cudaEventRecord(ev[1], ctx->stream);
+    for (int i = 0; i < n && rc == 0; ++i)
+      rc = enqueue_vjp(ctx, ctx->S.as<double>(), ctx->adjW.as<double>(), ctx->adjG.as<double>());
+    if (pass == 1) cudaEventRecord(ev[2], ctx->stream);
+  }
+  if (!rc) rc = sync_and_check(ctx);
+  if (!rc) {
+    float t0 = 0.f, t1 = 0.f;
+    cudaEventElapsedTime(&t0, ev[0], ev[1]);
+    cudaEventElapsedTime(&t1, ev[1], ev[2]);
+    *ms_residual = double(t0) / reps;
+    *ms_vjp = double(t1) / reps;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  return rc;
 }
 
 int fvgpu_synchronize(fvgpu_ctx *ctx) {

@@ -172,11 +172,36 @@ class Solver:
         self._call("fvgpu_conservation", _ptr(out))
         return out
 
+    # -- adjoint -------------------------------------------------------------
     def residual_vjp(self, w: np.ndarray) -> np.ndarray:
+        """(dR/dU)^T w at the current state (FP64 residual)."""
         w = np.ascontiguousarray(w, dtype=np.float64)
+        if w.shape != (self.neq, self.n):
+            raise ValueError(f"w must have shape {(self.neq, self.n)}")
         out = np.empty((self.neq, self.n))
         self._call("fvgpu_residual_vjp", _ptr(w), _ptr(out), C.c_int64(self.n))
         return out
+
+    def residual_vjp_device(self, w_ptr: int, out_ptr: int):
+        """(dR/dU)^T w on caller-owned device arrays [neq][ncells], queued on
+        the context's stream (:meth:`stream_handle`)."""
+        self._call("fvgpu_residual_vjp_device", C.c_void_p(w_ptr), C.c_void_p(out_ptr))
+
+    def adjoint_steps(self, gN: np.ndarray, dt: float, scheme="ssprk3", nsteps: int = 1) -> np.ndarray:
+        """Advance the current state nsteps fixed-dt steps (checkpointing each
+        step start) and return (dS_N/dS_0)^T gN."""
+        sc = abi.SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        g = np.array(gN, dtype=np.float64, order="C", copy=True)
+        if g.shape != (self.neq, self.n):
+            raise ValueError(f"gN must have shape {(self.neq, self.n)}")
+        self._call("fvgpu_adjoint_steps", sc, float(dt), int(nsteps), _ptr(g), _ptr(g), C.c_int64(self.n))
+        return g
+
+    def profile_adjoint(self, reps: int = 5) -> tuple[float, float]:
+        """Mean device ms of one residual evaluation and of one adjoint."""
+        a, b = C.c_double(), C.c_double()
+        self._call("fvgpu_profile_adjoint", int(reps), C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def profile_step(self, scheme="ssprk3", dt: float = 0.0, cfl: float = 0.0, nsteps: int = 1):
         """Per-kernel-kind device time (ms) and launch counts of nsteps eager steps."""

@@ -176,9 +176,42 @@ int fvgpu_conservation_noalloc(const double *S, const double *vol, int64_t ncell
                                void *stream);
 
 /* ---- adjoint ----------------------------------------------------------- */
-/* dJdU = (dR/dU)^T w for the residual R(U) of the current state (FP64),
- * w and dJdU host arrays [neq][ld]. */
+/* No reference counterpart: the reference has no derivative code.  These
+ * entry points give the transpose of the FP64 residual and step maps
+ * (residual_faces_AMR.c with hllc_euler.c, faceinterp.c / reconctruct_V3.c,
+ * RK.c), computed by hand-written reverse kernels: deterministic (gathers in a
+ * fixed order, no atomics).  Scope: model 1, ns = 0, first order or MUSCL,
+ * boundary codes other than the walls 3 and 4; other configurations return
+ * FVGPU_ERR_UNSUPPORTED.  Derivatives are those of the branch the forward
+ * takes at the given state (minmod, wave-speed and HLLC-region choices); at a
+ * branch switch they are one-sided. */
+
+/* dJdU = (dR/dU)^T w for the residual R(U) of the current state; w and dJdU
+ * host arrays [neq][ld].  The context's SF field then holds the face values
+ * of the current state. */
 int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld);
+
+/* The same on device arrays [neq][ncells] the caller owns, queued on the
+ * context's stream (fvgpu_get_stream) with no host copy or synchronisation. */
+int fvgpu_residual_vjp_device(fvgpu_ctx *ctx, const double *w, double *dJdU);
+
+/* Multi-step adjoint with one checkpoint per RK step.  From the current
+ * state S_0 it runs nsteps FP64 steps of `scheme` at the fixed time step dt
+ * (dt is a constant of the map, not a function of the state), keeping every
+ * step-start state on the device (nsteps * neq * ncells doubles, grown on
+ * demand and kept for reuse), then sweeps back: each step's stage states are
+ * recomputed from its checkpoint and the stages are reversed.  On return the
+ * current state is S_N, exactly as fvgpu_step(ctx, scheme, dt, 0, nsteps)
+ * leaves it, and g0 = (dS_N/dS_0)^T gN.  gN and g0 are host arrays
+ * [neq][ld]; they may be the same array. */
+int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const double *gN, double *g0,
+                        int64_t ld);
+
+/* Device time of the residual and of its adjoint on the current state: reps
+ * eager launches of each (FP64 face values + residual, then face values +
+ * the three reverse passes), timed with CUDA events on the context's stream
+ * after one untimed round; mean milliseconds per evaluation. */
+int fvgpu_profile_adjoint(fvgpu_ctx *ctx, int reps, double *ms_residual, double *ms_vjp);
 
 /* ---- diagnostics -------------------------------------------------------- */
 /* Kernel kinds reported by fvgpu_profile_step. */
@@ -189,6 +222,7 @@ int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld
 #define FVGPU_KIND_DT 4          /* CFL spectral radius / time step */
 #define FVGPU_KIND_MIXED_STAGE 5 /* mixed path: fused reconstruction + flux + RK stage */
 #define FVGPU_KIND_MIXED_AUX 6   /* mixed path: auxiliary kernels */
+#define FVGPU_KIND_ADJOINT 7     /* residual adjoint (reverse passes) */
 #define FVGPU_NKINDS 8
 /* Run nsteps steps eagerly (no graph) with a CUDA event recorded on the
  * context's stream before every kernel and after the last; ms[k] receives the

@@ -1,0 +1,218 @@
+"""Adjoint of the FP64 residual and of RK steps (hand-written reverse kernels).
+
+Checks, on the GPU through the C ABI:
+  * transposition: <w, J v> from the dual-number oracle (exact forward-mode
+    derivative of the reference arithmetic) equals <J^T w, v> from the GPU
+    adjoint, on the reference's golden meshes (AMR 1:4 faces, periodic,
+    inflow and transmissive boundaries, first order and MUSCL);
+  * the full gradient J^T w against the CPU FP64 reference gradient built
+    column by column from the oracle's tangents;
+  * multi-step adjoints (per-step checkpoints) of Euler / SSP-RK2 / SSP-RK3
+    against the oracle's step tangents, and the state they leave;
+  * a functional J(U^1) = sum_{x > 0.75} p V after one SSP-RK3 step against
+    central differences (h 1e-6) on 64 seeded entries, with kinks flagged;
+  * determinism, the torch.autograd wrappers, unsupported configurations.
+Tolerances: the oracle and the GPU differentiate the same branch of the same
+arithmetic, so they differ by rounding only (relative 1e-11 on dot products
+and 1e-10 on gradients); central differences carry O(h^2) truncation and
+cancellation error (bound stated in the test).
+"""
+import numpy as np
+import pytest
+
+from fv_140823_gb300 import abi, cases
+from fv_140823_gb300.abi import SolverConfig
+from fvtest import bits_equal, load_golden
+from pyoracle import Oracle, OracleAD
+
+pytestmark = pytest.mark.gpu
+
+AD_CASES = ["amr_periodic_first", "amr_periodic_muscl", "inflow_l3", "sod_l3"]
+
+
+def solver(t, cfg):
+    from fv_140823_gb300.solver import Solver
+    return Solver(t, cfg)
+
+
+def scaled_random(rng, U):
+    return rng.standard_normal(U.shape) * np.abs(U).mean(axis=1, keepdims=True)
+
+
+@pytest.mark.parametrize("name", AD_CASES)
+def test_residual_vjp_transposes_oracle_jvp(name):
+    t, cfg, z = load_golden(name)
+    U = z["U"]
+    rng = np.random.default_rng(3)
+    V, W = scaled_random(rng, U), rng.standard_normal(U.shape)
+    _, JV = OracleAD(t, cfg).jvp(U, V)
+    with solver(t, cfg) as s:
+        s.set_state(U)
+        g = s.residual_vjp(W)
+    lhs, rhs = float(np.sum(W * JV)), float(np.sum(g * V))
+    assert abs(lhs - rhs) <= 1e-11 * max(np.abs(W * JV).sum(), 1e-300), (lhs, rhs)
+
+
+@pytest.mark.parametrize("name", ["amr_periodic_muscl", "inflow_l3"])
+def test_residual_vjp_full_gradient_matches_cpu_reference(name):
+    t, cfg, z = load_golden(name)
+    U = z["U"]
+    ad = OracleAD(t, cfg)
+    rng = np.random.default_rng(5)
+    W = rng.standard_normal(U.shape)
+    ref = np.empty(U.size)
+    E = np.zeros(U.size)
+    for i in range(U.size):  # column i of J, dotted with w
+        E[i] = 1.0
+        ref[i] = np.sum(W * ad.jvp(U, E.reshape(U.shape))[1])
+        E[i] = 0.0
+    with solver(t, cfg) as s:
+        s.set_state(U)
+        g = s.residual_vjp(W)
+    err = np.abs(g.ravel() - ref).max() / np.abs(ref).max()
+    assert err <= 1e-10, err
+
+
+@pytest.mark.parametrize("name,scheme", [("amr_periodic_muscl", "ssprk3"), ("amr_periodic_first", "ssprk2"),
+                                         ("inflow_l3", "euler"), ("amr_periodic_muscl", "ssprk2"),
+                                         ("sod_l3", "ssprk3")])
+def test_adjoint_steps_transposes_oracle_step_tangent(name, scheme):
+    t, cfg, z = load_golden(name)
+    U, dt, nsteps = z["U"], float(z["dt"]), 3
+    rng = np.random.default_rng(9)
+    V, G = scaled_random(rng, U), rng.standard_normal(U.shape)
+    S_ref, JV = OracleAD(t, cfg).steps_jvp(U, V, dt, scheme, nsteps)
+    with solver(t, cfg) as s:
+        s.set_state(U)
+        g0 = s.adjoint_steps(G, dt, scheme, nsteps)
+        S_after = s.state()
+    assert bits_equal(S_after, S_ref)  # the forward sweep is the FP64 step, bit for bit
+    lhs, rhs = float(np.sum(G * JV)), float(np.sum(g0 * V))
+    assert abs(lhs - rhs) <= 1e-11 * max(np.abs(G * JV).sum(), 1e-300), (lhs, rhs)
+
+
+def _pressure_functional(t, gamma):
+    mask = t.centroid[0] > 0.75
+    vol = t.vol
+
+    def J(S):
+        r, m, E = S[0], S[1:4], S[4]
+        p = (gamma - 1.0) * (E - 0.5 * (m * m).sum(axis=0) / r)
+        return float(np.sum((p * vol)[mask]))
+
+    def dJ(S):
+        r, m, E = S[0], S[1:4], S[4]
+        g = np.zeros_like(S)
+        w = (gamma - 1.0) * vol * mask
+        g[0] = w * 0.5 * (m * m).sum(axis=0) / (r * r)
+        g[1:4] = -w * m / r
+        g[4] = w
+        return g
+    return J, dJ
+
+
+def test_functional_gradient_matches_central_differences():
+    """J = sum_{x > 0.75} p V after one SSP-RK3 step; central differences with
+    the absolute step h = 1e-6 on 64 seeded entries.  The smooth periodic flow
+    is perturbed by 0.1% seeded noise: its symmetric density field puts exact
+    ties between neighbours (a zero jump, the minmod kink) on an 8^3 mesh.
+    Tolerance: 1e-5 |g| plus the rounding bound of the difference quotient,
+    10 u sum|p V| / h; an entry whose one-sided slopes disagree sits at a kink
+    and is counted, not compared."""
+    c = cases.periodic(level=3)
+    t, cfg = c.tables, c.cfg
+    U = c.U * (1.0 + 1e-3 * np.random.default_rng(77).standard_normal(c.U.shape))
+    J, dJ = _pressure_functional(t, cfg.gamma)
+    h, u = 1e-6, 2.0 ** -53
+    with solver(t, cfg) as s:
+        s.set_state(U)
+        dt = s.compute_dt(0.5)
+        s.step("ssprk3", dt=dt, nsteps=1)
+        S1 = s.state()
+        s.set_state(U)
+        g = s.adjoint_steps(dJ(S1), dt, "ssprk3", 1)
+        assert bits_equal(s.state(), S1)
+
+        def Jat(Up):
+            s.set_state(Up)
+            s.step("ssprk3", dt=dt, nsteps=1)
+            return J(s.state())
+
+        J0 = J(S1)
+        r, m, E = S1[0], S1[1:4], S1[4]
+        p_abs = np.abs((cfg.gamma - 1.0) * (E - 0.5 * (m * m).sum(axis=0) / r) * t.vol)
+        noise = 10 * u * float(p_abs[t.centroid[0] > 0.75].sum()) / h
+        gmax = np.abs(g).max()
+        live = np.flatnonzero(np.abs(g).ravel() > 1e-3 * gmax)
+        rng = np.random.default_rng(2024)
+        bad, kinks = [], []
+        for i in rng.choice(live, size=64, replace=False):
+            v, c_ = np.unravel_index(i, U.shape)
+            Up, Um = U.copy(), U.copy()
+            Up[v, c_] += h
+            Um[v, c_] -= h
+            Jp, Jm = Jat(Up), Jat(Um)
+            fd = (Jp - Jm) / (2 * h)
+            fwd, bwd = (Jp - J0) / h, (J0 - Jm) / h
+            if abs(fwd - bwd) > 1e-3 * abs(fd) + 4 * noise:
+                kinks.append(int(i))
+                continue
+            if abs(fd - g[v, c_]) > 1e-5 * abs(g[v, c_]) + noise:
+                bad.append((int(i), fd, g[v, c_]))
+    assert len(kinks) <= 2, kinks
+    assert not bad, bad
+
+
+def test_adjoint_is_deterministic():
+    c = cases.periodic(level=4)
+    rng = np.random.default_rng(1)
+    W = rng.standard_normal(c.U.shape)
+    outs = []
+    for _ in range(2):
+        with solver(c.tables, c.cfg) as s:
+            s.set_state(c.U)
+            outs.append(s.residual_vjp(W))
+            s.set_state(c.U)
+            outs.append(s.adjoint_steps(W, 1e-3, "ssprk3", 2))
+    assert bits_equal(outs[0], outs[2]) and bits_equal(outs[1], outs[3])
+
+
+def test_autograd_wrappers():
+    torch = pytest.importorskip("torch")
+    from fv_140823_gb300.autograd import residual, steps
+    t, cfg, z = load_golden("amr_periodic_muscl")
+    U0, dt = z["U"], float(z["dt"])
+    rng = np.random.default_rng(4)
+    Wt = torch.from_numpy(rng.standard_normal(U0.shape))
+    with solver(t, cfg) as s:
+        U = torch.tensor(U0, requires_grad=True)
+        R = residual(s, U)
+        assert bits_equal(R.detach().numpy(), z["R"])
+        (R * Wt).sum().backward()
+        s.set_state(U0)
+        assert bits_equal(U.grad.numpy(), s.residual_vjp(Wt.numpy()))
+        U = torch.tensor(U0, requires_grad=True)
+        S = steps(s, U, dt, "ssprk3", 2)
+        assert bits_equal(S.detach().numpy(), Oracle(t, cfg).step(U0, dt, "ssprk3", 2))
+        (S * Wt).sum().backward()
+        s.set_state(U0)
+        assert bits_equal(U.grad.numpy(), s.adjoint_steps(Wt.numpy(), dt, "ssprk3", 2))
+
+
+@pytest.mark.parametrize("name", ["tgv_l3", "bubble_l3"])
+def test_adjoint_rejects_unsupported(name):
+    from fv_140823_gb300.solver import FvGpuError
+    t, cfg, z = load_golden(name)
+    with solver(t, cfg) as s:
+        s.set_state(z["U"])
+        with pytest.raises(FvGpuError) as ei:
+            s.residual_vjp(np.ones_like(z["U"]))
+    assert ei.value.code == abi.ERR_UNSUPPORTED
+
+
+def test_adjoint_cost_within_three_residuals():
+    c = cases.periodic(level=6)
+    with solver(c.tables, SolverConfig(**{**c.cfg.__dict__, "precision": abi.FP64})) as s:
+        s.set_state(c.U)
+        ms_res, ms_vjp = s.profile_adjoint(reps=5)
+    assert ms_vjp <= 3.0 * ms_res, (ms_res, ms_vjp)
