@@ -257,6 +257,11 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(hostU.numel() * 8),
                     "d2h_bytes_per_step": int(hostOut.numel() * 8)},
         }
+        if prec == abi.FP64:
+            # hand-written adjoint of the FP64 residual against one residual evaluation
+            s.set_state(case.U)
+            ms_res, ms_vjp = s.profile_adjoint(reps=5)
+            results[prec]["adjoint"] = {"ms_residual": ms_res, "ms_vjp": ms_vjp, "vjp_over_residual": ms_vjp / ms_res}
         s.close()
     err = None
     if abi.MIXED in states and abi.FP64 in states:
@@ -365,6 +370,8 @@ def main():
             line["mixed_over_fp64"] = r["value"] / f["value"]
         elif abi.MIXED in results and "unsupported" in results[abi.MIXED]:
             line["mixed"] = results[abi.MIXED]
+        if "adjoint" in results.get(abi.FP64, {}):
+            line["adjoint"] = results[abi.FP64]["adjoint"]
         if err is not None:
             line["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps, **err}
         if not args.no_cpu_baseline:

@@ -490,6 +490,15 @@ int ensure_mixed_f32(fvgpu_ctx *ctx) {
 int ensure_lambda(fvgpu_ctx *ctx) {
   if (ctx->lambda_valid) return FVGPU_OK;
   FV_CUDA(ctx, cudaMemsetAsync(ctx->d_lambda(), 0, sizeof(double), ctx->stream));
+  if (ctx->cfg.precision == FVGPU_MIXED) {
+    // the mixed path's radius is FP32 (as at the end of its steps); one pass
+    // also rebuilds the FP32 copy of the state
+    const cudaError_t e = fv::mixed_refresh_f32_lambda(ctx->mixed, ctx->ph, ctx->S.as<double>(), ctx->d_lambda(),
+                                                       ctx->marks, ctx->stream);
+    if (e != cudaSuccess) return set_err(ctx, FVGPU_ERR_CUDA, "state copy: %s", cudaGetErrorString(e));
+    ctx->lambda_valid = true;
+    return FVGPU_OK;
+  }
   ctx->marks.mark(FVGPU_KIND_DT);
   fv::launch_lambda_fp64(ctx->ph, ctx->view(), ctx->S.as<double>(), ctx->d_lambda(), ctx->stream);
   FV_LAUNCHED(ctx);
@@ -747,8 +756,12 @@ int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld) {
   if (rc) return rc;
   if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
   cudaSetDevice(ctx->cfg.device);
-  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->S.p, sizeof(double) * ctx->n, U, sizeof(double) * ld,
-                                 sizeof(double) * ctx->n, ctx->neq, cudaMemcpyHostToDevice, ctx->stream));
+  if (ld == ctx->n)  // dense: one linear copy
+    FV_CUDA(ctx, cudaMemcpyAsync(ctx->S.p, U, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  else
+    FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->S.p, sizeof(double) * ctx->n, U, sizeof(double) * ld,
+                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyHostToDevice, ctx->stream));
   ctx->lambda_valid = false;
   ctx->mixed.snf_valid = false;
   return FVGPU_OK;
@@ -759,8 +772,12 @@ int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld) {
   if (rc) return rc;
   if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
   cudaSetDevice(ctx->cfg.device);
-  FV_CUDA(ctx, cudaMemcpy2DAsync(U, sizeof(double) * ld, ctx->S.p, sizeof(double) * ctx->n,
-                                 sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ld == ctx->n)
+    FV_CUDA(ctx, cudaMemcpyAsync(U, ctx->S.p, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  else
+    FV_CUDA(ctx, cudaMemcpy2DAsync(U, sizeof(double) * ld, ctx->S.p, sizeof(double) * ctx->n,
+                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDeviceToHost, ctx->stream));
   return sync_and_check(ctx);
 }
 
@@ -872,11 +889,13 @@ int fvgpu_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int nsteps) {
   if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
   cudaSetDevice(ctx->cfg.device);
   if (nsteps == 0) return FVGPU_OK;
+  if (cfl_mode) {
+    rc = ensure_lambda(ctx);  // mixed: also refreshes the FP32 copy
+    if (rc) return rc;
+  }
   rc = ensure_mixed_f32(ctx);
   if (rc) return rc;
   if (cfl_mode) {
-    rc = ensure_lambda(ctx);
-    if (rc) return rc;
     k_set_double<<<1, 1, 0, ctx->stream>>>(&ctx->d_scal()->cfl, cfl);
   } else {
     k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);
@@ -922,11 +941,13 @@ int fvgpu_profile_step(fvgpu_ctx *ctx, int scheme, double dt, double cfl, int ns
   const bool cfl_mode = !(dt > 0.0);
   if (cfl_mode && !(cfl > 0.0)) return set_err(ctx, FVGPU_ERR_ARG, "dt <= 0 needs cfl > 0");
   cudaSetDevice(ctx->cfg.device);
+  if (cfl_mode) {
+    rc = ensure_lambda(ctx);  // mixed: also refreshes the FP32 copy
+    if (rc) return rc;
+  }
   rc = ensure_mixed_f32(ctx);
   if (rc) return rc;
   if (cfl_mode) {
-    rc = ensure_lambda(ctx);
-    if (rc) return rc;
     k_set_double<<<1, 1, 0, ctx->stream>>>(&ctx->d_scal()->cfl, cfl);
   } else {
     k_set_double<<<1, 1, 0, ctx->stream>>>(ctx->d_dt(), dt);

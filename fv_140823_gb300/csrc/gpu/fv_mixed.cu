@@ -41,6 +41,7 @@
 //
 // Geometry comes from per-level tables (octree-regular meshes): a packed
 // per-cell code (level + face relations) replaces the FP64 face tables.
+#include <algorithm>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -898,7 +899,26 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 // FP32 copy of an FP64 state (after an upload or an FP64-path step).
 __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-    Sf[i] = __double2float_rn(S[i]);
+    Sf[i] = d2f_rn(S[i]);
+}
+
+// The same with the CFL spectral radius of the copied state (the mixed
+// path's first CFL time step after an upload): one cell per thread.
+__global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, const int32_t *__restrict__ geom,
+                                                                const GeoTables *geo, const double *__restrict__ S,
+                                                                float *__restrict__ Sf, int n, double *lambda) {
+  float lam = 0.0f;
+  for (int c = blockIdx.x * kBlock + threadIdx.x; c < n; c += gridDim.x * kBlock) {
+    float q[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) {
+      if (v >= mc.neq) break;
+      q[v] = d2f_rn(S[int64_t(v) * n + c]);
+      Sf[int64_t(v) * n + c] = q[v];
+    }
+    lam = fmaxf(lam, cell_lambda_f(mc, geo, __ldg(geom + c), q));
+  }
+  block_max_lambda_f(lam, lambda);
 }
 
 MixedConst make_const(const Phys &ph) {
@@ -1226,6 +1246,18 @@ void mixed_swap_state(MixedResources &r, void *&state) {
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
   marks.mark(FVGPU_KIND_MIXED_AUX);
   k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) r.snf_valid = true;
+  return e;
+}
+
+cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const double *S, double *lambda,
+                                     LaunchMarks &marks, cudaStream_t st) {
+  marks.mark(FVGPU_KIND_MIXED_AUX);
+  const unsigned blocks = unsigned(std::min<int64_t>((r.n + kBlock - 1) / kBlock, 152 * 8));
+  k_state_to_f32_lambda<<<blocks, kBlock, 0, st>>>(make_const(ph), static_cast<const int32_t *>(r.buf[kBufGeom]),
+                                                   static_cast<const GeoTables *>(r.buf[kBufTables]), S,
+                                                   static_cast<float *>(r.buf[kBufSNf]), int(r.n), lambda);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;

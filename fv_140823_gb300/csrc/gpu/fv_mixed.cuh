@@ -35,6 +35,10 @@ double *mixed_alt_state(MixedResources &r);
 void mixed_swap_state(MixedResources &r, void *&state);
 // rebuild the FP32 copy of the FP64 state S (after uploads / FP64-path updates)
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st);
+// the same, plus the FP32 CFL spectral radius of S max-reduced into *lambda
+// (which the caller zeroes)
+cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const double *S, double *lambda,
+                                     LaunchMarks &marks, cudaStream_t st);
 // One RK step from FP64 state `in` to `out` (distinct buffers).
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,
