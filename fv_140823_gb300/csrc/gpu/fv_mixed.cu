@@ -43,6 +43,7 @@
 // per-cell code (level + face relations) replaces the FP64 face tables.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -139,6 +140,7 @@ __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x);
 __device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
 
 // FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
+template <int MODEL>
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
   s.r = q[0];
   const float rinv = fast_rcp(s.r);
@@ -147,7 +149,7 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
   s.w = q[3] * rinv;
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) s.q[v] = q[v];
-  if (mc.model == 1) {
+  if (MODEL == 1) {
     s.e = q[4];
     const float ke = fmaf(s.w, s.w, fmaf(s.v, s.v, s.u * s.u));
     const float e_int = fmaf(-0.5f, ke, s.e * rinv);
@@ -171,9 +173,10 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
 }
 
 // Boundary ghost (bc.c:19-49) from the own face state.
+template <int MODEL>
 __device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
   if (bc == 1) {
-    mixed_face_state(mc, mc.inflow, false, g);
+    mixed_face_state<MODEL>(mc, mc.inflow, false, g);
   } else if (bc == 3 || bc == 4) {
     const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
     if (bc == 3) {
@@ -193,40 +196,94 @@ __device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f,
 }
 
 // value across a boundary face: the own state, or its ghost (deltavalues.c:9-14)
+template <int MODEL>
 __device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float own[kNeqMax],
                                                float nb[kNeqMax]) {
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
   if (bc == 1 || bc == 3 || bc == 4) {
     FS g;
-    mixed_face_state(mc, own, false, g);
-    mixed_ghost(mc, bc, f, g);
+    mixed_face_state<MODEL>(mc, own, false, g);
+    mixed_ghost<MODEL>(mc, bc, f, g);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
   }
 }
 
-// Normal flux F.n + S_K (U*_K - U_K) through a face of frame f
-// (hllc_euler.c:3-55, compute_wave_speeds.c:3-88, star_region_euler.c:3-40,
-// contracted with n as residual_faces_AMR.c:145-149).
-__device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, int bc, const FS &L, const FS &R,
-                                                  float Fn[kNeqMax]) {
+// Face-local state: the momentum rotated into the face frame (normal n,
+// tangents t1, t2), its velocities, pressure and sound speed.  The mixed
+// path requires orthonormal frames (checked at upload), so the kinetic energy
+// and the stress contraction n.(p I).n = p are frame invariant.
+struct LS {
+  float r, mn, mm, ml, q4;  // density, local momentum, fifth conservative variable
+  float un, um, ul;         // local velocity
+  float p, c, e, y;
+};
+
+template <int MODEL>
+__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float q[kNeqMax], bool clip, LS &s) {
   const float *fr = mc.fr + 9 * f;
-  const float nx = fr[0], ny = fr[1], nz = fr[2];
-  const float mx = fr[3], my = fr[4], mz = fr[5];
-  const float lx = fr[6], ly = fr[7], lz = fr[8];
-  const float uL = fmaf(L.w, nz, fmaf(L.v, ny, L.u * nx));
-  const float vL = fmaf(L.w, mz, fmaf(L.v, my, L.u * mx));
-  const float wL = fmaf(L.w, lz, fmaf(L.v, ly, L.u * lx));
-  const float uR = fmaf(R.w, nz, fmaf(R.v, ny, R.u * nx));
-  const float vR = fmaf(R.w, mz, fmaf(R.v, my, R.u * mx));
-  const float wR = fmaf(R.w, lz, fmaf(R.v, ly, R.u * lx));
-  const float SR = fmaxf(uL + L.c, uR + R.c);
-  const float SL = fminf(uL - L.c, uR - R.c);
-  const float ruL = L.r * uL, ruR = R.r * uR;
-  const float nn = fmaf(nz, nz, fmaf(ny, ny, nx * nx));  // (R st R^T)[0][0] = p |n|^2
-  const float num = fmaf(SR, ruR, fmaf(-SL, ruL, fmaf(ruL, uL, L.p * nn) - fmaf(ruR, uR, R.p * nn)));
-  const float den = fmaf(SR, R.r, fmaf(-SL, L.r, ruL - ruR));
+  s.r = q[0];
+  s.q4 = q[4];
+  s.mn = fmaf(q[3], fr[2], fmaf(q[2], fr[1], q[1] * fr[0]));
+  s.mm = fmaf(q[3], fr[5], fmaf(q[2], fr[4], q[1] * fr[3]));
+  s.ml = fmaf(q[3], fr[8], fmaf(q[2], fr[7], q[1] * fr[6]));
+  const float rinv = fast_rcp(s.r);
+  s.un = s.mn * rinv;
+  s.um = s.mm * rinv;
+  s.ul = s.ml * rinv;
+  if (MODEL == 1) {
+    s.e = q[4];
+    s.y = 0.0f;
+    const float ke = fmaf(s.ul, s.ul, fmaf(s.um, s.um, s.un * s.un));
+    const float e_int = fmaf(-0.5f, ke, s.e * rinv);
+    s.p = fmaf(s.r * mc.gm1, e_int, -mc.gpinf);
+    s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
+    return true;
+  }
+  s.e = 0.0f;
+  s.y = q[4] * rinv;
+  if (clip) {
+    s.y = s.y < mc.ylo ? mc.ylo : s.y;
+    s.y = s.y > mc.yhi ? mc.yhi : s.y;
+  }
+  double p, c;
+  const bool ok = eos_mixture(double(s.r), double(s.y), p, c);
+  s.p = float(p);
+  s.c = float(c);
+  return ok;
+}
+
+// Ghost of a boundary face in the face-local frame (bc.c:19-49): inflow
+// state, transmissive copy, slip wall (normal velocity mirrored), no-slip
+// wall (velocity reversed).
+template <int MODEL>
+__device__ __forceinline__ void local_ghost(const MixedConst &mc, int bc, int f, LS &g) {
+  if (bc == 1) {
+    local_state<MODEL>(mc, f, mc.inflow, false, g);
+  } else if (bc == 3 || bc == 4) {
+    g.un = -g.un;
+    if (bc == 4) {
+      g.um = -g.um;
+      g.ul = -g.ul;
+    }
+    g.mn = g.r * g.un;
+    g.mm = g.r * g.um;
+    g.ml = g.r * g.ul;
+  }
+}
+
+// HLLC normal flux F.n + S_K (U*_K - U_K) through a face of frame f
+// (hllc_euler.c:3-55, compute_wave_speeds.c:3-88, star_region_euler.c:3-40,
+// contracted with n as residual_faces_AMR.c:145-149), evaluated in the face
+// frame and rotated back once.
+template <int MODEL>
+__device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, const LS &L, const LS &R,
+                                           float Fn[kNeqMax]) {
+  const float SR = fmaxf(L.un + L.c, R.un + R.c);
+  const float SL = fminf(L.un - L.c, R.un - R.c);
+  const float num = fmaf(SR, R.mn, fmaf(-SL, L.mn, fmaf(L.mn, L.un, L.p) - fmaf(R.mn, R.un, R.p)));
+  const float den = fmaf(SR, R.r, fmaf(-SL, L.r, L.mn - R.mn));
   float S_S = __fdividef(num, den);
   const bool ok = !isnan(S_S);
   if (bc == 3) S_S = 0.0f;
@@ -237,52 +294,52 @@ __device__ __forceinline__ bool mixed_hllc_normal(const MixedConst &mc, int f, i
   const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
   const bool left = r1 || r2;
   const bool star = r2 || r3;
-  // upwind side K, selected field by field (no reference to either struct)
-  const float Kr = left ? L.r : R.r, Ku = left ? L.u : R.u, Kv = left ? L.v : R.v, Kw = left ? L.w : R.w;
-  const float Ke = left ? L.e : R.e, Kp = left ? L.p : R.p, Ky = left ? L.y : R.y;
-  float Kq[kNeqMax];
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) Kq[v] = left ? L.q[v] : R.q[v];
-  const float uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
+  const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn, Kmm = left ? L.mm : R.mm;
+  const float Kml = left ? L.ml : R.ml, Kq4 = left ? L.q4 : R.q4;
+  const float Kun = left ? L.un : R.un, Kum = left ? L.um : R.um, Kul = left ? L.ul : R.ul;
+  const float Kp = left ? L.p : R.p, Ke = left ? L.e : R.e, Ky = left ? L.y : R.y;
   const float SK = left ? SL : SR;
-  const float run = Kr * uK;
-  Fn[0] = run;
-  Fn[1] = fmaf(Kp, nx, run * Ku);
-  Fn[2] = fmaf(Kp, ny, run * Kv);
-  Fn[3] = fmaf(Kp, nz, run * Kw);
-  Fn[4] = mc.model == 1 ? (Ke + Kp) * uK : run * Ky;
+  // physical flux in the face frame
+  float F0 = Kmn;
+  float Fa = fmaf(Kmn, Kun, Kp);
+  float Fb = Kmn * Kum;
+  float Fc = Kmn * Kul;
+  float F4 = MODEL == 1 ? (Ke + Kp) * Kun : Kmn * Ky;
   if (star) {
-    const float dK = SK - uK;
+    const float dK = SK - Kun;
     const float cS = __fdividef(Kr * dK, SK - S_S);
-    const float us0 = cS * fmaf(wK, lx, fmaf(vK, mx, S_S * nx));
-    const float us1 = cS * fmaf(wK, ly, fmaf(vK, my, S_S * ny));
-    const float us2 = cS * fmaf(wK, lz, fmaf(vK, mz, S_S * nz));
-    const float us4 = mc.model == 1
-                          ? cS * fmaf(S_S - uK, S_S + __fdividef(Kp, Kr * dK), __fdividef(Ke, Kr))
-                          : cS * Ky;
-    Fn[0] = fmaf(SK, cS - Kq[0], Fn[0]);
-    Fn[1] = fmaf(SK, us0 - Kq[1], Fn[1]);
-    Fn[2] = fmaf(SK, us1 - Kq[2], Fn[2]);
-    Fn[3] = fmaf(SK, us2 - Kq[3], Fn[3]);
-    Fn[4] = fmaf(SK, us4 - Kq[4], Fn[4]);
+    const float us4 = MODEL == 1 ? cS * fmaf(S_S - Kun, S_S + __fdividef(Kp, Kr * dK), __fdividef(Ke, Kr))
+                                    : cS * Ky;
+    F0 = fmaf(SK, cS - Kr, F0);
+    Fa = fmaf(SK, fmaf(cS, S_S, -Kmn), Fa);
+    Fb = fmaf(SK, fmaf(cS, Kum, -Kmm), Fb);
+    Fc = fmaf(SK, fmaf(cS, Kul, -Kml), Fc);
+    F4 = fmaf(SK, us4 - Kq4, F4);
   }
+  const float *fr = mc.fr + 9 * f;
+  Fn[0] = F0;
+  Fn[1] = fmaf(fr[6], Fc, fmaf(fr[3], Fb, fr[0] * Fa));
+  Fn[2] = fmaf(fr[7], Fc, fmaf(fr[4], Fb, fr[1] * Fa));
+  Fn[3] = fmaf(fr[8], Fc, fmaf(fr[5], Fb, fr[2] * Fa));
+  Fn[4] = F4;
   return ok && (r1 || r2 || r3 || r4);
 }
 
 // Canonical flux of a face from the lower / upper face values (bc > 0: a
 // domain-boundary face, the upper side is the ghost of the lower one).
+template <int MODEL>
 __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int bc, bool clip,
                                                const float lo[kNeqMax], const float hi[kNeqMax],
                                                float Fn[kNeqMax]) {
-  FS Ls, Rs;
-  bool ok = mixed_face_state(mc, lo, clip, Ls);
+  LS Ls, Rs;
+  bool ok = local_state<MODEL>(mc, f, lo, clip, Ls);
   if (bc > 0) {
     Rs = Ls;
-    mixed_ghost(mc, bc, f, Rs);
+    local_ghost<MODEL>(mc, bc, f, Rs);
   } else {
-    ok &= mixed_face_state(mc, hi, clip, Rs);
+    ok &= local_state<MODEL>(mc, f, hi, clip, Rs);
   }
-  ok &= mixed_hllc_normal(mc, f, bc, Ls, Rs, Fn);
+  ok &= local_hllc<MODEL>(mc, f, bc, Ls, Rs, Fn);
   return ok;
 }
 
@@ -323,11 +380,12 @@ __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
 }
 
 // CFL spectral radius of one cell (definition in fvgpu.h), FP32.
+template <int MODEL>
 __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTables *geo, int32_t g,
                                                const float q[kNeqMax]) {
   const int lev = level_of(g);
   FS s;
-  mixed_face_state(mc, q, false, s);
+  mixed_face_state<MODEL>(mc, q, false, s);
   float acc = 0.0f;
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
@@ -368,8 +426,9 @@ __device__ __forceinline__ float d2f_rn(double x) {
 
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
 // CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
+template <int MODEL>
 __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageArgs &a, int c, int32_t g,
-                                              const float R[kNeqMax], const float din[kNeqMax], float dt, bool ok) {
+                                              const float R[kNeqMax], float dt, bool ok) {
   const int n = a.n, neq = mc.neq;
   bool finite = true;
 #pragma unroll
@@ -382,11 +441,14 @@ __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageA
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     const float incr = dtv * R[v];
+    // the stage-input increment, read again here rather than kept in
+    // registers through the flux phase
+    const float din = (a.Din && v < neq) ? __ldg(a.Din + v * n + c) : 0.0f;
     switch (a.irk) {
       case 1: dn[v] = incr; break;
-      case 2: dn[v] = 0.25f * (din[v] + incr); break;
-      case 3: dn[v] = (2.0f / 3.0f) * (din[v] + incr); break;
-      default: dn[v] = 0.5f * (din[v] + incr); break;
+      case 2: dn[v] = 0.25f * (din + incr); break;
+      case 3: dn[v] = (2.0f / 3.0f) * (din + incr); break;
+      default: dn[v] = 0.5f * (din + incr); break;
     }
   }
   if (a.last) {
@@ -399,7 +461,7 @@ __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageA
       qn[v] = d2f_rn(snew);
       a.SNfout[v * n + c] = qn[v];
     }
-    return a.lambda ? cell_lambda_f(mc, a.geo, g, qn) : 0.0f;
+    return a.lambda ? cell_lambda_f<MODEL>(mc, a.geo, g, qn) : 0.0f;
   }
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v)
@@ -422,6 +484,7 @@ __device__ __forceinline__ void global_state(const MixedConst &mc, const StageAr
 
 // ============================ general kernel ================================
 
+template <int MODEL>
 struct Block {
   const StageArgs &a;
   const MixedConst &mc;
@@ -457,7 +520,7 @@ struct Block {
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
     } else {
-      boundary_value(mc, -1 - code, f, own, nb);
+      boundary_value<MODEL>(mc, -1 - code, f, own, nb);
     }
   }
   // face value of face f of any cell (used across block edges)
@@ -475,6 +538,7 @@ struct Block {
   }
 };
 
+template <int MODEL, bool MUSCL>
 __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageArgs a) {
   __shared__ float st[kNeqMax][kBlock];
   __shared__ float sf[6][kNeqMax][kBlock];
@@ -486,9 +550,9 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   const int c = c0 + t;
   const int n = a.n;
   const bool active = t < bd.count;
-  const int neq = mc.neq;
-  const bool muscl = mc.ischeme == 2;
-  Block blk(a, mc, c0, bd.count, st);
+  constexpr int neq = kNeqMax;  // models 1 and 3: five conservative variables
+  constexpr bool muscl = MUSCL;
+  Block<MODEL> blk(a, mc, c0, bd.count, st);
 
   // A: own stage state
   float din[kNeqMax], q[kNeqMax];
@@ -591,7 +655,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
           lo[v] = own_low ? own[v] : oth[v];
           hi[v] = own_low ? oth[v] : own[v];
         }
-        ok &= canonical_flux(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
+        ok &= canonical_flux<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
         if (plus && !boundary && !hanging) {
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
@@ -604,7 +668,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   }
 
   float lam = 0.0f;
-  if (active) lam = stage_update(mc, a, c, g, R, din, s_dt, ok);
+  if (active) lam = stage_update<MODEL>(mc, a, c, g, R, s_dt, ok);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
@@ -679,6 +743,7 @@ __device__ __forceinline__ int32_t brick_geom(int level, uint32_t bnd_edges) {
 #ifndef FV_BRICK_MIN_BLOCKS
 #define FV_BRICK_MIN_BLOCKS 5  // 48 registers: 5 blocks per SM measured faster than 4 (217 vs 257 us per stage, 128^3)
 #endif
+template <int MODEL, bool MUSCL>
 __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(MixedConst mc, StageArgs a) {
   __shared__ float tile[kNeqMax][kTile];
   __shared__ float flux[kNeqMax][kFaces];
@@ -688,8 +753,8 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   const BlockDesc *bdp = a.blocks + blockIdx.x;
   const int t = threadIdx.x;
   const int n = a.n;
-  const int neq = mc.neq;
-  const bool muscl = mc.ischeme == 2;
+  constexpr int neq = kNeqMax;  // models 1 and 3: five conservative variables
+  constexpr bool muscl = MUSCL;
   const int start = __ldg(&bdp->start), level = __ldg(&bdp->level);
   const int c = start + t;
   uint32_t bmask = 0;  // sides of the brick on the domain boundary
@@ -796,7 +861,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
         const int ti_own = tile_index(bx, by, bz);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
-        boundary_value(mc, -1 - s_side[side], side, own, gv);
+        boundary_value<MODEL>(mc, -1 - s_side[side], side, own, gv);
         const int t1 = tile_index(bx + sx, by + sy, bz + sz), t2 = tile_index(bx + 2 * sx, by + 2 * sy, bz + 2 * sz);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) {
@@ -857,7 +922,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
         recon_tile(ti, elo, fp, st, own);
       else
         recon_tile(ti + st, eup, fm, -st, own);
-      ok &= canonical_flux(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
+      ok &= canonical_flux<MODEL>(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
       if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
@@ -866,7 +931,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
       float lo[kNeqMax], hi[kNeqMax];
       recon_tile(ti, elo, fp, st, lo);
       recon_tile(ti + st, eup, fm, -st, hi);
-      ok &= canonical_flux(mc, fp, 0, muscl, lo, hi, Fn);
+      ok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
     }
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
@@ -892,7 +957,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   add_face(3, tx_p - 1, false);
   add_face(0, ty_p - BX, false);
   add_face(4, tz_p - BX * BY, false);
-  const float lam = stage_update(mc, a, c, brick_geom(level, be), R, din, s_dt, ok);
+  const float lam = stage_update<MODEL>(mc, a, c, brick_geom(level, be), R, s_dt, ok);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
@@ -904,6 +969,7 @@ __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__
 
 // The same with the CFL spectral radius of the copied state (the mixed
 // path's first CFL time step after an upload): one cell per thread.
+template <int MODEL>
 __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, const int32_t *__restrict__ geom,
                                                                 const GeoTables *geo, const double *__restrict__ S,
                                                                 float *__restrict__ Sf, int n, double *lambda) {
@@ -916,7 +982,7 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
       q[v] = d2f_rn(S[int64_t(v) * n + c]);
       Sf[int64_t(v) * n + c] = q[v];
     }
-    lam = fmaxf(lam, cell_lambda_f(mc, geo, __ldg(geom + c), q));
+    lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
   block_max_lambda_f(lam, lambda);
 }
@@ -1065,6 +1131,16 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         return FVGPU_ERR_UNSUPPORTED;
       }
     }
+    // fluxes are evaluated in the face frame: n, t1, t2 must be orthonormal
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const double *a = m->frames + 9 * f + 3 * i, *b = m->frames + 9 * f + 3 * j;
+        const double dot = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+        if (std::fabs(dot - (i == j ? 1.0 : 0.0)) > 1e-12) {
+          snprintf(why, whylen, "the mixed path needs orthonormal face frames (face %d)", f);
+          return FVGPU_ERR_UNSUPPORTED;
+        }
+      }
   }
   const int64_t n = m->ncells;
   GeoTables gt;
@@ -1255,12 +1331,35 @@ cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const do
                                      LaunchMarks &marks, cudaStream_t st) {
   marks.mark(FVGPU_KIND_MIXED_AUX);
   const unsigned blocks = unsigned(std::min<int64_t>((r.n + kBlock - 1) / kBlock, 152 * 8));
-  k_state_to_f32_lambda<<<blocks, kBlock, 0, st>>>(make_const(ph), static_cast<const int32_t *>(r.buf[kBufGeom]),
-                                                   static_cast<const GeoTables *>(r.buf[kBufTables]), S,
-                                                   static_cast<float *>(r.buf[kBufSNf]), int(r.n), lambda);
+  const MixedConst mc = make_const(ph);
+  const int32_t *geom = static_cast<const int32_t *>(r.buf[kBufGeom]);
+  const GeoTables *geo = static_cast<const GeoTables *>(r.buf[kBufTables]);
+  float *Sf = static_cast<float *>(r.buf[kBufSNf]);
+  if (ph.model == 1)
+    k_state_to_f32_lambda<1><<<blocks, kBlock, 0, st>>>(mc, geom, geo, S, Sf, int(r.n), lambda);
+  else
+    k_state_to_f32_lambda<3><<<blocks, kBlock, 0, st>>>(mc, geom, geo, S, Sf, int(r.n), lambda);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;
+}
+
+// the kernel instance of the configuration (EOS model, reconstruction order)
+template <int MODEL, bool MUSCL>
+void launch_instance(bool brick, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
+  if (brick)
+    k_mixed_brick<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+  else
+    k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+}
+
+void launch_kernel(const Phys &ph, bool brick, unsigned grid, const MixedConst &mc, const StageArgs &a,
+                   cudaStream_t st) {
+  const bool muscl = ph.ischeme == 2;
+  if (ph.model == 1)
+    muscl ? launch_instance<1, true>(brick, grid, mc, a, st) : launch_instance<1, false>(brick, grid, mc, a, st);
+  else
+    muscl ? launch_instance<3, true>(brick, grid, mc, a, st) : launch_instance<3, false>(brick, grid, mc, a, st);
 }
 
 // One RK step from FP64 state `in` (and its FP32 copy) to `out`.
@@ -1292,14 +1391,14 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     if (r.nbricks > 0) {
       a.blocks = blocks;
       marks.mark(FVGPU_KIND_MIXED_STAGE);
-      k_mixed_brick<<<unsigned(r.nbricks), kBlock, 0, st>>>(mc, a);
+      launch_kernel(ph, true, unsigned(r.nbricks), mc, a, st);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
     if (r.ngeneral > 0) {
       a.blocks = blocks + r.nbricks;
       marks.mark(FVGPU_KIND_MIXED_STAGE);
-      k_mixed_general<<<unsigned(r.ngeneral), kBlock, 0, st>>>(mc, a);
+      launch_kernel(ph, false, unsigned(r.ngeneral), mc, a, st);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
