@@ -379,22 +379,33 @@ __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
   }
 }
 
-// CFL spectral radius of one cell (definition in fvgpu.h), FP32.
-template <int MODEL>
-__device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTables *geo, int32_t g,
-                                               const float q[kNeqMax]) {
-  const int lev = level_of(g);
+// CFL spectral radius of one cell (definition in fvgpu.h), FP32, with the
+// area of face f from area(f) and 1 / (2 V).
+template <int MODEL, class AreaFn>
+__device__ __forceinline__ float cell_lambda_with(const MixedConst &mc, const float q[kNeqMax], AreaFn area,
+                                                  float inv2vol) {
   FS s;
   mixed_face_state<MODEL>(mc, q, false, s);
   float acc = 0.0f;
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
     const float un = fabsf(fmaf(s.w, mc.fr[9 * f + 2], fmaf(s.v, mc.fr[9 * f + 1], s.u * mc.fr[9 * f])));
-    const int rel = rel_of(g, f);
-    const float A = rel == kRelFiner ? 4.0f * geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
-    acc = fmaf(A, un + s.c, acc);
+    acc = fmaf(area(f), un + s.c, acc);
   }
-  return acc * geo->inv2vol[lev];
+  return acc * inv2vol;
+}
+
+template <int MODEL>
+__device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTables *geo, int32_t g,
+                                               const float q[kNeqMax]) {
+  const int lev = level_of(g);
+  return cell_lambda_with<MODEL>(
+      mc, q,
+      [&](int f) {
+        const int rel = rel_of(g, f);
+        return rel == kRelFiner ? 4.0f * geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
+      },
+      geo->inv2vol[lev]);
 }
 
 // Exact FP32 -> FP64 and round-to-nearest FP64 -> FP32 conversions on the
@@ -427,23 +438,22 @@ __device__ __forceinline__ float d2f_rn(double x) {
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
 // CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
 template <int MODEL>
-__device__ __forceinline__ float stage_update(const MixedConst &mc, const StageArgs &a, int c, int32_t g,
-                                              const float R[kNeqMax], float dt, bool ok) {
-  const int n = a.n, neq = mc.neq;
+__device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageArgs &a, int c, float dtv,
+                                             const float R[kNeqMax], bool ok, float qn[kNeqMax]) {
+  const int n = a.n;
   bool finite = true;
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v)
-    if (v < neq && !isfinite(R[v])) finite = false;
+    if (!isfinite(R[v])) finite = false;
   if (!ok) raise_error(a.err, kErrRegion, c);
   if (!finite) raise_error(a.err, kErrNonFinite, c);
-  const float dtv = dt * a.geo->inv_vol[level_of(g)];
   float dn[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     const float incr = dtv * R[v];
     // the stage-input increment, read again here rather than kept in
     // registers through the flux phase
-    const float din = (a.Din && v < neq) ? __ldg(a.Din + v * n + c) : 0.0f;
+    const float din = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
     switch (a.irk) {
       case 1: dn[v] = incr; break;
       case 2: dn[v] = 0.25f * (din + incr); break;
@@ -452,21 +462,18 @@ __device__ __forceinline__ float stage_update(const MixedConst &mc, const StageA
     }
   }
   if (a.last) {
-    float qn[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      if (v >= neq) break;
       const double snew = __ldg(a.SN + v * n + c) + f2d_exact(dn[v]);
       a.SNout[v * n + c] = snew;
       qn[v] = d2f_rn(snew);
       a.SNfout[v * n + c] = qn[v];
     }
-    return a.lambda ? cell_lambda_f<MODEL>(mc, a.geo, g, qn) : 0.0f;
+    return true;
   }
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v)
-    if (v < neq) a.Dout[v * n + c] = dn[v];
-  return 0.0f;
+  for (int v = 0; v < kNeqMax; ++v) a.Dout[v * n + c] = dn[v];
+  return false;
 }
 
 // stage state of any cell from global memory: SNf + D
@@ -668,7 +675,11 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   }
 
   float lam = 0.0f;
-  if (active) lam = stage_update<MODEL>(mc, a, c, g, R, s_dt, ok);
+  if (active) {
+    float qn[kNeqMax];
+    const float dtv = s_dt * a.geo->inv_vol[level_of(g)];
+    if (stage_update<MODEL>(mc, a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
+  }
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
@@ -730,16 +741,6 @@ constexpr BrickTasks make_brick_tasks() {
 }
 __device__ const BrickTasks g_brick_tasks = make_brick_tasks();
 
-// geometry code of a brick cell: its level, boundary relation on the faces
-// where it touches a domain-boundary side of the brick
-__device__ __forceinline__ int32_t brick_geom(int level, uint32_t bnd_edges) {
-  int32_t g = level;
-#pragma unroll
-  for (int f = 0; f < 6; ++f)
-    if ((bnd_edges >> f) & 1u) g |= kRelBoundary << (5 + 2 * f);
-  return g;
-}
-
 #ifndef FV_BRICK_MIN_BLOCKS
 #define FV_BRICK_MIN_BLOCKS 5  // 48 registers: 5 blocks per SM measured faster than 4 (217 vs 257 us per stage, 128^3)
 #endif
@@ -748,7 +749,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   __shared__ float tile[kNeqMax][kTile];
   __shared__ float flux[kNeqMax][kFaces];
   __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
-  __shared__ float s_dt;
+  __shared__ float s_dtv, s_inv2vol;  // dt / V and 1 / (2 V) of the brick's level
   __shared__ int s_side[6];  // brick sides (indexed at run time: kept out of local memory)
   const BlockDesc *bdp = a.blocks + blockIdx.x;
   const int t = threadIdx.x;
@@ -769,7 +770,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
     s_geo[f][r][1] = gf[1];
     s_geo[f][r][2] = gf[2];
   }
-  if (t == 0) s_dt = __double2float_rn(*a.dt);
+  if (t == 0) {
+    s_dtv = __double2float_rn(*a.dt) * a.geo->inv_vol[level];
+    s_inv2vol = a.geo->inv2vol[level];
+  }
 
   // A1: the brick's cells and the halo from the six neighbour bricks
   int x, y, z;
@@ -938,7 +942,9 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   }
   __syncthreads();
 
-  // C: gather in the fixed face order, RK stage update
+  // C: gather in the fixed face order, RK stage update (coordinates decoded
+  // again: cheaper than keeping them live through the flux phase)
+  morton_decode(t, x, y, z);
   const uint32_t be = edge_mask(x, y, z) & bmask;
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
@@ -957,7 +963,9 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   add_face(3, tx_p - 1, false);
   add_face(0, ty_p - BX, false);
   add_face(4, tz_p - BX * BY, false);
-  const float lam = stage_update<MODEL>(mc, a, c, brick_geom(level, be), R, s_dt, ok);
+  float qn[kNeqMax], lam = 0.0f;
+  if (stage_update<MODEL>(mc, a, c, s_dtv, R, ok, qn) && a.lambda)
+    lam = cell_lambda_with<MODEL>(mc, qn, [&](int f) { return s_geo[f][(be >> f) & 1u][2]; }, s_inv2vol);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
