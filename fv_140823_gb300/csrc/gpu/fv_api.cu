@@ -797,8 +797,9 @@ int fvgpu_download(fvgpu_ctx *ctx, int field, double *out) {
       if (ctx->cfg.ischeme != 2) return set_err(ctx, FVGPU_ERR_STATE, "SF exists only for ischeme 2");
       b = &ctx->SF; bytes = sizeof(double) * 6 * ctx->neq * n; break;
     case FVGPU_FIELD_SG:
-      if (ctx->cfg.ns != 1) return set_err(ctx, FVGPU_ERR_STATE, "SG exists only for ns 1");
-      b = &ctx->SG; bytes = sizeof(double) * (ctx->neq + 1) * 3 * n; break;
+      bytes = sizeof(double) * (ctx->neq + 1) * 3 * n;
+      if (ctx->SG.bytes < bytes) return set_err(ctx, FVGPU_ERR_STATE, "no gradients: call fvgpu_gradcalc first");
+      b = &ctx->SG; break;
     default: return set_err(ctx, FVGPU_ERR_ARG, "unknown field %d", field);
   }
   FV_CUDA(ctx, cudaMemcpyAsync(out, b->p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
@@ -816,8 +817,15 @@ int fvgpu_faceinterp(fvgpu_ctx *ctx) {
 int fvgpu_gradcalc(fvgpu_ctx *ctx) {
   int rc = ensure_state(ctx);
   if (rc) return rc;
-  if (ctx->cfg.ns != 1) return set_err(ctx, FVGPU_ERR_STATE, "gradcalc needs ns 1");
   cudaSetDevice(ctx->cfg.device);
+  // inviscid runs allocate the gradients on first use (the host exports them,
+  // loop.c:51)
+  const size_t sg_bytes = sizeof(double) * size_t(ctx->neq + 1) * 3 * size_t(ctx->n);
+  if (ctx->SG.bytes < sg_bytes) {
+    FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FV_CUDA(ctx, ctx->SG.alloc(sg_bytes));
+    ctx->drop_graphs();  // graphs captured the old gradient buffer
+  }
   return enqueue_gradcalc(ctx);
 }
 

@@ -133,7 +133,8 @@ int fvgpu_download(fvgpu_ctx *ctx, int field, double *out);
 /* ---- the reference's calls -------------------------------------------- */
 /* faceinterp(run), faceinterp.c:21-61: SF from S. */
 int fvgpu_faceinterp(fvgpu_ctx *ctx);
-/* gradcalc(run), gradcalc.c:9-47: SG from S. */
+/* gradcalc(run), gradcalc.c:9-47: SG from S (for ns == 0 the gradient
+ * array is allocated on the first call, as the host exports gradients). */
 int fvgpu_gradcalc(fvgpu_ctx *ctx);
 /* RHS(run), RHS.c:3-13: RHS from S, SF, SG (as the reference, faceinterp /
  * gradcalc must have been called first when ischeme == 2 / ns == 1). */
