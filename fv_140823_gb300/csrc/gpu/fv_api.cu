@@ -2,6 +2,7 @@
 // the reference's RHS / RK calls, graph-captured time steps, reductions.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -89,6 +90,9 @@ struct fvgpu_ctx {
   // adjoint work arrays (allocated by the first adjoint call)
   unsigned bc_mask = 0;  // bit b set when boundary code b occurs in the mesh
   DevBuf adjL, adjR, adjRh, adjW, adjG, adjAcc, adjOut, adjY1, adjY2, adjSN, adjCK;
+  // halo exchange index lists
+  DevBuf halo_send, halo_recv;
+  int64_t nsend = 0, nrecv = 0;
   int64_t adj_ck_steps = 0;
   bool adj_ready = false;
   fv::LaunchMarks marks;
@@ -192,6 +196,23 @@ __global__ void k_cons_final(int neq, const double *__restrict__ partial, double
     }
     if (threadIdx.x == 0) sums[v] = red[0];
     __syncthreads();
+  }
+}
+
+// halo exchange: gather / scatter of the state's rows
+__global__ void k_halo_gather(int neq, int64_t n, const double *__restrict__ S, const int32_t *__restrict__ cells,
+                              int64_t count, double *__restrict__ buf) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = cells[i];
+    for (int v = 0; v < neq; ++v) buf[v * count + i] = S[v * n + c];
+  }
+}
+
+__global__ void k_halo_scatter(int neq, int64_t n, double *__restrict__ S, const int32_t *__restrict__ cells,
+                               int64_t count, const double *__restrict__ buf) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = cells[i];
+    for (int v = 0; v < neq; ++v) S[v * n + c] = buf[v * count + i];
   }
 }
 
@@ -729,6 +750,9 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
     b->release();
   ctx->adj_ck_steps = 0;
   ctx->adj_ready = false;
+  ctx->halo_send.release();
+  ctx->halo_recv.release();
+  ctx->nsend = ctx->nrecv = 0;
   ctx->bc_mask = 0;
   for (int64_t i = 0; i < 6 * n; ++i) {
     const int32_t code = m->nbr[i];
@@ -1020,6 +1044,60 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums) {
   FV_CUDA(ctx, cudaMemcpyAsync(sums, d_sums, sizeof(double) * (ctx->neq + 1), cudaMemcpyDeviceToHost,
                                ctx->stream));
   return sync_and_check(ctx);
+}
+
+int fvgpu_halo_set(fvgpu_ctx *ctx, const int32_t *send_cells, int64_t nsend, const int32_t *recv_cells,
+                   int64_t nrecv) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (nsend < 0 || nrecv < 0 || (nsend > 0 && !send_cells) || (nrecv > 0 && !recv_cells))
+    return set_err(ctx, FVGPU_ERR_ARG, "bad halo lists");
+  std::vector<uint8_t> seen(size_t(ctx->n), 0);
+  for (int64_t i = 0; i < nsend; ++i)
+    if (send_cells[i] < 0 || send_cells[i] >= ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "send cell %lld out of range", (long long)i);
+  for (int64_t i = 0; i < nrecv; ++i) {
+    const int32_t c = recv_cells[i];
+    if (c < 0 || c >= ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "recv cell %lld out of range", (long long)i);
+    if (seen[size_t(c)]) return set_err(ctx, FVGPU_ERR_ARG, "recv cell %d listed twice", c);
+    seen[size_t(c)] = 1;
+  }
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  FV_CUDA(ctx, ctx->halo_send.alloc(sizeof(int32_t) * size_t(nsend)));
+  FV_CUDA(ctx, ctx->halo_recv.alloc(sizeof(int32_t) * size_t(nrecv)));
+  if (nsend) FV_CUDA(ctx, cudaMemcpy(ctx->halo_send.p, send_cells, sizeof(int32_t) * size_t(nsend), cudaMemcpyHostToDevice));
+  if (nrecv) FV_CUDA(ctx, cudaMemcpy(ctx->halo_recv.p, recv_cells, sizeof(int32_t) * size_t(nrecv), cudaMemcpyHostToDevice));
+  ctx->nsend = nsend;
+  ctx->nrecv = nrecv;
+  return FVGPU_OK;
+}
+
+int fvgpu_halo_pack(fvgpu_ctx *ctx, double *send_buf) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (ctx->nsend == 0) return FVGPU_OK;
+  if (!send_buf) return set_err(ctx, FVGPU_ERR_ARG, "null send buffer");
+  cudaSetDevice(ctx->cfg.device);
+  const unsigned blocks = unsigned(std::min<int64_t>((ctx->nsend + 255) / 256, 1024));
+  k_halo_gather<<<blocks, 256, 0, ctx->stream>>>(ctx->neq, ctx->n, ctx->S.as<double>(), ctx->halo_send.as<int32_t>(),
+                                                 ctx->nsend, send_buf);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+int fvgpu_halo_unpack(fvgpu_ctx *ctx, const double *recv_buf) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (ctx->nrecv == 0) return FVGPU_OK;
+  if (!recv_buf) return set_err(ctx, FVGPU_ERR_ARG, "null receive buffer");
+  cudaSetDevice(ctx->cfg.device);
+  const unsigned blocks = unsigned(std::min<int64_t>((ctx->nrecv + 255) / 256, 1024));
+  k_halo_scatter<<<blocks, 256, 0, ctx->stream>>>(ctx->neq, ctx->n, ctx->S.as<double>(), ctx->halo_recv.as<int32_t>(),
+                                                  ctx->nrecv, recv_buf);
+  FV_LAUNCHED(ctx);
+  ctx->lambda_valid = false;
+  ctx->mixed.snf_valid = false;
+  return FVGPU_OK;
 }
 
 int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld) {

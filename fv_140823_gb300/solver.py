@@ -172,6 +172,22 @@ class Solver:
         self._call("fvgpu_conservation", _ptr(out))
         return out
 
+    # -- halo exchange -------------------------------------------------------
+    def halo_set(self, send_cells: np.ndarray, recv_cells: np.ndarray):
+        """Local cells this rank packs for others / receives into (ghosts)."""
+        self._halo_send = np.ascontiguousarray(send_cells, dtype=np.int32)
+        self._halo_recv = np.ascontiguousarray(recv_cells, dtype=np.int32)
+        self._call("fvgpu_halo_set", _ptr(self._halo_send), C.c_int64(self._halo_send.size),
+                   _ptr(self._halo_recv), C.c_int64(self._halo_recv.size))
+
+    def halo_pack(self, send_ptr: int):
+        """Gather the send cells' state into a device buffer [neq][nsend]."""
+        self._call("fvgpu_halo_pack", C.c_void_p(send_ptr))
+
+    def halo_unpack(self, recv_ptr: int):
+        """Scatter a device buffer [neq][nrecv] into the ghost cells."""
+        self._call("fvgpu_halo_unpack", C.c_void_p(recv_ptr))
+
     # -- adjoint -------------------------------------------------------------
     def residual_vjp(self, w: np.ndarray) -> np.ndarray:
         """(dR/dU)^T w at the current state (FP64 residual)."""

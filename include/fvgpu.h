@@ -176,6 +176,22 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
 int fvgpu_conservation_noalloc(const double *S, const double *vol, int64_t ncells, int neq, double *sums,
                                void *stream);
 
+/* ---- halo exchange (domain decomposition) ------------------------------- */
+/* The reference exchanges the state of interface cells between MPI ranks
+ * once per stage (communicate_S, communicate1.c:44-229).  Here a rank's mesh
+ * holds its own cells plus a 2-deep ghost layer (fv_140823_gb300/halo.py
+ * builds both and the lists below); before each stage the owner packs the
+ * cells other ranks hold as ghosts, the caller moves the buffers (NCCL,
+ * MPI, or a copy between contexts on one GPU) and the receiver unpacks them
+ * into its ghost cells.  Index lists are host arrays of local cell indices,
+ * copied at the call; recv_cells must be distinct.  Buffers are DEVICE arrays
+ * [neq][count] the caller owns; pack and unpack are queued on the context's
+ * stream (fvgpu_get_stream).  FP64 state only. */
+int fvgpu_halo_set(fvgpu_ctx *ctx, const int32_t *send_cells, int64_t nsend, const int32_t *recv_cells,
+                   int64_t nrecv);
+int fvgpu_halo_pack(fvgpu_ctx *ctx, double *send_buf);
+int fvgpu_halo_unpack(fvgpu_ctx *ctx, const double *recv_buf);
+
 /* ---- adjoint ----------------------------------------------------------- */
 /* No reference counterpart: the reference has no derivative code.  These
  * entry points give the transpose of the FP64 residual and step maps
