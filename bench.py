@@ -134,6 +134,22 @@ def traffic_per_launch(kernel: str, ncells: int):
         return None
 
 
+def fp64_ops_per_cell(key: str):
+    """Counted FP64 operations per cell of a kernel (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
+            return float(json.load(fh)["fp64_ops"][key])
+    except Exception:
+        return None
+
+
+def measured_fp64_gops(device: int):
+    import ctypes as C
+    from fv_140823_gb300._native import load_gpu_lib
+    out = C.c_double()
+    return out.value if load_gpu_lib().fvgpu_measure_fp64(int(device), C.byref(out)) == 0 else None
+
+
 def time_steps(torch, s, stream, flush, steps: int, cfl: float, scheme="ssprk3"):
     """Per-step device times (ms), each step bracketed by events on the
     library's stream, with an L2 flush before each step outside the events."""
@@ -258,6 +274,19 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(hostOut.numel() * 8)},
         }
         if prec == abi.FP64:
+            # FP64-pipe roofline of the residual kernel: counted FP64 operations
+            # per launch over its live launch time, against the measured rate
+            ops = fp64_ops_per_cell("residual_per_cell")
+            gops = measured_fp64_gops(local)
+            if ops is not None and gops and "residual" in results[prec]["kernel_ms"]:
+                kl = results[prec]["kernel_launches"]["residual"]
+                res_ms = results[prec]["kernel_ms"]["residual"] / max(kl, 1)
+                ach = ops * n / (res_ms * 1e-3) / 1e9
+                results[prec]["roofline_fp64"] = {
+                    "bound": "fp64", "kernel": "residual", "achieved": ach, "peak": gops, "unit": "GFLOP/s",
+                    "frac": ach / gops, "ops_per_cell": ops, "avg_launch_ms": res_ms,
+                    "peak_source": "measured (fvgpu_measure_fp64: separate FP64 adds and multiplies)",
+                    "note": "FP64 divisions and square roots count one operation each"}
             # hand-written adjoint of the FP64 residual against one residual evaluation
             s.set_state(case.U)
             ms_res, ms_vjp = s.profile_adjoint(reps=5)
@@ -366,7 +395,7 @@ def main():
         if abi.FP64 in results and head != abi.FP64 and "value" in results[abi.FP64]:
             f = results[abi.FP64]
             line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "roofline": f["roofline"],
-                            "e2e": f["e2e"], "kernel_ms": f["kernel_ms"]}
+                            "roofline_fp64": f.get("roofline_fp64"), "e2e": f["e2e"], "kernel_ms": f["kernel_ms"]}
             line["mixed_over_fp64"] = r["value"] / f["value"]
         elif abi.MIXED in results and "unsupported" in results[abi.MIXED]:
             line["mixed"] = results[abi.MIXED]

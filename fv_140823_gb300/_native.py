@@ -67,6 +67,7 @@ _GPU_SIGS = {
     "fvgpu_compute_dt": ([C.c_void_p, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "fvgpu_conservation": ([C.c_void_p, C.c_void_p], C.c_int),
     "fvgpu_residual_vjp": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_measure_fp64": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
     "fvgpu_halo_set": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64], C.c_int),
     "fvgpu_halo_pack": ([C.c_void_p, C.c_void_p], C.c_int),
     "fvgpu_halo_unpack": ([C.c_void_p, C.c_void_p], C.c_int),

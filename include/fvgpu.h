@@ -231,6 +231,11 @@ int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const
 int fvgpu_profile_adjoint(fvgpu_ctx *ctx, int reps, double *ms_residual, double *ms_vjp);
 
 /* ---- diagnostics -------------------------------------------------------- */
+/* Measured FP64 arithmetic rate of the device (G operations/s): separate
+ * adds and multiplies from registers on every SM, as the FP64 path issues
+ * them; the denominator of that path's roofline.  No reference counterpart. */
+int fvgpu_measure_fp64(int device, double *gops);
+
 /* Kernel kinds reported by fvgpu_profile_step. */
 #define FVGPU_KIND_FACEINTERP 0  /* faceinterp.c */
 #define FVGPU_KIND_GRADCALC 1    /* gradcalc.c */

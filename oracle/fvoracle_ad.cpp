@@ -43,6 +43,30 @@ inline Dual sqrt(Dual a) {
 }
 inline Dual fabs(Dual a) { return a.v < 0.0 ? -a : a; }
 inline double val(Dual a) { return a.v; }
+
+// Operation-counting scalar: the FP64 arithmetic of the path, counted per
+// kind (sign changes and absolute values are operand modifiers, not counted).
+struct OpCounts {
+  uint64_t add, mul, div, sqrt;
+};
+OpCounts g_ops;
+struct Cnt {
+  double v;
+  Cnt() : v(0.0) {}
+  Cnt(double x) : v(x) {}
+};
+inline Cnt operator+(Cnt a, Cnt b) { g_ops.add++; return Cnt(a.v + b.v); }
+inline Cnt operator-(Cnt a, Cnt b) { g_ops.add++; return Cnt(a.v - b.v); }
+inline Cnt operator-(Cnt a) { return Cnt(-a.v); }
+inline Cnt operator*(Cnt a, Cnt b) { g_ops.mul++; return Cnt(a.v * b.v); }
+inline Cnt operator/(Cnt a, Cnt b) { g_ops.div++; return Cnt(a.v / b.v); }
+inline Cnt &operator+=(Cnt &a, Cnt b) { return a = a + b; }
+inline bool operator<(Cnt a, Cnt b) { return a.v < b.v; }
+inline bool operator>(Cnt a, Cnt b) { return a.v > b.v; }
+inline bool operator<=(Cnt a, Cnt b) { return a.v <= b.v; }
+inline Cnt sqrt(Cnt a) { g_ops.sqrt++; return Cnt(std::sqrt(a.v)); }
+inline Cnt fabs(Cnt a) { return Cnt(std::fabs(a.v)); }
+inline double val(Cnt a) { return a.v; }
 inline double val(double a) { return a; }
 using std::fabs;
 using std::sqrt;
@@ -67,7 +91,7 @@ void face_state(const fvgpu_config *cfg, const T *q, FState<T> &s) {
   s.e = q[4];
   s.vec[4] = q[4];
   const T e_int = (s.e / s.r) - T(0.5) * (s.u * s.u + s.v * s.v + s.w * s.w);
-  s.p = s.r * T(cfg->gamma - 1.0) * e_int - T(cfg->gamma) * T(cfg->pinf);
+  s.p = s.r * (T(cfg->gamma) - T(1.0)) * e_int - T(cfg->gamma) * T(cfg->pinf);
   s.c = sqrt(T(cfg->gamma) * (s.p + T(cfg->pinf)) / s.r);
 }
 
@@ -84,7 +108,7 @@ void inflow_state(const fvgpu_config *cfg, FState<T> &g) {
   for (int k = 0; k < NEQ; ++k) g.vec[k] = q[k];
   g.e = q[4];
   const T e_int = (q[4] / rho) - T(0.5) * (g.u * g.u + g.v * g.v + g.w * g.w);
-  g.p = g.r * T(cfg->gamma - 1.0) * e_int - T(cfg->gamma) * T(cfg->pinf);
+  g.p = g.r * (T(cfg->gamma) - T(1.0)) * e_int - T(cfg->gamma) * T(cfg->pinf);
   g.c = sqrt(T(cfg->gamma) * (g.p + T(cfg->pinf)) / g.r);
 }
 
@@ -301,7 +325,7 @@ void rk(int irk, double dt, const fvgpu_mesh_soa *m, T *S, T *SN, const T *R) {
       const int64_t i = int64_t(e) * n + c;
       switch (irk) {
         case 0: SN[i] = S[i]; break;
-        case 1: S[i] = SN[i] + T(dt) * T(1.0 / Vol) * R[i]; break;
+        case 1: S[i] = SN[i] + T(dt) * (T(1.0) / T(Vol)) * R[i]; break;
         case 2: S[i] = T(3.0 / 4.0) * SN[i] + T(1.0 / 4.0) * S[i] + T(1.0 / 4.0) * T(dt) * R[i] / T(Vol); break;
         case 3: S[i] = T(1.0 / 3.0) * SN[i] + T(2.0 / 3.0) * S[i] + T(2.0 / 3.0) * T(dt) * R[i] / T(Vol); break;
         case 4: S[i] = T(1.0 / 2.0) * SN[i] + T(1.0 / 2.0) * S[i] + T(1.0 / 2.0) * T(dt) * R[i] / T(Vol); break;
@@ -356,6 +380,55 @@ int fvo_ad_steps_jvp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const int
     if (S_out) S_out[i] = S[size_t(i)].v;
     JV[i] = S[size_t(i)].d;
   }
+  return 0;
+}
+
+// FP64 operations of nsteps RK steps from U (the FP64 path's arithmetic,
+// counted once per operation of the restated expressions): counts[0..3] =
+// additions / subtractions, multiplications, divisions, square roots.
+int fvo_ad_count_steps(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const int *stages, int nstages, double dt,
+                       int nsteps, const double *U, uint64_t *counts) {
+  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  const int64_t N = NEQ * m->ncells;
+  std::vector<Cnt> S(static_cast<size_t>(N)), SN(static_cast<size_t>(N)), R(static_cast<size_t>(N));
+  for (int64_t i = 0; i < N; ++i) S[size_t(i)] = Cnt(U[i]);
+  g_ops = OpCounts{0, 0, 0, 0};
+  for (int step = 0; step < nsteps; ++step) {
+    rk<Cnt>(0, dt, m, S.data(), SN.data(), R.data());
+    for (int k = 0; k < nstages; ++k) {
+      residual<Cnt>(cfg, m, S.data(), R.data());
+      rk<Cnt>(stages[k], dt, m, S.data(), SN.data(), R.data());
+    }
+  }
+  counts[0] = g_ops.add;
+  counts[1] = g_ops.mul;
+  counts[2] = g_ops.div;
+  counts[3] = g_ops.sqrt;
+  return 0;
+}
+
+// FP64 operations of one stage split by kernel: counts[0..3] faceinterp,
+// counts[4..7] residual with the fused RK(irk) update (kinds as above).
+int fvo_ad_count_stage(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, int irk, double dt, const double *U,
+                       uint64_t *counts) {
+  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  const int64_t N = NEQ * m->ncells;
+  std::vector<Cnt> S(static_cast<size_t>(N)), SN(static_cast<size_t>(N)), R(static_cast<size_t>(N));
+  std::vector<Cnt> SF(static_cast<size_t>(6 * N));
+  for (int64_t i = 0; i < N; ++i) S[size_t(i)] = SN[size_t(i)] = Cnt(U[i]);
+  g_ops = OpCounts{0, 0, 0, 0};
+  if (cfg->ischeme == 2) faceinterp(cfg, m, S.data(), SF.data());
+  counts[0] = g_ops.add;
+  counts[1] = g_ops.mul;
+  counts[2] = g_ops.div;
+  counts[3] = g_ops.sqrt;
+  g_ops = OpCounts{0, 0, 0, 0};
+  rhs(cfg, m, S.data(), cfg->ischeme == 2 ? SF.data() : nullptr, R.data());
+  rk<Cnt>(irk, dt, m, S.data(), SN.data(), R.data());
+  counts[4] = g_ops.add;
+  counts[5] = g_ops.mul;
+  counts[6] = g_ops.div;
+  counts[7] = g_ops.sqrt;
   return 0;
 }
 

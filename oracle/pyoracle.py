@@ -316,6 +316,8 @@ class OracleAD:
             L.fvo_ad_residual.argtypes = [vp, vp, vp, vp]
             L.fvo_ad_jvp.argtypes = [vp, vp, vp, vp, vp, vp]
             L.fvo_ad_steps_jvp.argtypes = [vp, vp, vp, C.c_int, C.c_double, C.c_int, vp, vp, vp, vp]
+            L.fvo_ad_count_steps.argtypes = [vp, vp, vp, C.c_int, C.c_double, C.c_int, vp, vp]
+            L.fvo_ad_count_stage.argtypes = [vp, vp, C.c_int, C.c_double, vp, vp]
             cls._lib = L
         return cls._lib
 
@@ -351,3 +353,21 @@ class OracleAD:
         assert self.L.fvo_ad_steps_jvp(C.byref(self.ccfg), C.byref(self.mesh.soa), st, len(SCHEMES[scheme]),
                                        float(dt), int(nsteps), _ptr(U), _ptr(V), _ptr(S), _ptr(JV)) == 0
         return S, JV
+
+    def count_steps(self, U, dt, scheme="ssprk3", nsteps=1):
+        """FP64 operations of nsteps steps: (add/sub, mul, div, sqrt)."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        out = np.zeros(4, np.uint64)
+        st = (C.c_int * len(SCHEMES[scheme]))(*SCHEMES[scheme])
+        assert self.L.fvo_ad_count_steps(C.byref(self.ccfg), C.byref(self.mesh.soa), st, len(SCHEMES[scheme]),
+                                         float(dt), int(nsteps), _ptr(U), out.ctypes.data) == 0
+        return out
+
+    def count_stage(self, U, irk, dt):
+        """FP64 operations of one stage: (faceinterp, residual + RK(irk)),
+        each (add/sub, mul, div, sqrt)."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        out = np.zeros(8, np.uint64)
+        assert self.L.fvo_ad_count_stage(C.byref(self.ccfg), C.byref(self.mesh.soa), int(irk), float(dt), _ptr(U),
+                                         out.ctypes.data) == 0
+        return out[:4], out[4:]

@@ -56,3 +56,20 @@ def test_ad_step_tangent_matches_central_differences():
     fd = (orc.step(U + eps * V, dt, "ssprk3", 2) - orc.step(U - eps * V, dt, "ssprk3", 2)) / (2 * eps)
     err = np.linalg.norm(JV - fd) / np.linalg.norm(fd)
     assert err <= 1e-6, err
+
+
+def test_fp64_operation_counts_match_committed_figures():
+    """profiles/traffic.json carries the FP64 operation counts bench.py uses for
+    the FP64 path's roofline; recount them (smaller mesh, same generator)."""
+    import json
+    import os
+
+    from fv_140823_gb300 import cases
+    with open(os.path.join(os.path.dirname(__file__), "..", "profiles", "traffic.json")) as fh:
+        figs = json.load(fh)["fp64_ops"]
+    c = cases.periodic(level=5)
+    dt = Oracle(c.tables, c.cfg).cfl_dt(c.U, 0.5)
+    fi, rr = OracleAD(c.tables, c.cfg).count_stage(c.U, 3, dt)
+    n = c.tables.ncells
+    assert rr.sum() / n == figs["residual_per_cell"]      # no data-dependent branch in the residual's count
+    assert abs(fi.sum() / n - figs["faceinterp_per_cell"]) <= 0.02 * figs["faceinterp_per_cell"]
