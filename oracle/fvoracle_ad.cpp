@@ -11,8 +11,9 @@
 // dot-product test <w, J v> = <J^T w, v> uses these JVPs.
 //
 // Scope: ideal / stiffened gas (model 1), first order and MUSCL/minmod,
-// inviscid, boundary codes 1 (inflow) and 2 (transmissive), 1:4 faces,
-// periodic meshes.
+// inviscid or viscous (Green-Gauss gradients, turb = 0, with or without the
+// energy work term), boundary codes 1 (inflow) and 2 (transmissive), 1:4
+// faces, periodic meshes.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -78,6 +79,7 @@ template <typename T>
 struct FState {
   T r, u, v, w, e, p, c;
   T vec[NEQ];
+  T g[9];  // ux uy uz vx vy vz wx wy wz: gradients of rho u, rho v, rho w (facercnstr.c:73-85)
 };
 
 // facevalues.c:113-129 / facercnstr.c:20-35 (model 1)
@@ -252,13 +254,96 @@ void faceinterp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, T 
   }
 }
 
+// gradcalc.c:9-47 (Green-Gauss, first-order face states; oracle fvo_gradcalc)
 template <typename T>
-void rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, const T *SF, T *R) {
+void gradcalc(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, T *SG) {
+  const int64_t n = m->ncells;
+  for (int64_t c = 0; c < n; ++c) {
+    T g[NEQ + 1][3];
+    for (int iv = 0; iv <= NEQ; ++iv) g[iv][0] = g[iv][1] = g[iv][2] = T(0.0);
+    T own[NEQ];
+    for (int v = 0; v < NEQ; ++v) own[v] = U[int64_t(v) * n + c];
+    const double Vol = m->vol[c];
+    for (int f = 0; f < 6; ++f) {
+      const int32_t code = m->nbr[int64_t(f) * n + c];
+      const double *fr = m->frames + 9 * f;
+      const int nsub = code <= FVGPU_HANG0 ? 4 : 1;
+      for (int ing = 0; ing < nsub; ++ing) {
+        FState<T> s, s1;
+        face_state(cfg, own, s);
+        double A;
+        if (code >= 0) {
+          T q[NEQ];
+          for (int v = 0; v < NEQ; ++v) q[v] = U[int64_t(v) * n + code];
+          face_state(cfg, q, s1);
+          A = m->area[int64_t(f) * n + c];
+        } else if (code <= FVGPU_HANG0) {
+          const int64_t r = FVGPU_HANG0 - code;
+          T q[NEQ];
+          for (int v = 0; v < NEQ; ++v) q[v] = U[int64_t(v) * n + m->hang_nbr[4 * r + ing]];
+          face_state(cfg, q, s1);
+          A = m->hang_area[4 * r + ing];
+        } else {
+          face_state(cfg, own, s1);
+          if (-1 - code == 1) inflow_state(cfg, s1);
+          A = m->area[int64_t(f) * n + c];
+        }
+        for (int iv = 0; iv < NEQ; ++iv)
+          for (int d = 0; d < 3; ++d) g[iv][d] += T(0.5) * (s1.vec[iv] + s.vec[iv]) * T(fr[d]) * T(A) / T(Vol);
+        for (int d = 0; d < 3; ++d) g[NEQ][d] += T(0.5) * (s1.p + s.p) * T(fr[d]) * T(A) / T(Vol);
+      }
+    }
+    for (int iv = 0; iv <= NEQ; ++iv)
+      for (int d = 0; d < 3; ++d) SG[(int64_t(iv) * 3 + d) * n + c] = g[iv][d];
+  }
+}
+
+// flux_viscous.c:57-232 with turb = 0 (oracle flux_visc)
+template <typename T>
+void flux_visc(const fvgpu_config *cfg, const FState<T> &s, const FState<T> &s1, T FV[NEQ][3]) {
+  const T h(0.5);
+  const T uf = h * (s.u + s1.u), vf = h * (s.v + s1.v), wf = h * (s.w + s1.w);
+  const T ux = h * (s.g[0] + s1.g[0]), uy = h * (s.g[1] + s1.g[1]), uz = h * (s.g[2] + s1.g[2]);
+  const T vx = h * (s.g[3] + s1.g[3]), vy = h * (s.g[4] + s1.g[4]), vz = h * (s.g[5] + s1.g[5]);
+  const T wx = h * (s.g[6] + s1.g[6]), wy = h * (s.g[7] + s1.g[7]), wz = h * (s.g[8] + s1.g[8]);
+  const T mu = T(cfg->visc) + T(0.0);
+  const T txx = mu * (T(2.0) * ux - T(2.0 / 3.0) * (ux + vy + wz));
+  const T tyy = mu * (T(2.0) * vy - T(2.0 / 3.0) * (ux + vy + wz));
+  const T tzz = mu * (T(2.0) * wz - T(2.0 / 3.0) * (ux + vy + wz));
+  const T txy = mu * (uy + vx);
+  const T txz = mu * (uz + wx);
+  const T tyz = mu * (vz + wy);
+  FV[0][0] = FV[0][1] = FV[0][2] = T(0.0);
+  FV[1][0] = txx;
+  FV[1][1] = txy;
+  FV[1][2] = txz;
+  FV[2][0] = txy;
+  FV[2][1] = tyy;
+  FV[2][2] = tyz;
+  FV[3][0] = txz;
+  FV[3][1] = tyz;
+  FV[3][2] = tzz;
+  if (cfg->eos == 1) {
+    FV[4][0] = uf * txx + vf * txy + wf * txz;
+    FV[4][1] = uf * txy + vf * tyy + wf * tyz;
+    FV[4][2] = uf * txz + vf * tyz + wf * tzz;
+  }
+}
+
+template <typename T>
+void rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, const T *SF, const T *SG, T *R) {
   const int64_t n = m->ncells;
   const bool muscl = cfg->ischeme == 2;
+  const bool ns = cfg->ns == 1;
+  auto grad9 = [&](int64_t k, T *g) {
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) g[a * 3 + d] = SG[(int64_t(1 + a) * 3 + d) * n + k];
+  };
   for (int64_t c = 0; c < n; ++c) {
     T acc[NEQ];
     for (int iv = 0; iv < NEQ; ++iv) acc[iv] = T(0.0);
+    T FV[NEQ][3];
+    for (int iv = 0; iv < NEQ; ++iv) FV[iv][0] = FV[iv][1] = FV[iv][2] = T(0.0);
     for (int f = 0; f < 6; ++f) {
       const int32_t code = m->nbr[int64_t(f) * n + c];
       const double *fr = m->frames + 9 * f;
@@ -270,6 +355,7 @@ void rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, const T *
       for (int v = 0; v < NEQ; ++v) qown[v] = muscl ? SF[(int64_t(f) * NEQ + v) * n + c] : U[int64_t(v) * n + c];
       FState<T> s;
       face_state(cfg, qown, s);
+      if (ns) grad9(c, s.g);
       for (int ineig = 0; ineig < nsub; ++ineig) {
         FState<T> s1;
         double A;
@@ -291,12 +377,14 @@ void rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, const T *
           T q[NEQ];
           for (int v = 0; v < NEQ; ++v) q[v] = muscl ? SF[(int64_t(nf) * NEQ + v) * n + k] : U[int64_t(v) * n + k];
           face_state(cfg, q, s1);
+          if (ns) grad9(k, s1.g);
         }
+        if (ns) flux_visc(cfg, s, s1, FV);
         T F[NEQ][3], FH[NEQ];
         hllc(fr, boundary ? -1 - code : 0, s, s1, F, FH);
         for (int iv = 0; iv < NEQ; ++iv)
-          flux_face[iv] += -T(A) * (((F[iv][0] - T(0.0)) * T(fr[0]) + (F[iv][1] - T(0.0)) * T(fr[1]) +
-                                     (F[iv][2] - T(0.0)) * T(fr[2])) +
+          flux_face[iv] += -T(A) * (((F[iv][0] - FV[iv][0]) * T(fr[0]) + (F[iv][1] - FV[iv][1]) * T(fr[1]) +
+                                     (F[iv][2] - FV[iv][2]) * T(fr[2])) +
                                     FH[iv]);
       }
       for (int iv = 0; iv < NEQ; ++iv) acc[iv] += flux_face[iv];
@@ -307,12 +395,16 @@ void rhs(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, const T *
 
 template <typename T>
 void residual(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const T *U, T *R) {
-  std::vector<T> SF;
+  std::vector<T> SF, SG;
   if (cfg->ischeme == 2) {
     SF.resize(size_t(6 * NEQ * m->ncells));
     faceinterp(cfg, m, U, SF.data());
   }
-  rhs(cfg, m, U, cfg->ischeme == 2 ? SF.data() : nullptr, R);
+  if (cfg->ns == 1) {
+    SG.resize(size_t(3 * (NEQ + 1) * m->ncells));
+    gradcalc(cfg, m, U, SG.data());
+  }
+  rhs(cfg, m, U, cfg->ischeme == 2 ? SF.data() : nullptr, cfg->ns == 1 ? SG.data() : nullptr, R);
 }
 
 // RK.c:16-47 stage formulas
@@ -341,7 +433,7 @@ extern "C" {
 
 // R(U) with T = double (bit-identical to fvo_rhs after fvo_faceinterp).
 int fvo_ad_residual(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U, double *R) {
-  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  if (cfg->model != 1) return -1;
   residual<double>(cfg, m, U, R);
   return 0;
 }
@@ -349,7 +441,7 @@ int fvo_ad_residual(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const doub
 // R(U) and J(U) V in one forward-mode pass.
 int fvo_ad_jvp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U, const double *V, double *R,
                double *JV) {
-  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  if (cfg->model != 1) return -1;
   const int64_t N = NEQ * m->ncells;
   std::vector<Dual> Ud(static_cast<size_t>(N)), Rd(static_cast<size_t>(N));
   for (int64_t i = 0; i < N; ++i) Ud[size_t(i)] = Dual(U[i], V[i]);
@@ -365,7 +457,7 @@ int fvo_ad_jvp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const double *U
 // tangent (the directional derivative of the step map).
 int fvo_ad_steps_jvp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const int *stages, int nstages, double dt,
                      int nsteps, const double *U, const double *V, double *S_out, double *JV) {
-  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  if (cfg->model != 1) return -1;
   const int64_t N = NEQ * m->ncells;
   std::vector<Dual> S(static_cast<size_t>(N)), SN(static_cast<size_t>(N)), R(static_cast<size_t>(N));
   for (int64_t i = 0; i < N; ++i) S[size_t(i)] = Dual(U[i], V[i]);
@@ -388,7 +480,7 @@ int fvo_ad_steps_jvp(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const int
 // additions / subtractions, multiplications, divisions, square roots.
 int fvo_ad_count_steps(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const int *stages, int nstages, double dt,
                        int nsteps, const double *U, uint64_t *counts) {
-  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  if (cfg->model != 1) return -1;
   const int64_t N = NEQ * m->ncells;
   std::vector<Cnt> S(static_cast<size_t>(N)), SN(static_cast<size_t>(N)), R(static_cast<size_t>(N));
   for (int64_t i = 0; i < N; ++i) S[size_t(i)] = Cnt(U[i]);
@@ -411,7 +503,7 @@ int fvo_ad_count_steps(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, const i
 // counts[4..7] residual with the fused RK(irk) update (kinds as above).
 int fvo_ad_count_stage(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, int irk, double dt, const double *U,
                        uint64_t *counts) {
-  if (cfg->model != 1 || cfg->ns != 0) return -1;
+  if (cfg->model != 1) return -1;
   const int64_t N = NEQ * m->ncells;
   std::vector<Cnt> S(static_cast<size_t>(N)), SN(static_cast<size_t>(N)), R(static_cast<size_t>(N));
   std::vector<Cnt> SF(static_cast<size_t>(6 * N));
@@ -423,7 +515,9 @@ int fvo_ad_count_stage(const fvgpu_config *cfg, const fvgpu_mesh_soa *m, int irk
   counts[2] = g_ops.div;
   counts[3] = g_ops.sqrt;
   g_ops = OpCounts{0, 0, 0, 0};
-  rhs(cfg, m, S.data(), cfg->ischeme == 2 ? SF.data() : nullptr, R.data());
+  std::vector<Cnt> SG(static_cast<size_t>(3 * (NEQ + 1) * m->ncells));
+  if (cfg->ns == 1) gradcalc(cfg, m, S.data(), SG.data());
+  rhs(cfg, m, S.data(), cfg->ischeme == 2 ? SF.data() : nullptr, SG.data(), R.data());
   rk<Cnt>(irk, dt, m, S.data(), SN.data(), R.data());
   counts[4] = g_ops.add;
   counts[5] = g_ops.mul;

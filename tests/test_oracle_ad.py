@@ -11,7 +11,7 @@ import pytest
 from fvtest import bits_equal, load_golden
 from pyoracle import Oracle, OracleAD
 
-AD_CASES = ["amr_periodic_first", "amr_periodic_muscl", "inflow_l3", "sod_l3"]
+AD_CASES = ["amr_periodic_first", "amr_periodic_muscl", "inflow_l3", "sod_l3", "tgv_l3"]
 
 
 @pytest.mark.parametrize("name", AD_CASES)
@@ -28,7 +28,7 @@ def test_ad_residual_and_steps_match_reference_golden(name):
 # Sod's piecewise-constant state sits on the minmod kink everywhere (a zero
 # jump takes the |d0| <= 1e-10 branch; any perturbation leaves it), so the
 # residual has no derivative there and central differences are meaningless.
-@pytest.mark.parametrize("name", [c for c in AD_CASES if c != "sod_l3"])
+@pytest.mark.parametrize("name", [c for c in AD_CASES if c not in ("sod_l3", "tgv_l3")])
 def test_ad_jvp_matches_central_differences(name):
     t, cfg, z = load_golden(name)
     ad, orc = OracleAD(t, cfg), Oracle(t, cfg)
@@ -41,6 +41,33 @@ def test_ad_jvp_matches_central_differences(name):
     fd = (orc.residual(U + eps * V) - orc.residual(U - eps * V)) / (2 * eps)
     err = np.linalg.norm(JV - fd) / np.linalg.norm(fd)
     assert err <= 1e-6, err
+
+
+def test_ad_viscous_jvp_matches_central_differences():
+    """Gradients (gradcalc) and viscous fluxes (flux_viscous, energy work term
+    on and off).  The Taylor-Green state's symmetries put minmod kinks
+    everywhere, so it is perturbed by 0.1 % seeded noise; the viscous part of
+    the tangent (tangent at visc minus tangent at visc = 0) is compared on its
+    own, with viscosity raised so that it stands above the difference noise."""
+    import dataclasses
+    t, cfg, z = load_golden("tgv_l3")
+    rng = np.random.default_rng(5)
+    U = z["U"] * (1 + 1e-3 * rng.standard_normal(z["U"].shape))
+    U[3] += 1e-3 * rng.standard_normal(U.shape[1])
+    V = rng.standard_normal(U.shape) * np.abs(U).mean(axis=1, keepdims=True)
+    eps = 1e-7
+    for eos in (0, 1):
+        parts = []
+        for visc in (0.5, 0.0):
+            c = dataclasses.replace(cfg, visc=visc, eos=eos)
+            ad, orc = OracleAD(t, c), Oracle(t, c)
+            R, JV = ad.jvp(U, V)
+            assert bits_equal(R, orc.residual(U))
+            fd = (orc.residual(U + eps * V) - orc.residual(U - eps * V)) / (2 * eps)
+            parts.append((JV, fd))
+        dj, dfd = parts[0][0] - parts[1][0], parts[0][1] - parts[1][1]
+        err = np.linalg.norm(dj - dfd) / np.linalg.norm(dfd)
+        assert err <= 1e-3, (eos, err)
 
 
 def test_ad_step_tangent_matches_central_differences():
