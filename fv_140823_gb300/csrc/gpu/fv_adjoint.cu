@@ -20,8 +20,9 @@
 // Forward quantities (states, wave speeds, HLLC region, limiter branch) are
 // recomputed with the same expressions as the forward kernels, so branch
 // decisions match the forward residual exactly.  Scope: model 1, inviscid,
-// first order or MUSCL/minmod, boundary codes other than the walls 3 and 4
-// (inflow 1, transmissive 2), 1:4 faces, periodic meshes.
+// first order or MUSCL/minmod, inviscid or viscous (4th pass: reverse of the
+// Green-Gauss gradients the viscous flux reads), boundary codes other than
+// the walls 3 and 4 (inflow 1, transmissive 2), 1:4 faces, periodic meshes.
 #include "fv_adjoint.cuh"
 
 #include <cstdio>
@@ -79,7 +80,8 @@ __device__ __forceinline__ void rev_state(const Phys &ph, const double q[NV], co
 // Reverse of the HLLC normal flux Phi = F(U_K).n + S_K (U*_K - U_K) of face
 // frame f: given Phib, accumulate qLb and qRb.
 __device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], const double qR[NV],
-                         const double Phib[NV], double qLb[NV], double qRb[NV]) {
+                         const double Phib[NV], const double velLb[3], const double velRb[3], double qLb[NV],
+                         double qRb[NV]) {
   const double *fr = ph.frames + 9 * f;
   const double nx = fr[0], ny = fr[1], nz = fr[2], mx = fr[3], my = fr[4], mz = fr[5], lx = fr[6], ly = fr[7],
                lz = fr[8];
@@ -216,8 +218,65 @@ __device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], con
   uxRb += uRb * nx + vRb * mx + wRb * lx;
   uyRb += uRb * ny + vRb * my + wRb * ly;
   uzRb += uRb * nz + vRb * mz + wRb * lz;
+  uxLb += velLb[0];  // viscous flux: face-averaged velocity
+  uyLb += velLb[1];
+  uzLb += velLb[2];
+  uxRb += velRb[0];
+  uyRb += velRb[1];
+  uzRb += velRb[2];
   rev_state(ph, qL, L, rLb, uxLb, uyLb, uzLb, eLb, pLb, cLb, qLb);
   rev_state(ph, qR, R, rRb, uxRb, uyRb, uzRb, eRb, pRb, cRb, qRb);
+}
+
+// Reverse of flux_viscous (flux_viscous.c:57-232, turb = 0) contracted with
+// the face normal: given the residual weight Phib (= -A w) of one face
+// evaluation, the bars of the face-averaged velocity gradients (gb, order
+// ux uy uz vx vy vz wx wy wz) and of the face-averaged velocity (ufb) when
+// the energy work term is on.  uf and g9 are the forward face averages.
+__device__ __forceinline__ void visc_vjp(const Phys &ph, const double *fr, const double Phib[NV],
+                                         const double uf[3], const double g9[9], double gb[9], double ufb[3]) {
+  // R_c += A (FV . n): FV bars are -Phib n
+  double FVb[NV][3];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) FVb[v][d] = -Phib[v] * fr[d];
+  const double mu = ph.visc + 0.0;
+  const double ux = g9[0], uy = g9[1], uz = g9[2], vx = g9[3], vy = g9[4], vz = g9[5], wx = g9[6], wy = g9[7],
+               wz = g9[8];
+  double txxb = FVb[1][0], txyb = FVb[1][1] + FVb[2][0], txzb = FVb[1][2] + FVb[3][0];
+  double tyyb = FVb[2][1], tyzb = FVb[2][2] + FVb[3][1], tzzb = FVb[3][2];
+  ufb[0] = ufb[1] = ufb[2] = 0.0;
+  if (ph.eos == 1) {
+    const double D = ux + vy + wz;
+    const double txx = mu * (2.0 * ux - (2.0 / 3.0) * D), tyy = mu * (2.0 * vy - (2.0 / 3.0) * D);
+    const double tzz = mu * (2.0 * wz - (2.0 / 3.0) * D);
+    const double txy = mu * (uy + vx), txz = mu * (uz + wx), tyz = mu * (vz + wy);
+    const double *e = FVb[4];
+    ufb[0] = e[0] * txx + e[1] * txy + e[2] * txz;
+    ufb[1] = e[0] * txy + e[1] * tyy + e[2] * tyz;
+    ufb[2] = e[0] * txz + e[1] * tyz + e[2] * tzz;
+    txxb += uf[0] * e[0];
+    txyb += uf[1] * e[0] + uf[0] * e[1];
+    txzb += uf[2] * e[0] + uf[0] * e[2];
+    tyyb += uf[1] * e[1];
+    tyzb += uf[2] * e[1] + uf[1] * e[2];
+    tzzb += uf[2] * e[2];
+  }
+  const double Db = -(2.0 / 3.0) * mu * (txxb + tyyb + tzzb);
+  gb[0] = 2.0 * mu * txxb + Db;
+  gb[4] = 2.0 * mu * tyyb + Db;
+  gb[8] = 2.0 * mu * tzzb + Db;
+  gb[1] = gb[3] = mu * txyb;
+  gb[2] = gb[6] = mu * txzb;
+  gb[5] = gb[7] = mu * tyzb;
+}
+
+__device__ __forceinline__ void load9(const double *__restrict__ SG, int64_t n, int64_t c, double g[9]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[a * 3 + d] = SG[((1 + a) * 3 + d) * n + c];
 }
 
 __device__ __forceinline__ void load5(const double *__restrict__ A, int64_t n, int64_t c, double q[NV]) {
@@ -286,8 +345,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArg
   if (c >= m.n) return;
   const int64_t n = m.n;
   const bool muscl = ph.ischeme == 2;
+  const bool ns = ph.ns == 1;
   double w[NV];
   load5(a.w, n, c, w);
+  double gown[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // bars of this cell's gradients
   for (int f = 0; f < 6; ++f) {
     const int32_t code = m.nbr[f * n + c];
     const bool boundary = is_boundary(code);
@@ -320,7 +381,35 @@ __global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArg
       double Phib[NV], gr[NV] = {0, 0, 0, 0, 0};
 #pragma unroll
       for (int v = 0; v < NV; ++v) Phib[v] = -(A)*w[v];
-      hllc_vjp(ph, f, boundary ? -1 - code : 0, qL, qR, Phib, gl, gr);
+      double vLb[3] = {0, 0, 0}, vRb[3] = {0, 0, 0}, gnb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      if (ns) {
+        // forward face averages: velocities of both face states, gradients of both cells
+        double gL9[9], gR9[9], g9[9], uf[3];
+        load9(a.SG, n, c, gL9);
+        if (k >= 0)
+          load9(a.SG, n, k, gR9);
+        else
+#pragma unroll
+          for (int i = 0; i < 9; ++i) gR9[i] = gL9[i];  // a ghost carries the own gradients
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g9[i] = 0.5 * (gL9[i] + gR9[i]);
+        uf[0] = 0.5 * (qL[1] / qL[0] + qR[1] / qR[0]);
+        uf[1] = 0.5 * (qL[2] / qL[0] + qR[2] / qR[0]);
+        uf[2] = 0.5 * (qL[3] / qL[0] + qR[3] / qR[0]);
+        double gb[9], ufb[3];
+        visc_vjp(ph, ph.frames + 9 * f, Phib, uf, g9, gb, ufb);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vLb[d] = vRb[d] = 0.5 * ufb[d];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          gown[i] += 0.5 * gb[i];
+          gnb[i] = 0.5 * gb[i];
+        }
+        if (boundary)
+#pragma unroll
+          for (int i = 0; i < 9; ++i) gown[i] += gnb[i];
+      }
+      hllc_vjp(ph, f, boundary ? -1 - code : 0, qL, qR, Phib, vLb, vRb, gl, gr);
       if (boundary) {
         if (-1 - code != 1)  // every supported code but inflow: ghost = own face value
 #pragma unroll
@@ -328,15 +417,24 @@ __global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArg
       } else if (code >= 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) a.gR[(f * NV + v) * n + c] = gr[v];
+        if (ns)
+#pragma unroll
+          for (int i = 0; i < 9; ++i) a.gRg[(f * 9 + i) * n + c] = gnb[i];
       } else {
         const int64_t r = hang_index(code);
 #pragma unroll
         for (int v = 0; v < NV; ++v) a.gRh[(r * 4 + s) * NV + v] = gr[v];
+        if (ns)
+#pragma unroll
+          for (int i = 0; i < 9; ++i) a.gRgh[(r * 4 + s) * 9 + i] = gnb[i];
       }
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) a.gL[(f * NV + v) * n + c] = gl[v];
   }
+  if (ns)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) a.gG[i * n + c] = gown[i];
 }
 
 // 2. adjoint of every face value: own evaluations + neighbour evaluations
@@ -374,7 +472,38 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs
 #pragma unroll
     for (int v = 0; v < NV; ++v) a.gSF[(f * NV + v) * n + c] = g[v];
   }
-  (void)ph;
+  if (ph.ns != 1) return;
+  // adjoint of this cell's gradients: own evaluations + the neighbour
+  // evaluations that read them (as s1.g)
+  double gt[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) gt[i] = a.gG[i * n + c];
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = m.nbr[f * n + c];
+    if (is_boundary(code)) continue;
+    const int nf = m.nbr_face[f * n + c];
+    if (code >= 0) {
+      const int32_t back = m.nbr[nf * n + code];
+      if (back >= 0) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gt[i] += a.gRg[(nf * 9 + i) * n + code];
+      } else {
+        const int64_t r = hang_index(back);
+        int sub = 0;
+        for (int s = 0; s < 4; ++s)
+          if (m.hang_nbr[4 * r + s] == c) sub = s;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gt[i] += a.gRgh[(r * 4 + sub) * 9 + i];
+      }
+    } else {
+      const int32_t *k = m.hang_nbr + 4 * hang_index(code);
+      for (int s = 0; s < 4; ++s)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gt[i] += a.gRg[(nf * 9 + i) * n + k[s]];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) a.gSG[i * n + c] = gt[i];
 }
 
 // 3. reverse of the reconstruction
@@ -441,6 +570,68 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
   for (int v = 0; v < NV; ++v) a.out[v * n + c] = gu[v];
 }
 
+// 4. reverse of gradcalc (gradcalc.c:9-47) for the momentum rows the viscous
+// flux reads: SG_k[1+a][d] = sum over k's faces 0.5 (q_nb + q_k)[1+a] n_d A / V_k
+__global__ void __launch_bounds__(kBlock) k_adj_grad(Phys ph, MeshView m, AdjArgs a) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const int64_t n = m.n;
+  const double Vc = m.vol[c];
+  double coef[3] = {0, 0, 0};  // d SG_c[.][d] / d q_c
+  double acc[3] = {0, 0, 0};   // contributions of the neighbours' gradients, per momentum row
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = m.nbr[f * n + c];
+    const double *fr = ph.frames + 9 * f;
+    if (is_boundary(code)) {
+      const double own = (-1 - code == 1) ? 0.5 : 1.0;  // ghost = own state except at an inflow
+      const double A = m.area[f * n + c];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) coef[d] += own * fr[d] * A / Vc;
+      continue;
+    }
+    const int nf = m.nbr_face[f * n + c];
+    const double *fk = ph.frames + 9 * nf;
+    const int nsub = is_hanging(code) ? 4 : 1;
+    for (int s = 0; s < nsub; ++s) {
+      int64_t k;
+      double A;  // this cell's (sub-)face area
+      if (code >= 0) {
+        k = code;
+        A = m.area[f * n + c];
+      } else {
+        const int64_t r = hang_index(code);
+        k = m.hang_nbr[4 * r + s];
+        A = m.hang_area[4 * r + s];
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) coef[d] += 0.5 * fr[d] * A / Vc;
+      // the area of k's (sub-)face toward this cell
+      double Ak;
+      const int32_t back = m.nbr[nf * n + k];
+      if (back >= 0) {
+        Ak = m.area[nf * n + k];
+      } else {
+        const int64_t r = hang_index(back);
+        Ak = 0.0;
+        for (int t = 0; t < 4; ++t)
+          if (m.hang_nbr[4 * r + t] == c) Ak = m.hang_area[4 * r + t];
+      }
+      const double wk = 0.5 * Ak / m.vol[k];
+#pragma unroll
+      for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[aa] += a.gSG[(aa * 3 + d) * n + k] * fk[d] * wk;
+    }
+  }
+#pragma unroll
+  for (int aa = 0; aa < 3; ++aa) {
+    double g = acc[aa];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g += a.gSG[(aa * 3 + d) * n + c] * coef[d];
+    a.out[(1 + aa) * n + c] += g;
+  }
+}
+
 // w = coef * dt / V * g (the residual weight of a stage's adjoint)
 __global__ void k_adj_scale(MeshView m, const double *__restrict__ g, const double *__restrict__ dt, double coef,
                             double *__restrict__ w) {
@@ -463,8 +654,8 @@ unsigned grid_of(int64_t n) { return unsigned((n + kBlock - 1) / kBlock); }
 }  // namespace
 
 bool adjoint_supported(const Phys &ph, char *why, size_t whylen) {
-  if (ph.model != 1 || ph.ns != 0) {
-    snprintf(why, whylen, "the adjoint implements model 1 without viscous fluxes");
+  if (ph.model != 1) {
+    snprintf(why, whylen, "the adjoint implements model 1 (ideal / stiffened gas)");
     return false;
   }
   return true;
@@ -474,6 +665,7 @@ void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStr
   k_adj_flux<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   k_adj_gsf<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   k_adj_recon<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  if (ph.ns == 1) k_adj_grad<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
 }
 
 void launch_adj_scale(const MeshView &m, const double *g, const double *dt, double coef, double *w, cudaStream_t st) {

@@ -21,6 +21,13 @@ namespace fv {
 //                         neighbour
 //   gSF [6][5][n]         adjoint of every face value (may alias gL)
 //   out [5][n]            result
+// viscous runs (ns 1) also:
+//   SG   [neq+1][3][n]    gradients of U (gradcalc)
+//   gG   [9][n]           bars of each cell's momentum gradients from its own
+//                         evaluations
+//   gRg  [6][9][n]        per single-neighbour face: the neighbour's gradient bars
+//   gRgh [nhang][4][9]    per 1:4 sub-face: the fine neighbour's gradient bars
+//   gSG  [9][n]           total gradient bars (may alias gG)
 struct AdjArgs {
   const double *U;
   const double *SF;
@@ -30,13 +37,19 @@ struct AdjArgs {
   double *gRh;
   double *gSF;
   double *out;
+  const double *SG;
+  double *gG;
+  double *gRg;
+  double *gRgh;
+  double *gSG;
 };
 
-// true when the adjoint implements the configuration (model 1, inviscid);
+// true when the adjoint implements the configuration (model 1);
 // otherwise writes the reason
 bool adjoint_supported(const Phys &ph, char *why, size_t whylen);
 
-// the three gather passes of g = (dR/dU)^T w (faceinterp of U must precede)
+// the gather passes of g = (dR/dU)^T w (faceinterp of U, and gradcalc of U
+// for ns 1, must precede)
 void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStream_t st);
 
 // w = coef * dt / vol * g

@@ -90,6 +90,7 @@ struct fvgpu_ctx {
   // adjoint work arrays (allocated by the first adjoint call)
   unsigned bc_mask = 0;  // bit b set when boundary code b occurs in the mesh
   DevBuf adjL, adjR, adjRh, adjW, adjG, adjAcc, adjOut, adjY1, adjY2, adjSN, adjCK;
+  DevBuf adjGo, adjRg, adjRgh;  // viscous: gradient bars
   // halo exchange index lists
   DevBuf halo_send, halo_recv;
   int64_t nsend = 0, nrecv = 0;
@@ -541,6 +542,12 @@ int ensure_adjoint(fvgpu_ctx *ctx) {
   FV_CUDA(ctx, ctx->adjRh.alloc(sizeof(double) * 4 * size_t(ctx->neq) * size_t(ctx->nhang)));
   for (DevBuf *b : {&ctx->adjW, &ctx->adjG, &ctx->adjAcc, &ctx->adjOut, &ctx->adjY1, &ctx->adjY2, &ctx->adjSN})
     FV_CUDA(ctx, b->alloc(cell));
+  if (ctx->cfg.ns == 1) {
+    const size_t row = sizeof(double) * size_t(ctx->n);
+    FV_CUDA(ctx, ctx->adjGo.alloc(9 * row));
+    FV_CUDA(ctx, ctx->adjRg.alloc(54 * row));
+    FV_CUDA(ctx, ctx->adjRgh.alloc(sizeof(double) * 36 * size_t(ctx->nhang)));
+  }
   ctx->adj_ready = true;
   return FVGPU_OK;
 }
@@ -553,6 +560,11 @@ int enqueue_vjp(fvgpu_ctx *ctx, const double *U, const double *w, double *out) {
     fv::launch_faceinterp_fp64(ctx->ph, mv, U, ctx->SF.as<double>(), ctx->stream);
     FV_LAUNCHED(ctx);
   }
+  if (ctx->cfg.ns == 1) {
+    ctx->marks.mark(FVGPU_KIND_GRADCALC);
+    fv::launch_gradcalc_fp64(ctx->ph, mv, U, ctx->SG.as<double>(), ctx->d_err(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
   fv::AdjArgs a{};
   a.U = U;
   a.SF = ctx->SF.as<double>();
@@ -562,6 +574,11 @@ int enqueue_vjp(fvgpu_ctx *ctx, const double *U, const double *w, double *out) {
   a.gRh = ctx->adjRh.as<double>();
   a.gSF = ctx->adjL.as<double>();  // each face's total replaces its own-evaluation part in place
   a.out = out;
+  a.SG = ctx->SG.as<double>();
+  a.gG = ctx->adjGo.as<double>();
+  a.gRg = ctx->adjRg.as<double>();
+  a.gRgh = ctx->adjRgh.as<double>();
+  a.gSG = ctx->adjGo.as<double>();  // likewise for the gradient bars
   ctx->marks.mark(FVGPU_KIND_ADJOINT);
   fv::launch_adjoint(ctx->ph, mv, a, ctx->stream);
   FV_LAUNCHED(ctx);
@@ -585,6 +602,11 @@ int enqueue_stage_out_of_place(fvgpu_ctx *ctx, int irk, const double *S_in, doub
   if (ctx->cfg.ischeme == 2) {
     ctx->marks.mark(FVGPU_KIND_FACEINTERP);
     fv::launch_faceinterp_fp64(ctx->ph, ctx->view(), S_in, ctx->SF.as<double>(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  if (ctx->cfg.ns == 1) {
+    ctx->marks.mark(FVGPU_KIND_GRADCALC);
+    fv::launch_gradcalc_fp64(ctx->ph, ctx->view(), S_in, ctx->SG.as<double>(), ctx->d_err(), ctx->stream);
     FV_LAUNCHED(ctx);
   }
   fv::ResidualArgs a = residual_args(ctx);
@@ -746,7 +768,7 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   ctx->inner.release();
   ctx->has_inner = false;
   for (DevBuf *b : {&ctx->adjL, &ctx->adjR, &ctx->adjRh, &ctx->adjW, &ctx->adjG, &ctx->adjAcc, &ctx->adjOut,
-                    &ctx->adjY1, &ctx->adjY2, &ctx->adjSN, &ctx->adjCK})
+                    &ctx->adjY1, &ctx->adjY2, &ctx->adjSN, &ctx->adjCK, &ctx->adjGo, &ctx->adjRg, &ctx->adjRgh})
     b->release();
   ctx->adj_ck_steps = 0;
   ctx->adj_ready = false;
