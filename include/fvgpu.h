@@ -197,9 +197,10 @@ int fvgpu_halo_unpack(fvgpu_ctx *ctx, const double *recv_buf);
  * entry points give the transpose of the FP64 residual and step maps
  * (residual_faces_AMR.c with hllc_euler.c, faceinterp.c / reconctruct_V3.c,
  * RK.c), computed by hand-written reverse kernels: deterministic (gathers in a
- * fixed order, no atomics).  Scope: model 1, ns = 0, first order or MUSCL,
- * boundary codes other than the walls 3 and 4; other configurations return
- * FVGPU_ERR_UNSUPPORTED.  Derivatives are those of the branch the forward
+ * fixed order, no atomics).  Scope: model 1, inviscid or viscous (the
+ * reverse of flux_viscous and of the Green-Gauss gradients it reads, turb =
+ * 0), first order or MUSCL, boundary codes other than the walls 3 and 4;
+ * other configurations return FVGPU_ERR_UNSUPPORTED.  Derivatives are those of the branch the forward
  * takes at the given state (minmod, wave-speed and HLLC-region choices); at a
  * branch switch they are one-sided. */
 
