@@ -67,6 +67,14 @@ _GPU_SIGS = {
     "fvgpu_compute_dt": ([C.c_void_p, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "fvgpu_conservation": ([C.c_void_p, C.c_void_p], C.c_int),
     "fvgpu_residual_vjp": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_checkpoint_save": ([C.c_void_p, C.c_char_p, C.c_double, C.c_int64], C.c_int),
+    "fvgpu_checkpoint_load": ([C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)], C.c_int),
+    "fvgpu_checkpoint_write": ([C.c_char_p, C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double, C.c_int64],
+                               C.c_int),
+    "fvgpu_checkpoint_read": ([C.c_char_p, C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.POINTER(C.c_double),
+                               C.POINTER(C.c_int64)], C.c_int),
+    "fvgpu_mesh_signature": ([C.c_void_p, C.POINTER(C.c_uint64)], C.c_int),
+    "fvgpu_criterion": ([C.c_void_p, C.c_int, C.c_double, C.c_int32, C.c_void_p], C.c_int),
     "fvgpu_measure_fp64": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
     "fvgpu_halo_set": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64], C.c_int),
     "fvgpu_halo_pack": ([C.c_void_p, C.c_void_p], C.c_int),

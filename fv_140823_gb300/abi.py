@@ -112,3 +112,8 @@ class MeshSoaHolder:
         for k, a in self.arrays.items():
             setattr(self.soa, k, a.ctypes.data)
         self.ncells = int(t.ncells)
+
+# fvgpu_criterion kinds (criterionsplt.c)
+CRIT_GRAD_RHO = 0
+CRIT_RHO_BELOW = 1
+CRIT_GRAD_RHO_H = 2

@@ -89,6 +89,7 @@ struct fvgpu_ctx {
   std::string mixed_why;
   // adjoint work arrays (allocated by the first adjoint call)
   unsigned bc_mask = 0;  // bit b set when boundary code b occurs in the mesh
+  uint64_t mesh_sig = 0;  // FNV-1a of the uploaded tables (restart files carry it)
   DevBuf adjL, adjR, adjRh, adjW, adjG, adjAcc, adjOut, adjY1, adjY2, adjSN, adjCK;
   DevBuf adjGo, adjRg, adjRgh;  // viscous: gradient bars
   // halo exchange index lists
@@ -131,6 +132,17 @@ struct fvgpu_ctx {
 };
 
 namespace {
+
+// FNV-1a, 64 bit
+uint64_t fnv1a(uint64_t h, const void *data, size_t bytes) {
+  const unsigned char *p = static_cast<const unsigned char *>(data);
+  for (size_t i = 0; i < bytes; ++i) {
+    h ^= p[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+constexpr uint64_t kFnvSeed = 0xcbf29ce484222325ull;
 
 int set_err(fvgpu_ctx *ctx, int code, const char *fmt, ...) {
   char buf[512];
@@ -197,6 +209,24 @@ __global__ void k_cons_final(int neq, const double *__restrict__ partial, double
     }
     if (threadIdx.x == 0) sums[v] = red[0];
     __syncthreads();
+  }
+}
+
+// refinement flags, criterionsplt.c:24-86 (pow(x, 2.0) is x*x in the
+// compiled reference)
+__global__ void k_criterion(int kind, double threshold, int level_hi, int64_t n, const double *__restrict__ S,
+                            const double *__restrict__ SG, const double *__restrict__ vol, int32_t *__restrict__ split) {
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
+    bool hit;
+    if (kind == FVGPU_CRIT_RHO_BELOW) {
+      hit = S[c] < threshold;
+    } else {
+      const double gx = SG[0 * n + c], gy = SG[1 * n + c], gz = SG[2 * n + c];
+      double mag = sqrt(gx * gx + gy * gy + gz * gz);
+      if (kind == FVGPU_CRIT_GRAD_RHO_H) mag = mag * cbrt(vol[c]);
+      hit = mag > threshold;
+    }
+    split[c] = hit ? level_hi : 1;
   }
 }
 
@@ -775,6 +805,21 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   ctx->halo_send.release();
   ctx->halo_recv.release();
   ctx->nsend = ctx->nrecv = 0;
+  {
+    uint64_t h = kFnvSeed;
+    h = fnv1a(h, &m->ncells, sizeof(int64_t));
+    h = fnv1a(h, &m->nhang, sizeof(int64_t));
+    h = fnv1a(h, m->nbr, sizeof(int32_t) * 6 * size_t(n));
+    h = fnv1a(h, m->nbr_face, sizeof(int32_t) * 6 * size_t(n));
+    h = fnv1a(h, m->area, sizeof(double) * 6 * size_t(n));
+    h = fnv1a(h, m->vol, sizeof(double) * size_t(n));
+    if (nh > 0) {
+      h = fnv1a(h, m->hang_nbr, sizeof(int32_t) * 4 * size_t(nh));
+      h = fnv1a(h, m->hang_area, sizeof(double) * 4 * size_t(nh));
+    }
+    if (m->level) h = fnv1a(h, m->level, sizeof(int32_t) * size_t(n));
+    ctx->mesh_sig = h;
+  }
   ctx->bc_mask = 0;
   for (int64_t i = 0; i < 6 * n; ++i) {
     const int32_t code = m->nbr[i];
@@ -1064,6 +1109,113 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums) {
   k_cons_final<<<1, kConsThreads, 0, ctx->stream>>>(ctx->neq, part, d_sums);
   FV_LAUNCHED(ctx);
   FV_CUDA(ctx, cudaMemcpyAsync(sums, d_sums, sizeof(double) * (ctx->neq + 1), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  return sync_and_check(ctx);
+}
+
+// ---- restart files ---------------------------------------------------------------------
+
+namespace {
+struct CkHeader {
+  char magic[8];
+  uint32_t version, neq;
+  int64_t ncells;
+  uint64_t mesh_sig;
+  double time;
+  int64_t step;
+};
+static_assert(sizeof(CkHeader) == 48, "restart header layout");
+}  // namespace
+
+int fvgpu_checkpoint_write(const char *path, const double *U, int neq, int64_t ncells, uint64_t mesh_sig,
+                           double time, int64_t step) {
+  if (!path || !U || neq <= 0 || ncells <= 0) return FVGPU_ERR_ARG;
+  CkHeader h{};
+  memcpy(h.magic, "FVGPUCK1", 8);
+  h.version = 1;
+  h.neq = uint32_t(neq);
+  h.ncells = ncells;
+  h.mesh_sig = mesh_sig;
+  h.time = time;
+  h.step = step;
+  const size_t bytes = sizeof(double) * size_t(neq) * size_t(ncells);
+  const uint64_t sum = fnv1a(fnv1a(kFnvSeed, &h, sizeof h), U, bytes);
+  FILE *f = fopen(path, "wb");
+  if (!f) return FVGPU_ERR_ARG;
+  const bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(U, 1, bytes, f) == bytes && fwrite(&sum, 8, 1, f) == 1;
+  return (fclose(f) == 0 && ok) ? FVGPU_OK : FVGPU_ERR_ARG;
+}
+
+int fvgpu_checkpoint_read(const char *path, double *U, int neq, int64_t ncells, uint64_t mesh_sig, double *time,
+                          int64_t *step) {
+  if (!path || !U || neq <= 0 || ncells <= 0) return FVGPU_ERR_ARG;
+  FILE *f = fopen(path, "rb");
+  if (!f) return FVGPU_ERR_ARG;
+  CkHeader h{};
+  const size_t bytes = sizeof(double) * size_t(neq) * size_t(ncells);
+  uint64_t sum = 0;
+  int rc = FVGPU_OK;
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, "FVGPUCK1", 8) != 0 || h.version != 1)
+    rc = FVGPU_ERR_STATE;
+  else if (h.neq != uint32_t(neq) || h.ncells != ncells || h.mesh_sig != mesh_sig)
+    rc = FVGPU_ERR_STATE;
+  else if (fread(U, 1, bytes, f) != bytes || fread(&sum, 8, 1, f) != 1)
+    rc = FVGPU_ERR_STATE;
+  else if (fgetc(f) != EOF || sum != fnv1a(fnv1a(kFnvSeed, &h, sizeof h), U, bytes))
+    rc = FVGPU_ERR_STATE;
+  fclose(f);
+  if (rc == FVGPU_OK) {
+    if (time) *time = h.time;
+    if (step) *step = h.step;
+  }
+  return rc;
+}
+
+int fvgpu_mesh_signature(fvgpu_ctx *ctx, uint64_t *sig) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!sig) return set_err(ctx, FVGPU_ERR_ARG, "null output");
+  *sig = ctx->mesh_sig;
+  return FVGPU_OK;
+}
+
+int fvgpu_checkpoint_save(fvgpu_ctx *ctx, const char *path, double time, int64_t step) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  std::vector<double> U(size_t(ctx->neq) * size_t(ctx->n));
+  rc = fvgpu_download_state(ctx, U.data(), ctx->n);
+  if (rc) return rc;
+  rc = fvgpu_checkpoint_write(path, U.data(), ctx->neq, ctx->n, ctx->mesh_sig, time, step);
+  return rc ? set_err(ctx, rc, "cannot write restart file %s", path ? path : "(null)") : FVGPU_OK;
+}
+
+int fvgpu_checkpoint_load(fvgpu_ctx *ctx, const char *path, double *time, int64_t *step) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  std::vector<double> U(size_t(ctx->neq) * size_t(ctx->n));
+  rc = fvgpu_checkpoint_read(path, U.data(), ctx->neq, ctx->n, ctx->mesh_sig, time, step);
+  if (rc) return set_err(ctx, rc, "restart file %s does not match this mesh or is damaged", path ? path : "(null)");
+  rc = fvgpu_upload_state(ctx, U.data(), ctx->n);
+  if (rc) return rc;
+  return sync_and_check(ctx);
+}
+
+int fvgpu_criterion(fvgpu_ctx *ctx, int kind, double threshold, int32_t level_hi, int32_t *split) {
+  int rc = ensure_state(ctx);
+  if (rc) return rc;
+  if (!split || kind < FVGPU_CRIT_GRAD_RHO || kind > FVGPU_CRIT_GRAD_RHO_H)
+    return set_err(ctx, FVGPU_ERR_ARG, "bad criterion or output");
+  const size_t sg_bytes = sizeof(double) * size_t(ctx->neq + 1) * 3 * size_t(ctx->n);
+  if (kind != FVGPU_CRIT_RHO_BELOW && ctx->SG.bytes < sg_bytes)
+    return set_err(ctx, FVGPU_ERR_STATE, "no gradients: call fvgpu_gradcalc first");
+  cudaSetDevice(ctx->cfg.device);
+  DevBuf flags;
+  FV_CUDA(ctx, flags.alloc(sizeof(int32_t) * size_t(ctx->n)));
+  const unsigned blocks = unsigned(std::min<int64_t>((ctx->n + 255) / 256, 4096));
+  k_criterion<<<blocks, 256, 0, ctx->stream>>>(kind, threshold, level_hi, ctx->n, ctx->S.as<double>(),
+                                               ctx->SG.as<double>(), ctx->vol.as<double>(), flags.as<int32_t>());
+  FV_LAUNCHED(ctx);
+  FV_CUDA(ctx, cudaMemcpyAsync(split, flags.p, sizeof(int32_t) * size_t(ctx->n), cudaMemcpyDeviceToHost,
                                ctx->stream));
   return sync_and_check(ctx);
 }

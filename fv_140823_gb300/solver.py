@@ -172,6 +172,27 @@ class Solver:
         self._call("fvgpu_conservation", _ptr(out))
         return out
 
+    # -- restart and adaptation helpers ------------------------------------------
+    def checkpoint_save(self, path: str, time: float = 0.0, step: int = 0):
+        """Bit-exact binary restart file of the state (fvgpu_checkpoint_save)."""
+        self._call("fvgpu_checkpoint_save", str(path).encode(), float(time), C.c_int64(step))
+
+    def checkpoint_load(self, path: str) -> tuple[float, int]:
+        t, st = C.c_double(), C.c_int64()
+        self._call("fvgpu_checkpoint_load", str(path).encode(), C.byref(t), C.byref(st))
+        return t.value, st.value
+
+    def mesh_signature(self) -> int:
+        out = C.c_uint64()
+        self._call("fvgpu_mesh_signature", C.byref(out))
+        return out.value
+
+    def criterion(self, kind: int, threshold: float, level_hi: int) -> np.ndarray:
+        """Refinement flags of criterionsplt.c (abi.CRIT_*)."""
+        out = np.empty(self.n, np.int32)
+        self._call("fvgpu_criterion", int(kind), float(threshold), C.c_int32(level_hi), _ptr(out))
+        return out
+
     # -- halo exchange -------------------------------------------------------
     def halo_set(self, send_cells: np.ndarray, recv_cells: np.ndarray):
         """Local cells this rank packs for others / receives into (ghosts)."""
@@ -235,3 +256,23 @@ class Solver:
 
     def synchronize(self):
         self._call("fvgpu_synchronize")
+
+
+def checkpoint_write(path: str, U: np.ndarray, mesh_sig: int, time: float = 0.0, step: int = 0):
+    """Write a restart file from a host array (no GPU needed)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    rc = load_gpu_lib().fvgpu_checkpoint_write(str(path).encode(), _ptr(U), U.shape[0], C.c_int64(U.shape[1]),
+                                               C.c_uint64(mesh_sig), float(time), C.c_int64(step))
+    if rc != 0:
+        raise FvGpuError(rc, -1, f"cannot write {path}")
+
+
+def checkpoint_read(path: str, neq: int, ncells: int, mesh_sig: int):
+    """Read a restart file into a host array: (U, time, step)."""
+    U = np.empty((neq, ncells))
+    t, st = C.c_double(), C.c_int64()
+    rc = load_gpu_lib().fvgpu_checkpoint_read(str(path).encode(), _ptr(U), int(neq), C.c_int64(ncells),
+                                              C.c_uint64(mesh_sig), C.byref(t), C.byref(st))
+    if rc != 0:
+        raise FvGpuError(rc, -1, f"{path}: not a restart file of this mesh, or damaged")
+    return U, t.value, st.value

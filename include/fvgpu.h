@@ -176,6 +176,38 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
 int fvgpu_conservation_noalloc(const double *S, const double *vol, int64_t ncells, int neq, double *sums,
                                void *stream);
 
+/* ---- restart and adaptation helpers ------------------------------------ */
+/* Bit-exact binary restart of the state.  The reference writes its restart
+ * as "%15.10e" text (restart_save.c:41, restart_load.c), which drops about
+ * five significant digits; this file holds the FP64 state as stored: header
+ * {magic "FVGPUCK1", version 1, neq, ncells, mesh signature (FNV-1a of the
+ * uploaded neighbour, level, area and volume tables), time, step}, the state
+ * [neq][ncells] as little-endian doubles, then an FNV-1a checksum of the
+ * payload.  fvgpu_checkpoint_load rejects a file whose checksum, size or mesh
+ * signature does not match the context (FVGPU_ERR_STATE). */
+int fvgpu_checkpoint_save(fvgpu_ctx *ctx, const char *path, double time, int64_t step);
+int fvgpu_checkpoint_load(fvgpu_ctx *ctx, const char *path, double *time, int64_t *step);
+/* The same format on host arrays, without a context (tools, tests). */
+int fvgpu_checkpoint_write(const char *path, const double *U, int neq, int64_t ncells, uint64_t mesh_sig,
+                           double time, int64_t step);
+int fvgpu_checkpoint_read(const char *path, double *U, int neq, int64_t ncells, uint64_t mesh_sig, double *time,
+                          int64_t *step);
+/* Mesh signature of the context's uploaded tables. */
+int fvgpu_mesh_signature(fvgpu_ctx *ctx, uint64_t *sig);
+
+/* Refinement flags from the current state (criterionsplt.c:24-86): split[c]
+ * = level_hi where the criterion holds, else 1 (the reference's default).
+ *   FVGPU_CRIT_GRAD_RHO   |grad rho| > threshold (i_case 204; the gradients
+ *                         of the last fvgpu_gradcalc, row 0 of SG)
+ *   FVGPU_CRIT_RHO_BELOW  rho < threshold (i_case 2500)
+ *   FVGPU_CRIT_GRAD_RHO_H |grad rho| * h > threshold, h = V^(1/3) (the
+ *                         cell-size-scaled form used to build AMR cases)
+ * split: host array [ncells]. */
+#define FVGPU_CRIT_GRAD_RHO 0
+#define FVGPU_CRIT_RHO_BELOW 1
+#define FVGPU_CRIT_GRAD_RHO_H 2
+int fvgpu_criterion(fvgpu_ctx *ctx, int kind, double threshold, int32_t level_hi, int32_t *split);
+
 /* ---- halo exchange (domain decomposition) ------------------------------- */
 /* The reference exchanges the state of interface cells between MPI ranks
  * once per stage (communicate_S, communicate1.c:44-229).  Here a rank's mesh

@@ -36,7 +36,7 @@ REF_SOURCES = [
     "bc_inlet", "asinvalues", "asinvalues_multiphase", "barotropic_eos", "rotate_vectors",
     "pvrs_mc", "leafallocation", "memallocation", "createutility", "faceinterp", "distance",
     "deltavalues", "facevalues_MUSCL", "reconctruct_V3", "cons2primtv", "prim2conc",
-    "operatetp", "gradcalc", "timecpu",
+    "operatetp", "gradcalc", "timecpu", "criterionsplt",
 ]
 
 

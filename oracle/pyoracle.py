@@ -86,6 +86,7 @@ class RefHarness:
             L.refh_rk.argtypes = [vp, C.c_int]
             L.refh_step.argtypes = [vp, vp, C.c_int]
             L.refh_conservation.argtypes = [vp, vp]
+            L.refh_criterion.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
             cls._lib = L
         return cls._lib
 
@@ -174,6 +175,12 @@ class RefHarness:
     def conservation(self) -> np.ndarray:
         out = np.empty(self.neq + 1)
         self.lib().refh_conservation(self._h, _ptr(out))
+        return out
+
+    def criterion(self, i_case: int, level: int, geo_adapth: int = 0) -> np.ndarray:
+        """criterionsplt.c flags of the leaves (gradients from the last gradcalc)."""
+        out = np.empty(self.n, np.int32)
+        self.lib().refh_criterion(self._h, int(i_case), int(geo_adapth), int(level), _ptr(out))
         return out
 
 
@@ -371,3 +378,18 @@ class OracleAD:
         assert self.L.fvo_ad_count_stage(C.byref(self.ccfg), C.byref(self.mesh.soa), int(irk), float(dt), _ptr(U),
                                          out.ctypes.data) == 0
         return out[:4], out[4:]
+
+
+def criterion(U, SG, vol, kind, threshold, level_hi):
+    """Refinement flags, criterionsplt.c:24-86 (restated; i_case 204 is
+    |grad rho| > threshold, i_case 2500 is rho < threshold; kind 2 scales
+    |grad rho| by the cell size V^(1/3)).  SG: gradcalc output [neq+1][3][n]."""
+    g = SG[0]
+    mag = np.sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2])
+    if kind == 1:
+        hit = U[0] < threshold
+    else:
+        if kind == 2:
+            mag = mag * np.cbrt(vol)
+        hit = mag > threshold
+    return np.where(hit, level_hi, 1).astype(np.int32)

@@ -359,6 +359,19 @@ void refh_step(refh *h, const int *stages, int nstages) {
   }
 }
 
+/* The reference's refinement flags (criterionsplt.c) for case i_case with
+ * target level `level`; split[c] receives brch->split. */
+void refh_criterion(refh *h, int i_case, int geo_adapth, int level, int32_t *split) {
+  RUN *run = h->run;
+  const int saved = run->con->i_case;
+  run->con->i_case = i_case;
+  run->con->geo_adapth = geo_adapth;
+  run->con->level = level;
+  criterionsplt(run);
+  run->con->i_case = saved;
+  for (int64_t c = 0; c < h->n; ++c) split[c] = h->cells[c]->split;
+}
+
 /* Conservation sums, conservationcalc.c:19-34 without the file output. */
 void refh_conservation(const refh *h, double *sums) {
   const int neq = h->run->con->neq;
