@@ -222,8 +222,9 @@ __global__ void k_criterion(int kind, double threshold, int level_hi, int64_t n,
       hit = S[c] < threshold;
     } else {
       const double gx = SG[0 * n + c], gy = SG[1 * n + c], gz = SG[2 * n + c];
-      double mag = sqrt(gx * gx + gy * gy + gz * gz);
-      if (kind == FVGPU_CRIT_GRAD_RHO_H) mag = mag * cbrt(vol[c]);
+      // ((gx gx + gy gy) + gz gz) without contraction, as the reference evaluates it
+      double mag = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz)));
+      if (kind == FVGPU_CRIT_GRAD_RHO_H) mag = __dmul_rn(mag, cbrt(vol[c]));
       hit = mag > threshold;
     }
     split[c] = hit ? level_hi : 1;
