@@ -71,7 +71,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except Exception:
@@ -211,14 +211,15 @@ def run_gpu(args):
         torch.cuda.synchronize()
         clocks = ClockSampler(local)
         clocks.start()
-        ms = time_steps(torch, s, stream, flush, args.steps, cfl)
+        nsteps = args.steps if prec == abi.MIXED or args.precision == "fp64" else min(args.steps, args.fp64_steps)
+        ms = time_steps(torch, s, stream, flush, nsteps, cfl)
         clk = clocks.stop()
         total_ms = float(sum(ms))
         if dist:
             tt = torch.tensor([total_ms], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             total_ms = float(tt.item())
-        value = ws * n * args.steps / (total_ms * 1e-3) / 1e6
+        value = ws * n * nsteps / (total_ms * 1e-3) / 1e6
         # live per-kernel timing (eager, events between launches on the library stream)
         s.set_state(case.U)
         kms, klaunch = s.profile_step("ssprk3", cfl=cfl, nsteps=max(3, min(args.steps, 10)))
@@ -236,7 +237,7 @@ def run_gpu(args):
         import ctypes as C
         e2e_ms = []
         lib = s.lib
-        for it in range(args.warmup + args.steps):
+        for it in range(args.warmup + nsteps):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -255,14 +256,14 @@ def run_gpu(args):
             tt = torch.tensor([e2e_total], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             e2e_total = float(tt.item())
-        e2e_value = ws * n * args.steps / (e2e_total * 1e-3) / 1e6
+        e2e_value = ws * n * nsteps / (e2e_total * 1e-3) / 1e6
         # state after a fixed number of steps at a fixed dt, for the error check
         s.set_state(case.U)
         dt0 = s.compute_dt(cfl)
         s.step("ssprk3", dt=dt0, nsteps=args.err_steps)
         states[prec] = (s.state(), dt0)
         results[prec] = {
-            "value": value, "ms_per_step": total_ms / args.steps, "clocks": clk,
+            "value": value, "ms_per_step": total_ms / nsteps, "steps": nsteps, "clocks": clk,
             "kernel_ms": {abi.KIND_NAMES[k]: float(kms[k]) for k in range(len(kms)) if klaunch[k]},
             "kernel_launches": {abi.KIND_NAMES[k]: int(klaunch[k]) for k in range(len(kms)) if klaunch[k]},
             "launches_per_step": launches_per_step,
@@ -325,11 +326,19 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    case = build_case(args.level)
+    full = build_case(args.level)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     from pyoracle import Oracle
     threads = os.cpu_count() or 1
     Oracle.set_threads(threads)
+    # bounded sample: the largest periodic mesh of the same generator whose
+    # K + W steps fit about two minutes on these cores (~0.3 Mcell-updates/s
+    # per core for the C restatement)
+    budget_cells = 120.0 * 0.3e6 * threads / max(args.steps + args.warmup, 1)
+    level = args.level
+    while level > 4 and 8 ** level > budget_cells:
+        level -= 1
+    case = full if level == args.level else build_case(level)
     orc = Oracle(case.tables, case.cfg)
     S = case.U
     for _ in range(args.warmup):
@@ -346,10 +355,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_of(case, args),
+        "data": "synthetic", "config": config_of(full, args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
                          "sample": f"every step is one full SSP-RK3 step (CFL dt) of the "
-                                   f"{case.tables.ncells}-cell mesh on {Oracle.threads()} threads"},
+                                   f"{case.tables.ncells}-cell periodic mesh of the same generator"
+                                   f"{'' if case is full else ' (the workload at level ' + str(level) + ')'}"
+                                   f" on {Oracle.threads()} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -366,7 +377,9 @@ def config_of(case, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--fp64-steps", type=int, default=20,
+                    help="timed steps of the FP64 comparison arm (default 20: it runs ~37 ms per step)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fvgpu", choices=["fvgpu", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
