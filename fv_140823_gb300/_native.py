@@ -67,6 +67,7 @@ _GPU_SIGS = {
     "fvgpu_compute_dt": ([C.c_void_p, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "fvgpu_conservation": ([C.c_void_p, C.c_void_p], C.c_int),
     "fvgpu_residual_vjp": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "fvgpu_upload_leaves": ([C.c_void_p, C.c_void_p], C.c_int),
     "fvgpu_checkpoint_save": ([C.c_void_p, C.c_char_p, C.c_double, C.c_int64], C.c_int),
     "fvgpu_checkpoint_load": ([C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)], C.c_int),
     "fvgpu_checkpoint_write": ([C.c_char_p, C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double, C.c_int64],

@@ -117,3 +117,9 @@ class MeshSoaHolder:
 CRIT_GRAD_RHO = 0
 CRIT_RHO_BELOW = 1
 CRIT_GRAD_RHO_H = 2
+
+
+class FvLeaves(C.Structure):
+    """fvgpu_leaves (include/fvgpu.h)."""
+    _fields_ = [("ncells", C.c_int64), ("level", C.c_void_p), ("ijk", C.c_void_p), ("lo", C.c_double * 3),
+                ("len", C.c_double * 3), ("periodic", C.c_int * 3), ("side_bc", C.c_int * 6)]

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "fv_adjoint.cuh"
+#include "fv_flatten.cuh"
 #include "fv_kernels.cuh"
 #include "fv_mixed.cuh"
 #include "fvgpu.h"
@@ -143,6 +144,12 @@ uint64_t fnv1a(uint64_t h, const void *data, size_t bytes) {
   return h;
 }
 constexpr uint64_t kFnvSeed = 0xcbf29ce484222325ull;
+
+// Face frames of an axis-aligned box (fvmesh_flatten's table: outward normal,
+// t1 along the face's first edge, t2 = n x t1; normalvector.c / tagvector.c)
+const double kBoxFrames[54] = {0, -1, 0, 1, 0, 0, 0, 0, 1,  1, 0, 0, 0, 0, 1, 0, -1, 0,
+                               0, 1, 0, 0, 0, 1, 1, 0, 0,   -1, 0, 0, 0, -1, 0, 0, 0, 1,
+                               0, 0, -1, 1, 0, 0, 0, -1, 0, 0, 0, 1, 0, -1, 0, 1, 0, 0};
 
 int set_err(fvgpu_ctx *ctx, int code, const char *fmt, ...) {
   char buf[512];
@@ -759,6 +766,8 @@ int fvgpu_set_precision(fvgpu_ctx *ctx, int precision) {
   return FVGPU_OK;
 }
 
+static int finish_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m);
+
 int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   if (!ctx || !m) return set_err(ctx, FVGPU_ERR_ARG, "null argument");
   int rc = validate_mesh(ctx, m);
@@ -786,6 +795,15 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
     FV_CUDA(ctx, u.buf->alloc(u.bytes));
     if (u.src && u.bytes) FV_CUDA(ctx, cudaMemcpy(u.buf->p, u.src, u.bytes, cudaMemcpyHostToDevice));
   }
+  return finish_mesh(ctx, m);
+}
+
+// Everything after the tables are on the device: state and work arrays,
+// mesh signature, boundary codes present, the mixed path's tables.  m holds
+// host copies of the same tables.
+static int finish_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
+  const int64_t n = m->ncells, nh = m->nhang;
+  const int neq = ctx->neq;
   FV_CUDA(ctx, ctx->S.alloc(sizeof(double) * neq * n));
   FV_CUDA(ctx, ctx->SN.alloc(sizeof(double) * neq * n));
   FV_CUDA(ctx, ctx->R.alloc(sizeof(double) * neq * n));
@@ -841,6 +859,104 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   FV_CUDA(ctx, cudaDeviceSynchronize());
   ctx->has_mesh = true;
   return FVGPU_OK;
+}
+
+int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *lv) {
+  if (!ctx || !lv) return set_err(ctx, FVGPU_ERR_ARG, "null argument");
+  const int64_t n = lv->ncells;
+  if (n <= 0 || n > 300000000 || !lv->level || !lv->ijk)  // 6 n record numbers fit int32
+    return set_err(ctx, FVGPU_ERR_ARG, "need 1 <= ncells <= 3e8 and level / ijk arrays");
+  fv::LeafGeom g;
+  for (int a = 0; a < 3; ++a) {
+    g.lo[a] = lv->lo[a];
+    g.len[a] = lv->len[a];
+    g.periodic[a] = lv->periodic[a] ? 1 : 0;
+    if (!(g.len[a] > 0.0) || !std::isfinite(g.lo[a])) return set_err(ctx, FVGPU_ERR_ARG, "bad box");
+  }
+  static const int kAxisOf[6] = {1, 0, 1, 0, 2, 2};
+  for (int f = 0; f < 6; ++f) {
+    g.side_bc[f] = g.periodic[kAxisOf[f]] ? 0 : lv->side_bc[f];
+    if (!g.periodic[kAxisOf[f]] && (g.side_bc[f] < 1 || g.side_bc[f] > 4))
+      return set_err(ctx, FVGPU_ERR_ARG, "side_bc must be 1..4 on non-periodic sides");
+  }
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->drop_graphs();
+  fv::release_mixed(ctx->mixed);
+  ctx->has_mesh = false;
+  // pass 1: keys, 1:4 counts, record numbers
+  DevBuf d_level, d_ijk, d_keys, d_off, d_tiles, d_scal;
+  const int64_t ntiles = (n + 1023) / 1024;
+  FV_CUDA(ctx, d_level.alloc(sizeof(int32_t) * size_t(n)));
+  FV_CUDA(ctx, d_ijk.alloc(sizeof(int32_t) * 3 * size_t(n)));
+  FV_CUDA(ctx, d_keys.alloc(sizeof(uint64_t) * size_t(n)));
+  FV_CUDA(ctx, d_off.alloc(sizeof(int32_t) * size_t(n)));
+  FV_CUDA(ctx, d_tiles.alloc(sizeof(int64_t) * size_t(ntiles)));
+  FV_CUDA(ctx, d_scal.alloc(2 * sizeof(int64_t)));
+  FV_CUDA(ctx, cudaMemcpy(d_level.p, lv->level, sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice));
+  FV_CUDA(ctx, cudaMemcpy(d_ijk.p, lv->ijk, sizeof(int32_t) * 3 * size_t(n), cudaMemcpyHostToDevice));
+  FV_CUDA(ctx, cudaMemset(d_scal.p, 0, 2 * sizeof(int64_t)));
+  int64_t *d_nhang = d_scal.as<int64_t>();
+  unsigned long long *d_ferr = reinterpret_cast<unsigned long long *>(d_scal.as<int64_t>() + 1);
+  FV_CUDA(ctx, fv::flatten_count(g, n, d_level.as<int32_t>(), d_ijk.as<int32_t>(), d_keys.as<uint64_t>(),
+                                 d_off.as<int32_t>(), d_tiles.as<int64_t>(), d_nhang, d_ferr, ctx->stream));
+  int64_t hs[2] = {0, 0};
+  FV_CUDA(ctx, cudaMemcpyAsync(hs, d_scal.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream));
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  auto leaf_error = [&](uint64_t e) {
+    const int code = int(e >> 40);
+    const long long cell = (long long)(e & 0xffffffffffull);
+    if (code == 1) return set_err(ctx, FVGPU_ERR_MESH, "leaf %lld: level or position out of range", cell);
+    if (code == 2) return set_err(ctx, FVGPU_ERR_MESH, "leaves are not in Morton order (at %lld)", cell);
+    return set_err(ctx, FVGPU_ERR_MESH, "leaf %lld: a face sees more than one level of refinement", cell);
+  };
+  if (hs[1]) return leaf_error(uint64_t(hs[1]));
+  const int64_t nh = hs[0];
+  if (nh > 6 * n) return set_err(ctx, FVGPU_ERR_MESH, "hanging-face count %lld out of range", (long long)nh);
+  // pass 2: the tables, straight into the context's buffers
+  for (DevBuf *b : {&ctx->nbr, &ctx->nbr_face}) FV_CUDA(ctx, b->alloc(sizeof(int32_t) * 6 * size_t(n)));
+  for (DevBuf *b : {&ctx->area, &ctx->dcf, &ctx->dcc}) FV_CUDA(ctx, b->alloc(sizeof(double) * 6 * size_t(n)));
+  FV_CUDA(ctx, ctx->vol.alloc(sizeof(double) * size_t(n)));
+  FV_CUDA(ctx, ctx->level.alloc(sizeof(int32_t) * size_t(n)));
+  FV_CUDA(ctx, ctx->hang_nbr.alloc(sizeof(int32_t) * 4 * size_t(nh)));
+  FV_CUDA(ctx, ctx->hang_area.alloc(sizeof(double) * 4 * size_t(nh)));
+  fv::DevTables t{ctx->nbr.as<int32_t>(), ctx->nbr_face.as<int32_t>(), ctx->hang_nbr.as<int32_t>(),
+                  ctx->level.as<int32_t>(), ctx->area.as<double>(), ctx->dcf.as<double>(),
+                  ctx->dcc.as<double>(), ctx->vol.as<double>(), ctx->hang_area.as<double>()};
+  FV_CUDA(ctx, fv::flatten_tables(g, n, d_level.as<int32_t>(), d_ijk.as<int32_t>(), d_keys.as<uint64_t>(),
+                                  d_off.as<int32_t>(), t, d_ferr, ctx->stream));
+  FV_CUDA(ctx, cudaMemcpyAsync(hs, d_scal.p, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream));
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hs[1]) return leaf_error(uint64_t(hs[1]));
+  // host copies for the signature, the boundary codes and the mixed path's brick detection
+  const size_t un = static_cast<size_t>(n), unh = static_cast<size_t>(nh);
+  std::vector<int32_t> h_nbr(6 * un), h_nface(6 * un), h_hnbr(4 * unh), h_level(un);
+  std::vector<double> h_area(6 * un), h_dcf(6 * un), h_dcc(6 * un), h_vol(un), h_harea(4 * unh);
+  struct Down {
+    void *dst;
+    const DevBuf *src;
+    size_t bytes;
+  } downs[] = {{h_nbr.data(), &ctx->nbr, h_nbr.size() * 4},         {h_nface.data(), &ctx->nbr_face, h_nface.size() * 4},
+               {h_area.data(), &ctx->area, h_area.size() * 8},      {h_dcf.data(), &ctx->dcf, h_dcf.size() * 8},
+               {h_dcc.data(), &ctx->dcc, h_dcc.size() * 8},         {h_vol.data(), &ctx->vol, h_vol.size() * 8},
+               {h_hnbr.data(), &ctx->hang_nbr, h_hnbr.size() * 4}, {h_harea.data(), &ctx->hang_area, h_harea.size() * 8},
+               {h_level.data(), &ctx->level, h_level.size() * 4}};
+  for (auto &d : downs)
+    if (d.bytes) FV_CUDA(ctx, cudaMemcpy(d.dst, d.src->p, d.bytes, cudaMemcpyDeviceToHost));
+  fvgpu_mesh_soa m{};
+  m.ncells = n;
+  m.nhang = nh;
+  m.nbr = h_nbr.data();
+  m.nbr_face = h_nface.data();
+  m.area = h_area.data();
+  m.dcf = h_dcf.data();
+  m.dcc = h_dcc.data();
+  m.vol = h_vol.data();
+  m.hang_nbr = h_hnbr.data();
+  m.hang_area = h_harea.data();
+  m.frames = kBoxFrames;
+  m.level = h_level.data();
+  return finish_mesh(ctx, &m);
 }
 
 int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld) {

@@ -172,6 +172,25 @@ class Solver:
         self._call("fvgpu_conservation", _ptr(out))
         return out
 
+    def upload_leaves(self, level: np.ndarray, ijk: np.ndarray, lo, length, periodic, side_bc):
+        """Build the mesh tables on the GPU from the Morton-sorted leaf list
+        (fvgpu_upload_leaves): bit-identical to the host flattener's tables."""
+        self._leaf_level = np.ascontiguousarray(level, dtype=np.int32)
+        self._leaf_ijk = np.ascontiguousarray(ijk, dtype=np.int32)
+        lv = abi.FvLeaves(self._leaf_level.size, _ptr(self._leaf_level).value, _ptr(self._leaf_ijk).value,
+                          (C.c_double * 3)(*lo), (C.c_double * 3)(*length), (C.c_int * 3)(*periodic),
+                          (C.c_int * 6)(*side_bc))
+        self._call("fvgpu_upload_leaves", C.byref(lv))
+        self.n = int(self._leaf_level.size)
+
+    @classmethod
+    def from_leaves(cls, tables, cfg: abi.SolverConfig | None = None) -> "Solver":
+        """A context whose tables are flattened on the device from `tables`'
+        leaf list (level, ijk and the box)."""
+        s = cls(None, cfg)
+        s.upload_leaves(tables.level, tables.ijk, tables.lo, tables.length, tables.periodic, tables.side_bc)
+        return s
+
     # -- restart and adaptation helpers ------------------------------------------
     def checkpoint_save(self, path: str, time: float = 0.0, step: int = 0):
         """Bit-exact binary restart file of the state (fvgpu_checkpoint_save)."""

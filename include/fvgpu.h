@@ -124,6 +124,24 @@ int fvgpu_set_precision(fvgpu_ctx *ctx, int precision);
 /* ---- data in / out ---------------------------------------------------- */
 /* Validates and uploads the tables (once per adaptation); resets the state. */
 int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *mesh);
+/* Device-side flattening: builds the tables of fvgpu_upload_mesh on the GPU
+ * from the leaf list of an axis-aligned box -- the level and the integer
+ * position (i, j, k at that level) of every leaf, leaves 2:1 balanced and in
+ * Morton order -- with the host builder's arithmetic (fvmesh_flatten of
+ * fvmesh.h), so the tables are the same bit for bit.  The host keeps its
+ * octree and uploads 16 bytes per leaf after an adaptation instead of
+ * flattening on the CPU.  No reference counterpart (the reference walks its
+ * leaf list in every call).  FVGPU_ERR_MESH for unsorted, out-of-range or
+ * unbalanced leaves. */
+typedef struct fvgpu_leaves {
+  int64_t ncells;
+  const int32_t *level;  /* [ncells] */
+  const int32_t *ijk;    /* [3][ncells] */
+  double lo[3], len[3];  /* the box */
+  int periodic[3];       /* per axis */
+  int side_bc[6];        /* boundary code per face side (ignored on periodic axes) */
+} fvgpu_leaves;
+int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *leaves);
 /* S <- U (host, [neq][ld]); LEAF.S of every leaf (strdata.h:80). */
 int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld);
 int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld);
