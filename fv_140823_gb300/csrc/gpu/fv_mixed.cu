@@ -113,8 +113,10 @@ struct StageArgs {
   const GeoTables *geo;
   const BlockDesc *blocks;
   const float *SNf;         // [neq][n] FP32 copy of the step-start state
+  const float *Sin;         // [neq][n] FP32 stage-input state SNf + Din (SNf at the first stage)
   const float *Din;         // [neq][n] stage-input increment (null: zero)
   float *Dout;              // [neq][n]
+  float *Sout;              // [neq][n] non-last stages: the next stage's input SNf + Dout
   const double *SN;         // [neq][n] step-start state (last stage)
   double *SNout;            // [neq][n] last stage: SN + D
   float *SNfout;            // [neq][n] last stage: FP32 copy of SNout
@@ -472,21 +474,18 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     return true;
   }
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) a.Dout[v * n + c] = dn[v];
+  for (int v = 0; v < kNeqMax; ++v) {
+    a.Dout[v * n + c] = dn[v];
+    a.Sout[v * n + c] = __ldg(a.SNf + v * n + c) + dn[v];  // the value the next stage would form
+  }
   return false;
 }
 
-// stage state of any cell from global memory: SNf + D
+// stage state of any cell from global memory (SNf + D, written by the
+// previous stage)
 __device__ __forceinline__ void global_state(const MixedConst &mc, const StageArgs &a, int x, float q[kNeqMax]) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) {
-    float s = 0.0f;
-    if (v < mc.neq) {
-      s = __ldg(a.SNf + v * a.n + x);
-      if (a.Din) s += __ldg(a.Din + v * a.n + x);
-    }
-    q[v] = s;
-  }
+  for (int v = 0; v < kNeqMax; ++v) q[v] = v < mc.neq ? __ldg(a.Sin + v * a.n + x) : 0.0f;
 }
 
 // ============================ general kernel ================================
@@ -562,15 +561,10 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   Block<MODEL> blk(a, mc, c0, bd.count, st);
 
   // A: own stage state
-  float din[kNeqMax], q[kNeqMax];
+  float q[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
-    din[v] = 0.0f;
-    q[v] = 0.0f;
-    if (active && v < neq) {
-      din[v] = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-      q[v] = __ldg(a.SNf + v * n + c) + din[v];
-    }
+    q[v] = (active && v < neq) ? __ldg(a.Sin + v * n + c) : 0.0f;
     st[v][t] = q[v];
   }
   int32_t nb[6];
@@ -778,19 +772,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   // A1: the brick's cells and the halo from the six neighbour bricks
   int x, y, z;
   morton_decode(t, x, y, z);
-  float din[kNeqMax];
   {
     const int ti = tile_index(x, y, z);
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      din[v] = 0.0f;
-      float s = 0.0f;
-      if (v < neq) {
-        din[v] = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-        s = __ldg(a.SNf + v * n + c) + din[v];
-      }
-      tile[v][ti] = s;
-    }
+    for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = v < neq ? __ldg(a.Sin + v * n + c) : 0.0f;
   }
 #pragma unroll 1
   for (int h = t; h < kHalo; h += kBlock) {
@@ -1013,7 +998,10 @@ MixedConst make_const(const Phys &ph) {
 }
 
 // resource slots
-enum { kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6, kBufBlocks = 7 };
+enum {
+  kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6, kBufBlocks = 7,
+  kBufX1 = 8, kBufX2 = 9
+};
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
   if (r.buf[slot]) cudaFree(r.buf[slot]);
@@ -1294,7 +1282,9 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess) {
+      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
   }
@@ -1306,7 +1296,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
 }
 
 void release_mixed(MixedResources &r) {
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 0; i < 10; ++i) {
     if (r.buf[i]) cudaFree(r.buf[i]);
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
@@ -1381,13 +1371,16 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     launch_dt_from_lambda(lambda, lambda, cfl, dt, err, st);
   }
   float *D[2] = {static_cast<float *>(r.buf[kBufD1]), static_cast<float *>(r.buf[kBufD2])};
+  float *X[2] = {static_cast<float *>(r.buf[kBufX1]), static_cast<float *>(r.buf[kBufX2])};
   const MixedConst mc = make_const(ph);
   const BlockDesc *blocks = static_cast<const BlockDesc *>(r.buf[kBufBlocks]);
   for (int k = 0; k < nst; ++k) {
     StageArgs a = stage_args(r, m);
     a.SNf = static_cast<const float *>(r.buf[kBufSNf]);
+    a.Sin = k == 0 ? a.SNf : X[(k - 1) & 1];
     a.Din = k == 0 ? nullptr : D[(k - 1) & 1];
     a.Dout = D[k & 1];
+    a.Sout = X[k & 1];
     a.SN = in;
     a.SNout = out;
     a.SNfout = static_cast<float *>(r.buf[kBufSNfAlt]);
