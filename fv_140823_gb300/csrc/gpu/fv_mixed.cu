@@ -735,6 +735,24 @@ constexpr BrickTasks make_brick_tasks() {
 }
 __device__ const BrickTasks g_brick_tasks = make_brick_tasks();
 
+// CFL radius of a brick cell: the frames are axis-aligned (checked at
+// upload), so |u.n| on face f is the magnitude of one velocity component --
+// the same value cell_lambda_with forms from the frame, without it.
+template <int MODEL>
+__device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float q[kNeqMax], uint32_t be,
+                                              const float (*geo)[2][4], float inv2vol) {
+  FS s;
+  mixed_face_state<MODEL>(mc, q, false, s);
+  const float au = fabsf(s.u), av = fabsf(s.v), aw = fabsf(s.w);
+  float acc = 0.0f;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    const float un = (f == 1 || f == 3) ? au : ((f == 0 || f == 2) ? av : aw);
+    acc = fmaf(geo[f][(be >> f) & 1u][2], un + s.c, acc);
+  }
+  return acc * inv2vol;
+}
+
 #ifndef FV_BRICK_MIN_BLOCKS
 #define FV_BRICK_MIN_BLOCKS 5  // 48 registers: 5 blocks per SM measured faster than 4 (217 vs 257 us per stage, 128^3)
 #endif
@@ -769,6 +787,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
     s_inv2vol = a.geo->inv2vol[level];
   }
 
+  if (a.last && t < 80) {  // the step-start state this block adds to at the end: on its way to L2
+    const int v = t >> 4, l = t & 15;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SN + int64_t(v) * n + start + 16 * l));
+  }
   // A1: the brick's cells and the halo from the six neighbour bricks
   int x, y, z;
   morton_decode(t, x, y, z);
@@ -777,7 +799,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = v < neq ? __ldg(a.Sin + v * n + c) : 0.0f;
   }
-#pragma unroll 1
+#pragma unroll
   for (int h = t; h < kHalo; h += kBlock) {
     // halo cell h: side, layer and position (x sides, y sides, z sides)
     int hx, hy, hz, side, lx, ly, lz;
@@ -950,7 +972,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   add_face(4, tz_p - BX * BY, false);
   float qn[kNeqMax], lam = 0.0f;
   if (stage_update<MODEL>(mc, a, c, s_dtv, R, ok, qn) && a.lambda)
-    lam = cell_lambda_with<MODEL>(mc, qn, [&](int f) { return s_geo[f][(be >> f) & 1u][2]; }, s_inv2vol);
+    lam = brick_lambda<MODEL>(mc, qn, be, s_geo, s_inv2vol);
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
