@@ -154,3 +154,30 @@ def test_brick_kernel_bit_identical_to_general_kernel(name):
     a = _mixed_state(c, 0, 4, dt)
     b = _mixed_state(c, abi.FLAG_NO_BRICKS, 4, dt)
     assert np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
+@pytest.mark.parametrize("flags", [0, abi.FLAG_NO_BRICKS])
+def test_mixed_nonfinite_state_reports_and_context_recovers(flags):
+    """A NaN in the state surfaces as FVGPU_ERR_NONFINITE / _EOS with a cell at
+    the next synchronising call, in the brick and in the general kernel; the
+    context then steps a clean state bit-identically to a fresh context."""
+    from fv_140823_gb300.solver import FvGpuError
+    c = cases.periodic(level=4)
+    cfg = SolverConfig(**{**c.cfg.__dict__, "precision": abi.MIXED, "flags": flags})
+    dt = fixed_dt(c)
+    U = c.U.copy()
+    U[0, 1234] = np.nan
+    with solver(c.tables, cfg) as s:
+        s.set_state(U)
+        with pytest.raises(FvGpuError) as ei:
+            s.step("ssprk3", dt=dt, nsteps=1)
+            s.synchronize()
+        assert ei.value.code in (abi.ERR_NONFINITE, abi.ERR_EOS)
+        assert ei.value.cell >= 0
+        s.set_state(c.U)
+        s.step("ssprk3", dt=dt, nsteps=2)
+        got = s.state()
+    with solver(c.tables, cfg) as s:
+        s.set_state(c.U)
+        s.step("ssprk3", dt=dt, nsteps=2)
+        assert np.array_equal(got.view(np.int64), s.state().view(np.int64))
