@@ -92,6 +92,8 @@ struct MixedConst {
   float fr[54];  // face frames n, t1, t2 per face index
   float gamma, pinf, gm1, gpinf;
   float ylo, yhi;  // mass-fraction clip (facercnstr.c:43-44)
+  float visc;      // dynamic viscosity (flux_viscous.c, turb = 0)
+  int ns, eos;     // viscous fluxes on; energy work term on
   float inflow[kNeqMax];
   int model, neq, ischeme, pad;
 };
@@ -117,6 +119,7 @@ struct StageArgs {
   const float *Din;         // [neq][n] stage-input increment (null: zero)
   float *Dout;              // [neq][n]
   float *Sout;              // [neq][n] non-last stages: the next stage's input SNf + Dout
+  const float *SG;          // [9][n] viscous runs: momentum gradients of Sin (ux uy uz vx ... wz)
   const double *SN;         // [neq][n] step-start state (last stage)
   double *SNout;            // [neq][n] last stage: SN + D
   float *SNfout;            // [neq][n] last stage: FP32 copy of SNout
@@ -488,6 +491,149 @@ __device__ __forceinline__ void global_state(const MixedConst &mc, const StageAr
   for (int v = 0; v < kNeqMax; ++v) q[v] = v < mc.neq ? __ldg(a.Sin + v * a.n + x) : 0.0f;
 }
 
+// ============================ viscous terms =================================
+
+// Cartesian velocity of the ghost across a boundary face f (bc.c:19-49) from
+// the own face values q.
+__device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float q[kNeqMax],
+                                               float u[3]) {
+  if (bc == 1) {
+    const float rinv = fast_rcp(mc.inflow[0]);
+    u[0] = mc.inflow[1] * rinv;
+    u[1] = mc.inflow[2] * rinv;
+    u[2] = mc.inflow[3] * rinv;
+    return;
+  }
+  const float rinv = fast_rcp(q[0]);
+  u[0] = q[1] * rinv;
+  u[1] = q[2] * rinv;
+  u[2] = q[3] * rinv;
+  if (bc == 3) {  // slip wall: normal component mirrored
+    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
+    const float un = fmaf(u[2], nz, fmaf(u[1], ny, u[0] * nx));
+    u[0] = fmaf(-2.0f * un, nx, u[0]);
+    u[1] = fmaf(-2.0f * un, ny, u[1]);
+    u[2] = fmaf(-2.0f * un, nz, u[2]);
+  } else if (bc == 4) {  // no-slip wall: reversed
+    u[0] = -u[0];
+    u[1] = -u[1];
+    u[2] = -u[2];
+  }
+}
+
+// FV . n of one face (flux_viscous.c:57-232 with turb = 0) from the face
+// values of both sides (bc > 0: a boundary face, the other side is the
+// ghost of lo) and the momentum gradients of both cells, FP32.
+__device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int bc, const float lo[kNeqMax],
+                                               const float hi[kNeqMax], const float gl[9], const float gh[9],
+                                               float FVn[kNeqMax]) {
+  float ul[3], uh[3];
+  {
+    const float rinv = fast_rcp(lo[0]);
+    ul[0] = lo[1] * rinv;
+    ul[1] = lo[2] * rinv;
+    ul[2] = lo[3] * rinv;
+  }
+  if (bc > 0) {
+    ghost_velocity(mc, bc, f, lo, uh);
+  } else {
+    const float rinv = fast_rcp(hi[0]);
+    uh[0] = hi[1] * rinv;
+    uh[1] = hi[2] * rinv;
+    uh[2] = hi[3] * rinv;
+  }
+  const float uf = 0.5f * (ul[0] + uh[0]), vf = 0.5f * (ul[1] + uh[1]), wf = 0.5f * (ul[2] + uh[2]);
+  float g[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] = 0.5f * (gl[i] + gh[i]);
+  const float mu = mc.visc;
+  const float D = g[0] + g[4] + g[8];
+  const float txx = mu * fmaf(2.0f, g[0], -(2.0f / 3.0f) * D);
+  const float tyy = mu * fmaf(2.0f, g[4], -(2.0f / 3.0f) * D);
+  const float tzz = mu * fmaf(2.0f, g[8], -(2.0f / 3.0f) * D);
+  const float txy = mu * (g[1] + g[3]), txz = mu * (g[2] + g[6]), tyz = mu * (g[5] + g[7]);
+  const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
+  FVn[0] = 0.0f;
+  FVn[1] = fmaf(txz, nz, fmaf(txy, ny, txx * nx));
+  FVn[2] = fmaf(tyz, nz, fmaf(tyy, ny, txy * nx));
+  FVn[3] = fmaf(tzz, nz, fmaf(tyz, ny, txz * nx));
+  FVn[4] = 0.0f;
+  if (mc.eos == 1) {
+    const float ex = fmaf(wf, txz, fmaf(vf, txy, uf * txx));
+    const float ey = fmaf(wf, tyz, fmaf(vf, tyy, uf * txy));
+    const float ez = fmaf(wf, tzz, fmaf(vf, tyz, uf * txz));
+    FVn[4] = fmaf(ez, nz, fmaf(ey, ny, ex * nx));
+  }
+}
+
+__device__ __forceinline__ void load_grad9f(const float *__restrict__ SG, int n, int c, float g[9]) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] = __ldg(SG + i * n + c);
+}
+
+// Green-Gauss momentum gradients of the stage-input state (gradcalc.c:9-47,
+// rows of rho u, rho v, rho w), FP32, one cell per thread.
+template <int MODEL>
+__global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs a, float *__restrict__ SGout) {
+  const int c = blockIdx.x * kBlock + threadIdx.x;
+  const int n = a.n;
+  if (c >= n) return;
+  float q[kNeqMax];
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) q[v] = __ldg(a.Sin + v * n + c);
+  const int32_t g = __ldg(a.geom + c);
+  const int lev = level_of(g);
+  const float inv_vol = a.geo->inv_vol[lev];
+  float gr[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int f = 0; f < 6; ++f) {
+    const int32_t code = __ldg(a.nbr + f * n + c);
+    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
+    auto add = [&](const float m[3], float A) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float h = 0.5f * (m[k] + q[1 + k]) * A * inv_vol;
+        gr[k * 3 + 0] = fmaf(h, nx, gr[k * 3 + 0]);
+        gr[k * 3 + 1] = fmaf(h, ny, gr[k * 3 + 1]);
+        gr[k * 3 + 2] = fmaf(h, nz, gr[k * 3 + 2]);
+      }
+    };
+    if (is_boundary(code)) {
+      const int bc = -1 - code;
+      float m[3];
+      if (bc == 1) {
+        m[0] = mc.inflow[1];
+        m[1] = mc.inflow[2];
+        m[2] = mc.inflow[3];
+      } else {
+        float u[3];
+        ghost_velocity(mc, bc, f, q, u);
+        m[0] = q[0] * u[0];
+        m[1] = q[0] * u[1];
+        m[2] = q[0] * u[2];
+        if (bc != 3 && bc != 4) {
+          m[0] = q[1];
+          m[1] = q[2];
+          m[2] = q[3];
+        }
+      }
+      add(m, geo_face(a.geo, lev, f, kRelBoundary)[2]);
+    } else if (is_hanging(code)) {
+      const int32_t *k = a.hang_nbr + 4 * hang_index(code);
+      const float A = a.geo->sub_area[lev * 6 + f];
+      for (int s = 0; s < 4; ++s) {
+        const int ks = __ldg(k + s);
+        const float m[3] = {__ldg(a.Sin + 1 * n + ks), __ldg(a.Sin + 2 * n + ks), __ldg(a.Sin + 3 * n + ks)};
+        add(m, A);
+      }
+    } else {
+      const float m[3] = {__ldg(a.Sin + 1 * n + code), __ldg(a.Sin + 2 * n + code), __ldg(a.Sin + 3 * n + code)};
+      add(m, geo_face(a.geo, lev, f, rel_of(g, f))[2]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) SGout[i * n + c] = gr[i];
+}
+
 // ============================ general kernel ================================
 
 template <int MODEL>
@@ -657,6 +803,15 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
           hi[v] = own_low ? oth[v] : own[v];
         }
         ok &= canonical_flux<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
+        if (mc.ns == 1) {  // (F - FV).n + FH
+          float gl[9], gh[9], FVn[kNeqMax];
+          const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
+          load_grad9f(a.SG, n, clo, gl);
+          load_grad9f(a.SG, n, chi, gh);
+          viscous_normal(mc, own_low ? f : fo, boundary ? -1 - code : 0, lo, hi, gl, gh, FVn);
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
+        }
         if (plus && !boundary && !hanging) {
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
@@ -1016,13 +1171,16 @@ MixedConst make_const(const Phys &ph) {
   mc.model = ph.model;
   mc.neq = ph.neq;
   mc.ischeme = ph.ischeme;
+  mc.visc = float(ph.visc);
+  mc.ns = ph.ns;
+  mc.eos = ph.eos;
   return mc;
 }
 
 // resource slots
 enum {
   kBufGeom = 0, kBufTables = 1, kBufD1 = 2, kBufD2 = 3, kBufAlt = 4, kBufSNf = 5, kBufSNfAlt = 6, kBufBlocks = 7,
-  kBufX1 = 8, kBufX2 = 9
+  kBufX1 = 8, kBufX2 = 9, kBufSG = 10
 };
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
@@ -1117,10 +1275,6 @@ int brick_side(const fvgpu_mesh_soa *m, int64_t i, int f, const std::vector<char
 bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
   if (ph.model != 1 && ph.model != 3) {
     snprintf(why, whylen, "the mixed path implements models 1 and 3");
-    return false;
-  }
-  if (ph.ns != 0) {
-    snprintf(why, whylen, "the mixed path does not implement viscous fluxes (use FVGPU_FP64)");
     return false;
   }
   return true;
@@ -1243,7 +1397,9 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   }
   // bricks: candidate starts, then keep those whose six sides resolve
   std::vector<char> is_brick(size_t(n), 0);
-  if (!r.force_general) {
+  // viscous runs take the general kernel everywhere: its face evaluations read
+  // both cells' gradients straight from the gradient pass
+  if (!r.force_general && ph.ns != 1) {
     for (int64_t i = 0; i + kBlock <= n;) {
       if (brick_interior(m, i)) {
         is_brick[size_t(i)] = 1;
@@ -1306,7 +1462,8 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufX1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess) {
+      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSG, ph.ns == 1 ? sizeof(float) * 9 * n : 16)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
   }
@@ -1318,7 +1475,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
 }
 
 void release_mixed(MixedResources &r) {
-  for (int i = 0; i < 10; ++i) {
+  for (int i = 0; i < 11; ++i) {
     if (r.buf[i]) cudaFree(r.buf[i]);
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
@@ -1403,6 +1560,7 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.Din = k == 0 ? nullptr : D[(k - 1) & 1];
     a.Dout = D[k & 1];
     a.Sout = X[k & 1];
+    a.SG = static_cast<const float *>(r.buf[kBufSG]);
     a.SN = in;
     a.SNout = out;
     a.SNfout = static_cast<float *>(r.buf[kBufSNfAlt]);
@@ -1411,6 +1569,16 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.last = k == nst - 1;
     a.lambda = (a.last && cfl_mode) ? lambda : nullptr;
     a.err = err;
+    if (ph.ns == 1) {
+      marks.mark(FVGPU_KIND_MIXED_AUX);
+      const unsigned gg = unsigned((m.n + kBlock - 1) / kBlock);
+      if (ph.model == 1)
+        k_mixed_grad<1><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
+      else
+        k_mixed_grad<3><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
     if (r.nbricks > 0) {
       a.blocks = blocks;
       marks.mark(FVGPU_KIND_MIXED_STAGE);

@@ -12,11 +12,11 @@ namespace fv {
 
 // Device resources the mixed path derives from the mesh at upload time:
 // packed per-cell geometry codes, per-level geometry tables, the two FP32
-// stage increments, the two FP32 stage-input states and the second FP64
-// state buffer (ping-pong).
+// stage increments, the two FP32 stage-input states, the FP32 gradients of
+// viscous runs and the second FP64 state buffer (ping-pong).
 struct MixedResources {
-  void *buf[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  size_t bytes[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  void *buf[11] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t bytes[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   int64_t n = 0;
   int64_t nbricks = 0;     // brick blocks (structured fast path)
   int64_t ngeneral = 0;    // general blocks

@@ -53,8 +53,9 @@ extern "C" {
 
 /* arithmetic of the residual */
 #define FVGPU_FP64 0   /* everything in FP64, reference operation order */
-#define FVGPU_MIXED 1  /* reconstruction, EOS and fluxes in FP32; residual
-                          accumulation, RK update, sums and dt in FP64 */
+#define FVGPU_MIXED 1  /* reconstruction, EOS, gradients and fluxes (HLLC and
+                          viscous) in FP32; residual accumulation, RK update,
+                          sums, dt and the mixture-EOS pressure in FP64 */
 
 /* fvgpu_config.flags */
 #define FVGPU_FLAG_NO_BRICKS 1  /* mixed path: run every cell through the general
