@@ -12,10 +12,11 @@ noisy pressure).  The metric is Mcell-updates/s = cells x steps / s.
 precision (FP32-mixed when the library supports the case, else FP64) with
 the state resident in HBM; `fp64` holds the FP64 path; `e2e` repeats the
 measurement through the C ABI with the state copied from / to pinned host
-memory every step.  --impl reference times the CPU implementation of the
-same step (the oracle's C restatement of the reference, all host threads).
-Under torchrun each rank runs an independent replica (the path has no
-inter-rank exchange in this build); value = all ranks' cells / max time.
+memory every step (three contexts on three host threads by default).
+--impl reference times the CPU implementation of the same step (the
+oracle's C restatement of the reference, all host threads).  Under torchrun
+each rank runs an independent replica of the whole workload (the timed path
+exchanges nothing between ranks); value = all ranks' cells / max time.
 """
 from __future__ import annotations
 
