@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
       }
       const float sA = (plus || boundary) ? -A : A;
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, Fn[v], R[v]);
+      for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];  // separate roundings: equal and opposite face fluxes cancel exactly
     }
   }
 
@@ -1117,7 +1117,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
     const float A = s_geo[f][(be >> f) & 1u][2];
     const float sA = plus ? -A : A;
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(sA, flux[v][task], R[v]);
+    for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * flux[v][task];  // as the general kernel
   };
   add_face(1, tx_p, true);
   add_face(2, ty_p, true);
