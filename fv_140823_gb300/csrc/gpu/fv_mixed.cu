@@ -46,6 +46,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "fv_mixed.cuh"
@@ -348,9 +349,21 @@ __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int 
   return ok;
 }
 
+// Minmod-limited slope of one variable towards a face (reconctruct_V3.c:17-43,
+// slopes divided by dist_cc as multiplications) from the delta across the
+// face (d0) and across the opposite face (d1): zero unless the face is active
+// (not a domain boundary) and |d0| > 1e-10; otherwise the slope of smaller
+// magnitude when both have the same sign, else zero.  Written with min / max,
+// without branches; it equals the reference's sm*sp > 0 test except where that
+// product underflows.
+__device__ __forceinline__ float minmod_slope(bool active, float d0, float d1, float inv_p, float inv_m) {
+  const float sp = (active && fabsf(d0) > 1e-10f) ? d0 * inv_p : 0.0f;
+  const float sm = -d1 * inv_m;
+  return fmaxf(fminf(sp, sm), 0.0f) + fminf(fmaxf(sp, sm), 0.0f);
+}
+
 // Minmod face value of face f of a cell with geometry code gx from its state
-// and the deltas across f (d0) and across the opposite face (d1)
-// (reconctruct_V3.c:17-43, slopes divided by dist_cc as multiplications).
+// and the deltas across f (d0) and across the opposite face (d1).
 __device__ __forceinline__ void recon_face(const GeoTables *geo, int32_t gx, int f, const float qx[kNeqMax],
                                            const float d0[kNeqMax], const float d1[kNeqMax],
                                            float out[kNeqMax]) {
@@ -360,15 +373,8 @@ __device__ __forceinline__ void recon_face(const GeoTables *geo, int32_t gx, int
   const float dcf = gf[0], inv_p = gf[1];
   const float inv_m = geo_face(geo, lev, opp_face(f), ro)[1];
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) {
-    float grad = 0.0f;
-    if (rf != kRelBoundary && fabsf(d0[v]) > 1e-10f) {
-      const float sp = d0[v] * inv_p;
-      const float sm = -d1[v] * inv_m;
-      if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
-    }
-    out[v] = fmaf(dcf, grad, qx[v]);
-  }
+  for (int v = 0; v < kNeqMax; ++v)
+    out[v] = fmaf(dcf, minmod_slope(rf != kRelBoundary, d0[v], d1[v], inv_p, inv_m), qx[v]);
 }
 
 __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
@@ -838,14 +844,9 @@ __host__ __device__ constexpr int tile_index(int x, int y, int z) { return ((z +
 __host__ __device__ constexpr bool in_brick(int x, int y, int z) {
   return x >= 0 && x < BX && y >= 0 && y < BY && z >= 0 && z < BZ;
 }
-__device__ __forceinline__ int morton_local(int x, int y, int z) {
+__host__ __device__ constexpr int morton_local(int x, int y, int z) {
   return (x & 1) | ((y & 1) << 1) | ((z & 1) << 2) | (((x >> 1) & 1) << 3) | (((y >> 1) & 1) << 4) |
          (((z >> 1) & 1) << 5) | (((x >> 2) & 1) << 6) | (((y >> 2) & 1) << 7);
-}
-__device__ __forceinline__ void morton_decode(int t, int &x, int &y, int &z) {
-  x = (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2);
-  y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
-  z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
 }
 // bit f set when a brick cell lies on the brick's face-f side (0 for halo cells)
 __host__ __device__ constexpr uint32_t edge_mask(int x, int y, int z) {
@@ -889,6 +890,69 @@ constexpr BrickTasks make_brick_tasks() {
   return T;
 }
 __device__ const BrickTasks g_brick_tasks = make_brick_tasks();
+
+// Halo cells of a brick, two layers beyond each side: x sides, then y, then
+// z.  Packed: tile index (11 bits), brick side the cell lies beyond (3),
+// Morton offset of the cell within its own brick (8).
+struct BrickHalo {
+  uint32_t h[kHalo];
+};
+constexpr BrickHalo make_brick_halo() {
+  BrickHalo H{};
+  for (int h = 0; h < kHalo; ++h) {
+    int hx = 0, hy = 0, hz = 0, side = 0, lx = 0, ly = 0, lz = 0;
+    if (h < 4 * BY * BZ) {
+      const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ), layer = 1 + r / (BY * BZ), rr = r % (BY * BZ);
+      hy = ly = rr % BY;
+      hz = lz = rr / BY;
+      side = s == 0 ? 3 : 1;
+      hx = s == 0 ? -layer : BX - 1 + layer;
+      lx = s == 0 ? BX - layer : layer - 1;
+    } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
+      const int hh = h - 4 * BY * BZ;
+      const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ), layer = 1 + r / (BX * BZ), rr = r % (BX * BZ);
+      hx = lx = rr % BX;
+      hz = lz = rr / BX;
+      side = s == 0 ? 0 : 2;
+      hy = s == 0 ? -layer : BY - 1 + layer;
+      ly = s == 0 ? BY - layer : layer - 1;
+    } else {
+      const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
+      const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY), layer = 1 + r / (BX * BY), rr = r % (BX * BY);
+      hx = lx = rr % BX;
+      hy = ly = rr / BX;
+      side = s == 0 ? 4 : 5;
+      hz = s == 0 ? -layer : BZ - 1 + layer;
+      lz = s == 0 ? BZ - layer : layer - 1;
+    }
+    H.h[h] = uint32_t(tile_index(hx, hy, hz)) | (uint32_t(side) << 11) | (uint32_t(morton_local(lx, ly, lz)) << 14);
+  }
+  return H;
+}
+__device__ const BrickHalo g_brick_halo = make_brick_halo();
+
+// Brick cells in Morton order.  Word 0: tile index (11 bits), edge mask (6),
+// face task of the +x face (9); word 1: face tasks of the +y and +z faces
+// (10 + 10).  The -x, -y, -z tasks are 1, BX and BX*BY below them.
+struct BrickCells {
+  uint32_t w[2 * kBlock];
+};
+constexpr BrickCells make_brick_cells() {
+  BrickCells C{};
+  for (int t = 0; t < kBlock; ++t) {
+    const int x = (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2);
+    const int y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
+    const int z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
+    const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
+    const int ty_p = kFacesX + z * BX * (BY + 1) + (y + 1) * BX + x;
+    const int tz_p = kFacesX + kFacesY + (z + 1) * BX * BY + y * BX + x;
+    C.w[2 * t] = uint32_t(tile_index(x, y, z)) | (edge_mask(x, y, z) << 11) | (uint32_t(tx_p) << 17);
+    C.w[2 * t + 1] = uint32_t(ty_p) | (uint32_t(tz_p) << 10);
+  }
+  return C;
+}
+__device__ const BrickCells g_brick_cells = make_brick_cells();
+static_assert(kTile <= 2048 && kFacesX <= 512 && kFaces <= 1024, "brick table fields");
 
 // CFL radius of a brick cell: the frames are axis-aligned (checked at
 // upload), so |u.n| on face f is the magnitude of one velocity component --
@@ -947,46 +1011,19 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SN + int64_t(v) * n + start + 16 * l));
   }
   // A1: the brick's cells and the halo from the six neighbour bricks
-  int x, y, z;
-  morton_decode(t, x, y, z);
   {
-    const int ti = tile_index(x, y, z);
+    const int ti = int(__ldg(&g_brick_cells.w[2 * t]) & 2047u);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = v < neq ? __ldg(a.Sin + v * n + c) : 0.0f;
   }
 #pragma unroll
   for (int h = t; h < kHalo; h += kBlock) {
-    // halo cell h: side, layer and position (x sides, y sides, z sides)
-    int hx, hy, hz, side, lx, ly, lz;
-    if (h < 4 * BY * BZ) {
-      const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ), layer = 1 + r / (BY * BZ), rr = r % (BY * BZ);
-      hy = ly = rr % BY;
-      hz = lz = rr / BY;
-      side = s == 0 ? 3 : 1;
-      hx = s == 0 ? -layer : BX - 1 + layer;
-      lx = s == 0 ? BX - layer : layer - 1;
-    } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
-      const int hh = h - 4 * BY * BZ;
-      const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ), layer = 1 + r / (BX * BZ), rr = r % (BX * BZ);
-      hx = lx = rr % BX;
-      hz = lz = rr / BX;
-      side = s == 0 ? 0 : 2;
-      hy = s == 0 ? -layer : BY - 1 + layer;
-      ly = s == 0 ? BY - layer : layer - 1;
-    } else {
-      const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
-      const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY), layer = 1 + r / (BX * BY), rr = r % (BX * BY);
-      hx = lx = rr % BX;
-      hy = ly = rr / BX;
-      side = s == 0 ? 4 : 5;
-      hz = s == 0 ? -layer : BZ - 1 + layer;
-      lz = s == 0 ? BZ - layer : layer - 1;
-    }
-    const int base = __ldg(&bdp->side[side]);
+    const uint32_t e = __ldg(&g_brick_halo.h[h]);
+    const int base = __ldg(&bdp->side[(e >> 11) & 7u]);
     if (base >= 0) {
       float q[kNeqMax];
-      global_state(mc, a, base + morton_local(lx, ly, lz), q);
-      const int ti = tile_index(hx, hy, hz);
+      global_state(mc, a, base + int(e >> 14), q);
+      const int ti = int(e & 2047u);
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = q[v];
     }
@@ -1040,8 +1077,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   __syncthreads();
 
   // face value of the face g of the tile cell at ti (edge mask e), with the
-  // values across g at ti + dg and across the opposite face at ti - dg
-  auto recon_tile = [&](int ti, uint32_t e, int g, int dg, float out[kNeqMax]) {
+  // values across g at ti + dg and across the opposite face at ti - dg.
+  // EDGE: the brick has a side on the domain boundary.
+  auto recon_tile = [&](auto edge, int ti, uint32_t e, int g, int dg, float out[kNeqMax]) {
+    constexpr bool EDGE = decltype(edge)::value;
     float qp[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) qp[v] = tile[v][ti];
@@ -1050,68 +1089,68 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
       for (int v = 0; v < kNeqMax; ++v) out[v] = qp[v];
       return;
     }
-    const uint32_t be = e & bmask;
-    const int rg = (be >> g) & 1u, ro = (be >> opp_face(g)) & 1u;
+    int rg = 0, ro = 0;
+    if (EDGE) {
+      const uint32_t be = e & bmask;
+      rg = (be >> g) & 1u;
+      ro = (be >> opp_face(g)) & 1u;
+    }
     const float dcf = s_geo[g][rg][0], inv_p = s_geo[g][rg][1], inv_m = s_geo[opp_face(g)][ro][1];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
       const float d0 = tile[v][ti + dg] - qp[v];
       const float d1 = tile[v][ti - dg] - qp[v];
-      float grad = 0.0f;
-      if (!rg && fabsf(d0) > 1e-10f) {
-        const float sp = d0 * inv_p;
-        const float sm = -d1 * inv_m;
-        if (sm * sp > 0.0f) grad = fabsf(sm) > fabsf(sp) ? sp : sm;
-      }
-      out[v] = fmaf(dcf, grad, qp[v]);
+      out[v] = fmaf(dcf, minmod_slope(!rg, d0, d1, inv_p, inv_m), qp[v]);
     }
   };
 
   // B: face tasks -- each face of the brick once
-  bool ok = true;
+  auto face_tasks = [&](auto edge) {
+    constexpr bool EDGE = decltype(edge)::value;
+    bool fok = true;
 #pragma unroll 1
-  for (int task = t; task < kFaces; task += kBlock) {
-    const uint32_t e = __ldg(&g_brick_tasks.task[task]);
-    const int ti = int(e & 2047u);
-    const int axis = int((e >> 11) & 3u);
-    const bool low_in = (e >> 13) & 1u, up_in = (e >> 14) & 1u;
-    const uint32_t elo = (e >> 15) & 63u, eup = (e >> 21) & 63u;
-    const int st = axis == 0 ? 1 : (axis == 1 ? TX : TX * TY);
-    const int fp = axis == 0 ? 1 : (axis == 1 ? 2 : 5);
-    const int fm = opp_face(fp);
-    float Fn[kNeqMax];
-    const int bside = low_in ? fp : fm;
-    if (!(low_in && up_in) && s_side[bside] < 0) {
-      // the brick cell's own domain-boundary face, own frame (residual_faces_AMR.c:196-209)
-      float own[kNeqMax];
-      if (low_in)
-        recon_tile(ti, elo, fp, st, own);
-      else
-        recon_tile(ti + st, eup, fm, -st, own);
-      ok &= canonical_flux<MODEL>(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
-      if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
+    for (int task = t; task < kFaces; task += kBlock) {
+      const uint32_t e = __ldg(&g_brick_tasks.task[task]);
+      const int ti = int(e & 2047u);
+      const int axis = int((e >> 11) & 3u);
+      const bool low_in = (e >> 13) & 1u, up_in = (e >> 14) & 1u;
+      const uint32_t elo = (e >> 15) & 63u, eup = (e >> 21) & 63u;
+      const int st = axis == 0 ? 1 : (axis == 1 ? TX : TX * TY);
+      const int fp = axis == 0 ? 1 : (axis == 1 ? 2 : 5);
+      const int fm = opp_face(fp);
+      float Fn[kNeqMax];
+      const int bside = low_in ? fp : fm;
+      if (EDGE && !(low_in && up_in) && s_side[bside] < 0) {
+        // the brick cell's own domain-boundary face, own frame (residual_faces_AMR.c:196-209)
+        float own[kNeqMax];
+        if (low_in)
+          recon_tile(edge, ti, elo, fp, st, own);
+        else
+          recon_tile(edge, ti + st, eup, fm, -st, own);
+        fok &= canonical_flux<MODEL>(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
+        if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
+          for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
+        }
+      } else {
+        float lo[kNeqMax], hi[kNeqMax];
+        recon_tile(edge, ti, elo, fp, st, lo);
+        recon_tile(edge, ti + st, eup, fm, -st, hi);
+        fok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
       }
-    } else {
-      float lo[kNeqMax], hi[kNeqMax];
-      recon_tile(ti, elo, fp, st, lo);
-      recon_tile(ti + st, eup, fm, -st, hi);
-      ok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
-    }
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
-  }
+      for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
+    }
+    return fok;
+  };
+  const bool ok = bmask ? face_tasks(std::true_type{}) : face_tasks(std::false_type{});
   __syncthreads();
 
-  // C: gather in the fixed face order, RK stage update (coordinates decoded
-  // again: cheaper than keeping them live through the flux phase)
-  morton_decode(t, x, y, z);
-  const uint32_t be = edge_mask(x, y, z) & bmask;
+  // C: gather in the fixed face order, RK stage update
+  const uint32_t cw0 = __ldg(&g_brick_cells.w[2 * t]), cw1 = __ldg(&g_brick_cells.w[2 * t + 1]);
+  const uint32_t be = (cw0 >> 11) & 63u & bmask;
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
-  const int ty_p = kFacesX + z * BX * (BY + 1) + (y + 1) * BX + x;
-  const int tz_p = kFacesX + kFacesY + (z + 1) * BX * BY + y * BX + x;
+  const int tx_p = int(cw0 >> 17), ty_p = int(cw1 & 1023u), tz_p = int(cw1 >> 10);
   // order +x, +y, +z, -x, -y, -z as in the general kernel
   auto add_face = [&](int f, int task, bool plus) {
     const float A = s_geo[f][(be >> f) & 1u][2];
