@@ -81,7 +81,6 @@ struct GeoTables {
 
 __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return ((level * 6 + f) * 4 + rel); }
 // + faces: normals +x (1), +y (2), +z (5); their slot in the flux table
-__host__ __device__ constexpr bool is_plus_face(int f) { return f == 1 || f == 2 || f == 5; }
 __device__ __forceinline__ int plus_slot(int f) { return f == 1 ? 0 : (f == 2 ? 1 : 2); }
 // residual accumulation order (both kernels): +x, +y, +z, -x, -y, -z
 __device__ __forceinline__ int face_of_iter(int it) {
@@ -226,14 +225,91 @@ struct LS {
   float p, c, e, y;
 };
 
-template <int MODEL>
+// Face frames of the reference's hexahedral cells (tagvector.c:40-53 on
+// axis-aligned cells; the mixed path requires them, checked at upload): n,
+// t1, t2 per face index.  Every row has one nonzero entry, +-1, so rotating
+// into and out of a face frame is a signed permutation of the components:
+// exact, and the same bits whether the face index is known at compile time
+// (brick faces) or only at run time.
+__host__ __device__ constexpr float std_frame(int f, int k) {
+  constexpr float t[6][9] = {{0, -1, 0, 1, 0, 0, 0, 0, 1},  {1, 0, 0, 0, 0, 1, 0, -1, 0},
+                             {0, 1, 0, 0, 0, 1, 1, 0, 0},   {-1, 0, 0, 0, -1, 0, 0, 0, 1},
+                             {0, 0, -1, 1, 0, 0, 0, -1, 0}, {0, 0, 1, 0, -1, 0, 1, 0, 0}};
+  return t[f][k];
+}
+// column of the nonzero entry of row r of frame f; row whose nonzero entry
+// is in column k; sign of row r (compile-time use only)
+__host__ __device__ constexpr int frame_col(int f, int r) {
+  return std_frame(f, 3 * r) != 0.0f ? 0 : (std_frame(f, 3 * r + 1) != 0.0f ? 1 : 2);
+}
+__host__ __device__ constexpr int frame_row(int f, int k) {
+  return std_frame(f, k) != 0.0f ? 0 : (std_frame(f, 3 + k) != 0.0f ? 1 : 2);
+}
+__host__ __device__ constexpr bool frame_neg(int f, int r) { return std_frame(f, 3 * r + frame_col(f, r)) < 0.0f; }
+
+template <int F, int R>
+__device__ __forceinline__ float frame_in_row(const float q[kNeqMax]) {
+  constexpr int k = frame_col(F, R);
+  constexpr bool neg = frame_neg(F, R);
+  return neg ? -q[1 + k] : q[1 + k];
+}
+template <int F, int K>
+__device__ __forceinline__ float frame_out_col(float a, float b, float c) {
+  constexpr int r = frame_row(F, K);
+  constexpr bool neg = frame_neg(F, r);
+  const float x = r == 0 ? a : (r == 1 ? b : c);
+  return neg ? -x : x;
+}
+template <int F>
+__device__ __forceinline__ void frame_in_f(const float q[kNeqMax], float &mn, float &mm, float &ml) {
+  mn = frame_in_row<F, 0>(q);
+  mm = frame_in_row<F, 1>(q);
+  ml = frame_in_row<F, 2>(q);
+}
+template <int F>
+__device__ __forceinline__ void frame_out_f(float a, float b, float c, float out[kNeqMax]) {
+  out[1] = frame_out_col<F, 0>(a, b, c);
+  out[2] = frame_out_col<F, 1>(a, b, c);
+  out[3] = frame_out_col<F, 2>(a, b, c);
+}
+// momentum into the frame of face F (F < 0: face f, known at run time)
+template <int F>
+__device__ __forceinline__ void frame_in(int f, const float q[kNeqMax], float &mn, float &mm, float &ml) {
+  if constexpr (F >= 0) {
+    frame_in_f<F>(q, mn, mm, ml);
+  } else {
+    switch (f) {
+      case 0: frame_in_f<0>(q, mn, mm, ml); break;
+      case 1: frame_in_f<1>(q, mn, mm, ml); break;
+      case 2: frame_in_f<2>(q, mn, mm, ml); break;
+      case 3: frame_in_f<3>(q, mn, mm, ml); break;
+      case 4: frame_in_f<4>(q, mn, mm, ml); break;
+      default: frame_in_f<5>(q, mn, mm, ml); break;
+    }
+  }
+}
+// face-frame momentum components (a, b, c) back to out[1..3]
+template <int F>
+__device__ __forceinline__ void frame_out(int f, float a, float b, float c, float out[kNeqMax]) {
+  if constexpr (F >= 0) {
+    frame_out_f<F>(a, b, c, out);
+  } else {
+    switch (f) {
+      case 0: frame_out_f<0>(a, b, c, out); break;
+      case 1: frame_out_f<1>(a, b, c, out); break;
+      case 2: frame_out_f<2>(a, b, c, out); break;
+      case 3: frame_out_f<3>(a, b, c, out); break;
+      case 4: frame_out_f<4>(a, b, c, out); break;
+      default: frame_out_f<5>(a, b, c, out); break;
+    }
+  }
+}
+
+template <int MODEL, int F = -1>
 __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float q[kNeqMax], bool clip, LS &s) {
-  const float *fr = mc.fr + 9 * f;
   s.r = q[0];
   s.q4 = q[4];
-  s.mn = fmaf(q[3], fr[2], fmaf(q[2], fr[1], q[1] * fr[0]));
-  s.mm = fmaf(q[3], fr[5], fmaf(q[2], fr[4], q[1] * fr[3]));
-  s.ml = fmaf(q[3], fr[8], fmaf(q[2], fr[7], q[1] * fr[6]));
+  frame_in<F>(f, q, s.mn, s.mm, s.ml);
   const float rinv = fast_rcp(s.r);
   s.un = s.mn * rinv;
   s.um = s.mm * rinv;
@@ -263,10 +339,10 @@ __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const f
 // Ghost of a boundary face in the face-local frame (bc.c:19-49): inflow
 // state, transmissive copy, slip wall (normal velocity mirrored), no-slip
 // wall (velocity reversed).
-template <int MODEL>
+template <int MODEL, int F = -1>
 __device__ __forceinline__ void local_ghost(const MixedConst &mc, int bc, int f, LS &g) {
   if (bc == 1) {
-    local_state<MODEL>(mc, f, mc.inflow, false, g);
+    local_state<MODEL, F>(mc, f, mc.inflow, false, g);
   } else if (bc == 3 || bc == 4) {
     g.un = -g.un;
     if (bc == 4) {
@@ -283,7 +359,7 @@ __device__ __forceinline__ void local_ghost(const MixedConst &mc, int bc, int f,
 // (hllc_euler.c:3-55, compute_wave_speeds.c:3-88, star_region_euler.c:3-40,
 // contracted with n as residual_faces_AMR.c:145-149), evaluated in the face
 // frame and rotated back once.
-template <int MODEL>
+template <int MODEL, int F = -1>
 __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, const LS &L, const LS &R,
                                            float Fn[kNeqMax]) {
   const float SR = fmaxf(L.un + L.c, R.un + R.c);
@@ -322,30 +398,27 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
     Fc = fmaf(SK, fmaf(cS, Kul, -Kml), Fc);
     F4 = fmaf(SK, us4 - Kq4, F4);
   }
-  const float *fr = mc.fr + 9 * f;
   Fn[0] = F0;
-  Fn[1] = fmaf(fr[6], Fc, fmaf(fr[3], Fb, fr[0] * Fa));
-  Fn[2] = fmaf(fr[7], Fc, fmaf(fr[4], Fb, fr[1] * Fa));
-  Fn[3] = fmaf(fr[8], Fc, fmaf(fr[5], Fb, fr[2] * Fa));
+  frame_out<F>(f, Fa, Fb, Fc, Fn);
   Fn[4] = F4;
   return ok && (r1 || r2 || r3 || r4);
 }
 
 // Canonical flux of a face from the lower / upper face values (bc > 0: a
 // domain-boundary face, the upper side is the ghost of the lower one).
-template <int MODEL>
+template <int MODEL, int F = -1>
 __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int bc, bool clip,
                                                const float lo[kNeqMax], const float hi[kNeqMax],
                                                float Fn[kNeqMax]) {
   LS Ls, Rs;
-  bool ok = local_state<MODEL>(mc, f, lo, clip, Ls);
+  bool ok = local_state<MODEL, F>(mc, f, lo, clip, Ls);
   if (bc > 0) {
     Rs = Ls;
-    local_ghost<MODEL>(mc, bc, f, Rs);
+    local_ghost<MODEL, F>(mc, bc, f, Rs);
   } else {
-    ok &= local_state<MODEL>(mc, f, hi, clip, Rs);
+    ok &= local_state<MODEL, F>(mc, f, hi, clip, Rs);
   }
-  ok &= local_hllc<MODEL>(mc, f, bc, Ls, Rs, Fn);
+  ok &= local_hllc<MODEL, F>(mc, f, bc, Ls, Rs, Fn);
   return ok;
 }
 
@@ -1132,11 +1205,29 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
         }
-      } else {
+      } else if (EDGE) {
         float lo[kNeqMax], hi[kNeqMax];
         recon_tile(edge, ti, elo, fp, st, lo);
         recon_tile(edge, ti + st, eup, fm, -st, hi);
         fok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
+      } else {
+        // face index, stride and frame as compile-time constants (the axis is
+        // uniform across each warp: the task table lists x, y, z faces in
+        // runs of 288, 288, 320)
+        auto inner = [&](auto fpc) {
+          constexpr int FP = decltype(fpc)::value;
+          constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : TX * TY);
+          float lo[kNeqMax], hi[kNeqMax];
+          recon_tile(edge, ti, elo, FP, ST, lo);
+          recon_tile(edge, ti + ST, eup, opp_face(FP), -ST, hi);
+          fok &= canonical_flux<MODEL, FP>(mc, FP, 0, muscl, lo, hi, Fn);
+        };
+        if (axis == 0)
+          inner(std::integral_constant<int, 1>{});
+        else if (axis == 1)
+          inner(std::integral_constant<int, 2>{});
+        else
+          inner(std::integral_constant<int, 5>{});
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
@@ -1331,28 +1422,14 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     snprintf(why, whylen, "the mixed path needs the per-cell level array");
     return FVGPU_ERR_UNSUPPORTED;
   }
-  // + faces must carry +x, +y, +z normals and each face its opposite's negation
-  static const int axis[6] = {1, 0, 1, 0, 2, 2};
-  for (int f = 0; f < 6; ++f) {
-    for (int k = 0; k < 3; ++k) {
-      const double nk = m->frames[9 * f + k];
-      const double want = k == axis[f] ? (is_plus_face(f) ? 1.0 : -1.0) : 0.0;
-      if (nk != want) {
-        snprintf(why, whylen, "the mixed path needs axis-aligned face frames (face %d)", f);
+  // fluxes are evaluated in the face frames of the reference's hexahedral
+  // cells, compiled in as signed permutations
+  for (int f = 0; f < 6; ++f)
+    for (int k = 0; k < 9; ++k)
+      if (m->frames[9 * f + k] != double(std_frame(f, k))) {
+        snprintf(why, whylen, "the mixed path needs the hexahedral cells' face frames (face %d)", f);
         return FVGPU_ERR_UNSUPPORTED;
       }
-    }
-    // fluxes are evaluated in the face frame: n, t1, t2 must be orthonormal
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        const double *a = m->frames + 9 * f + 3 * i, *b = m->frames + 9 * f + 3 * j;
-        const double dot = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-        if (std::fabs(dot - (i == j ? 1.0 : 0.0)) > 1e-12) {
-          snprintf(why, whylen, "the mixed path needs orthonormal face frames (face %d)", f);
-          return FVGPU_ERR_UNSUPPORTED;
-        }
-      }
-  }
   const int64_t n = m->ncells;
   GeoTables gt;
   memset(&gt, 0, sizeof gt);
