@@ -928,32 +928,46 @@ __host__ __device__ constexpr uint32_t edge_mask(int x, int y, int z) {
          (z == 0 ? 16u : 0u) | (z == BZ - 1 ? 32u : 0u);
 }
 
-// Face tasks of a brick: x faces (lower x = -1..7), then y, then z.  Packed:
-// tile index of the lower cell (11 bits), axis (2), lower / upper cell inside
-// the brick (1 + 1), edge masks of the lower and upper cells (6 + 6).
+// Face tasks of a brick, in flux-slot order: the +x, +y, +z faces of the
+// 256 brick cells in Morton order (slots axis * 256 + t), then the faces on
+// the brick's -x, -y, -z sides (32 + 32 + 64 slots, x fastest).  Lanes of a
+// warp then read tile cells in distinct shared-memory banks.  Packed: tile
+// index of the lower cell (11 bits), axis (2), lower / upper cell inside the
+// brick (1 + 1), edge masks of the lower and upper cells (6 + 6).
 struct BrickTasks {
   uint32_t task[kFaces];
 };
+__host__ __device__ constexpr int morton_x(int t) { return (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2); }
+__host__ __device__ constexpr int morton_y(int t) { return ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2); }
+__host__ __device__ constexpr int morton_z(int t) { return ((t >> 2) & 1) | (((t >> 5) & 1) << 1); }
+constexpr int kSlotSideX = 3 * kBlock, kSlotSideY = kSlotSideX + BY * BZ, kSlotSideZ = kSlotSideY + BX * BZ;
 constexpr BrickTasks make_brick_tasks() {
   BrickTasks T{};
   for (int task = 0; task < kFaces; ++task) {
     int axis = 0, lx = 0, ly = 0, lz = 0;
-    if (task < kFacesX) {
-      lx = task % (BX + 1) - 1;
-      ly = (task / (BX + 1)) % BY;
-      lz = task / ((BX + 1) * BY);
-    } else if (task < kFacesX + kFacesY) {
-      const int r = task - kFacesX;
+    if (task < kSlotSideX) {
+      axis = task / kBlock;
+      const int t = task % kBlock;
+      lx = morton_x(t);
+      ly = morton_y(t);
+      lz = morton_z(t);
+    } else if (task < kSlotSideY) {
+      const int r = task - kSlotSideX;
+      lx = -1;
+      ly = r % BY;
+      lz = r / BY;
+    } else if (task < kSlotSideZ) {
+      const int r = task - kSlotSideY;
       axis = 1;
       lx = r % BX;
-      ly = (r / BX) % (BY + 1) - 1;
-      lz = r / (BX * (BY + 1));
+      ly = -1;
+      lz = r / BX;
     } else {
-      const int r = task - kFacesX - kFacesY;
+      const int r = task - kSlotSideZ;
       axis = 2;
       lx = r % BX;
-      ly = (r / BX) % BY;
-      lz = r / (BX * BY) - 1;
+      ly = r / BX;
+      lz = -1;
     }
     const int ux = lx + (axis == 0), uy = ly + (axis == 1), uz = lz + (axis == 2);
     T.task[task] = uint32_t(tile_index(lx, ly, lz)) | (uint32_t(axis) << 11) |
@@ -1004,28 +1018,26 @@ constexpr BrickHalo make_brick_halo() {
 }
 __device__ const BrickHalo g_brick_halo = make_brick_halo();
 
-// Brick cells in Morton order.  Word 0: tile index (11 bits), edge mask (6),
-// face task of the +x face (9); word 1: face tasks of the +y and +z faces
-// (10 + 10).  The -x, -y, -z tasks are 1, BX and BX*BY below them.
+// Brick cells in Morton order.  Word 0: tile index (11 bits), edge mask (6);
+// word 1: flux slots of the cell's -x, -y, -z faces (10 bits each).  The +x,
+// +y, +z faces are slots t, 256 + t, 512 + t.
 struct BrickCells {
   uint32_t w[2 * kBlock];
 };
 constexpr BrickCells make_brick_cells() {
   BrickCells C{};
   for (int t = 0; t < kBlock; ++t) {
-    const int x = (t & 1) | (((t >> 3) & 1) << 1) | (((t >> 6) & 1) << 2);
-    const int y = ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2);
-    const int z = ((t >> 2) & 1) | (((t >> 5) & 1) << 1);
-    const int tx_p = z * (BX + 1) * BY + y * (BX + 1) + x + 1;
-    const int ty_p = kFacesX + z * BX * (BY + 1) + (y + 1) * BX + x;
-    const int tz_p = kFacesX + kFacesY + (z + 1) * BX * BY + y * BX + x;
-    C.w[2 * t] = uint32_t(tile_index(x, y, z)) | (edge_mask(x, y, z) << 11) | (uint32_t(tx_p) << 17);
-    C.w[2 * t + 1] = uint32_t(ty_p) | (uint32_t(tz_p) << 10);
+    const int x = morton_x(t), y = morton_y(t), z = morton_z(t);
+    const int mx = x > 0 ? morton_local(x - 1, y, z) : kSlotSideX + y + BY * z;
+    const int my = y > 0 ? kBlock + morton_local(x, y - 1, z) : kSlotSideY + x + BX * z;
+    const int mz = z > 0 ? 2 * kBlock + morton_local(x, y, z - 1) : kSlotSideZ + x + BX * y;
+    C.w[2 * t] = uint32_t(tile_index(x, y, z)) | (edge_mask(x, y, z) << 11);
+    C.w[2 * t + 1] = uint32_t(mx) | (uint32_t(my) << 10) | (uint32_t(mz) << 20);
   }
   return C;
 }
 __device__ const BrickCells g_brick_cells = make_brick_cells();
-static_assert(kTile <= 2048 && kFacesX <= 512 && kFaces <= 1024, "brick table fields");
+static_assert(kTile <= 2048 && kFaces <= 1024 && kSlotSideZ + BX * BY == kFaces, "brick table fields");
 
 // CFL radius of a brick cell: the frames are axis-aligned (checked at
 // upload), so |u.n| on face f is the magnitude of one velocity component --
@@ -1213,7 +1225,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
       } else {
         // face index, stride and frame as compile-time constants (the axis is
         // uniform across each warp: the task table lists x, y, z faces in
-        // runs of 288, 288, 320)
+        // runs of 256, then 32, 32, 64)
         auto inner = [&](auto fpc) {
           constexpr int FP = decltype(fpc)::value;
           constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : TX * TY);
@@ -1241,7 +1253,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   const uint32_t cw0 = __ldg(&g_brick_cells.w[2 * t]), cw1 = __ldg(&g_brick_cells.w[2 * t + 1]);
   const uint32_t be = (cw0 >> 11) & 63u & bmask;
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  const int tx_p = int(cw0 >> 17), ty_p = int(cw1 & 1023u), tz_p = int(cw1 >> 10);
+  const int sx_m = int(cw1 & 1023u), sy_m = int((cw1 >> 10) & 1023u), sz_m = int(cw1 >> 20);
   // order +x, +y, +z, -x, -y, -z as in the general kernel
   auto add_face = [&](int f, int task, bool plus) {
     const float A = s_geo[f][(be >> f) & 1u][2];
@@ -1249,12 +1261,12 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * flux[v][task];  // as the general kernel
   };
-  add_face(1, tx_p, true);
-  add_face(2, ty_p, true);
-  add_face(5, tz_p, true);
-  add_face(3, tx_p - 1, false);
-  add_face(0, ty_p - BX, false);
-  add_face(4, tz_p - BX * BY, false);
+  add_face(1, t, true);
+  add_face(2, kBlock + t, true);
+  add_face(5, 2 * kBlock + t, true);
+  add_face(3, sx_m, false);
+  add_face(0, sy_m, false);
+  add_face(4, sz_m, false);
   float qn[kNeqMax], lam = 0.0f;
   if (stage_update<MODEL>(mc, a, c, s_dtv, R, ok, qn) && a.lambda)
     lam = brick_lambda<MODEL>(mc, qn, be, s_geo, s_inv2vol);
