@@ -1095,6 +1095,14 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
     const int v = t >> 4, l = t & 15;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SN + int64_t(v) * n + start + 16 * l));
   }
+  if (a.Din && t >= 128 && t < 168) {  // the stage-input increment read in the update
+    const int v = (t - 128) >> 3, l = t & 7;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + int64_t(v) * n + start + 32 * l));
+  }
+  if (a.Din && !a.last && t >= 168 && t < 208) {  // and the FP32 step-start state
+    const int v = (t - 168) >> 3, l = (t - 168) & 7;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + int64_t(v) * n + start + 32 * l));
+  }
   // A1: the brick's cells and the halo from the six neighbour bricks
   {
     const int ti = int(__ldg(&g_brick_cells.w[2 * t]) & 2047u);
