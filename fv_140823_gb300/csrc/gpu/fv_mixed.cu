@@ -1166,8 +1166,8 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
         }
       }
     }
+    __syncthreads();  // bmask is uniform across the block
   }
-  __syncthreads();
 
   // face value of the face g of the tile cell at ti (edge mask e), with the
   // values across g at ti + dg and across the opposite face at ti - dg.
@@ -1225,36 +1225,52 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
         }
-      } else if (EDGE) {
+      } else {
         float lo[kNeqMax], hi[kNeqMax];
         recon_tile(edge, ti, elo, fp, st, lo);
         recon_tile(edge, ti + st, eup, fm, -st, hi);
         fok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
-      } else {
-        // face index, stride and frame as compile-time constants (the axis is
-        // uniform across each warp: the task table lists x, y, z faces in
-        // runs of 256, then 32, 32, 64)
-        auto inner = [&](auto fpc) {
-          constexpr int FP = decltype(fpc)::value;
-          constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : TX * TY);
-          float lo[kNeqMax], hi[kNeqMax];
-          recon_tile(edge, ti, elo, FP, ST, lo);
-          recon_tile(edge, ti + ST, eup, opp_face(FP), -ST, hi);
-          fok &= canonical_flux<MODEL, FP>(mc, FP, 0, muscl, lo, hi, Fn);
-        };
-        if (axis == 0)
-          inner(std::integral_constant<int, 1>{});
-        else if (axis == 1)
-          inner(std::integral_constant<int, 2>{});
-        else
-          inner(std::integral_constant<int, 5>{});
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
     }
     return fok;
   };
-  const bool ok = bmask ? face_tasks(std::true_type{}) : face_tasks(std::false_type{});
+  // The same for a brick off the domain boundary: each thread its cell's +x,
+  // +y, +z faces (slots t, 256 + t, 512 + t), then threads 0-127 the faces on
+  // the brick's lower sides; face index, stride and frame as compile-time
+  // constants (the axis is uniform across each warp).
+  auto face_tasks_inner = [&]() {
+    bool fok = true;
+    const int ti_own = int(__ldg(&g_brick_cells.w[2 * t]) & 2047u);
+    auto inner = [&](auto fpc, int ti, int slot) {
+      constexpr int FP = decltype(fpc)::value;
+      constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : TX * TY);
+      float lo[kNeqMax], hi[kNeqMax], Fn[kNeqMax];
+      recon_tile(std::false_type{}, ti, 0u, FP, ST, lo);
+      recon_tile(std::false_type{}, ti + ST, 0u, opp_face(FP), -ST, hi);
+      fok &= canonical_flux<MODEL, FP>(mc, FP, 0, muscl, lo, hi, Fn);
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
+    };
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+      int ti = ti_own, slot = k * kBlock + t, axis = k;
+      if (k == 3) {
+        if (slot >= kFaces) break;
+        ti = int(__ldg(&g_brick_tasks.task[slot]) & 2047u);
+        axis = slot < kSlotSideY ? 0 : (slot < kSlotSideZ ? 1 : 2);
+      }
+      if (axis == 0)
+        inner(std::integral_constant<int, 1>{}, ti, slot);
+      else if (axis == 1)
+        inner(std::integral_constant<int, 2>{}, ti, slot);
+      else
+        inner(std::integral_constant<int, 5>{}, ti, slot);
+    }
+    return fok;
+  };
+  const bool ok = bmask ? face_tasks(std::true_type{}) : face_tasks_inner();
   __syncthreads();
 
   // C: gather in the fixed face order, RK stage update
