@@ -492,33 +492,6 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
       geo->inv2vol[lev]);
 }
 
-// Exact FP32 -> FP64 and round-to-nearest FP64 -> FP32 conversions on the
-// integer pipe (the hardware conversions run on GB300's slow FP64 pipe);
-// zero, subnormal, infinite and NaN values take the hardware path.
-__device__ __forceinline__ double f2d_exact(float x) {
-  const uint32_t b = __float_as_uint(x);
-  const uint32_t e = (b >> 23) & 0xffu;
-  if (e - 1u < 254u)
-    return __longlong_as_double(static_cast<long long>((uint64_t(b & 0x80000000u) << 32) |
-                                                       (uint64_t(e + 896u) << 52) | (uint64_t(b & 0x7fffffu) << 29)));
-  if ((b << 1) == 0u) return __longlong_as_double(static_cast<long long>(uint64_t(b) << 32));
-  return double(x);
-}
-__device__ __forceinline__ float d2f_rn(double x) {
-  const uint64_t d = static_cast<uint64_t>(__double_as_longlong(x));
-  const uint32_t hi = uint32_t(d >> 32), lo = uint32_t(d);
-  const int e = int((hi >> 20) & 0x7ffu) - 896;
-  if (e >= 1 && e <= 254) {
-    const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    uint32_t r = (hi & 0x80000000u) | (uint32_t(e) << 23) | m;
-    const uint32_t rem = lo & 0x1fffffffu, half = 0x10000000u;
-    if (rem > half || (rem == half && (m & 1u))) r += 1u;
-    return __uint_as_float(r);
-  }
-  if ((d << 1) == 0u) return __uint_as_float(hi);
-  return __double2float_rn(x);
-}
-
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
 // CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
 template <int MODEL>
@@ -548,9 +521,9 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
   if (a.last) {
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      const double snew = __ldg(a.SN + v * n + c) + f2d_exact(dn[v]);
+      const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
       a.SNout[v * n + c] = snew;
-      qn[v] = d2f_rn(snew);
+      qn[v] = __double2float_rn(snew);
       a.SNfout[v * n + c] = qn[v];
     }
     return true;
@@ -1300,7 +1273,7 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
 // FP32 copy of an FP64 state (after an upload or an FP64-path step).
 __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-    Sf[i] = d2f_rn(S[i]);
+    Sf[i] = __double2float_rn(S[i]);
 }
 
 // The same with the CFL spectral radius of the copied state (the mixed
@@ -1315,7 +1288,7 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
       if (v >= mc.neq) break;
-      q[v] = d2f_rn(S[int64_t(v) * n + c]);
+      q[v] = __double2float_rn(S[int64_t(v) * n + c]);
       Sf[int64_t(v) * n + c] = q[v];
     }
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
