@@ -184,20 +184,26 @@ __device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f,
   if (bc == 1) {
     mixed_face_state<MODEL>(mc, mc.inflow, false, g);
   } else if (bc == 3 || bc == 4) {
+    // velocity and momentum mirrored as such (the momentum is not rebuilt as
+    // rho * u): exact on the axis-aligned faces, as in the FP64 path
     const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
     if (bc == 3) {
       const float un = fmaf(g.w, nz, fmaf(g.v, ny, g.u * nx));
       g.u = fmaf(-2.0f * un, nx, g.u);
       g.v = fmaf(-2.0f * un, ny, g.v);
       g.w = fmaf(-2.0f * un, nz, g.w);
+      const float mn = fmaf(g.q[3], nz, fmaf(g.q[2], ny, g.q[1] * nx));
+      g.q[1] = fmaf(-2.0f * mn, nx, g.q[1]);
+      g.q[2] = fmaf(-2.0f * mn, ny, g.q[2]);
+      g.q[3] = fmaf(-2.0f * mn, nz, g.q[3]);
     } else {
       g.u = -g.u;
       g.v = -g.v;
       g.w = -g.w;
+      g.q[1] = -g.q[1];
+      g.q[2] = -g.q[2];
+      g.q[3] = -g.q[3];
     }
-    g.q[1] = g.r * g.u;
-    g.q[2] = g.r * g.v;
-    g.q[3] = g.r * g.w;
   }
 }
 
@@ -346,13 +352,13 @@ __device__ __forceinline__ void local_ghost(const MixedConst &mc, int bc, int f,
     local_state<MODEL, F>(mc, f, mc.inflow, false, g);
   } else if (bc == 3 || bc == 4) {
     g.un = -g.un;
+    g.mn = -g.mn;
     if (bc == 4) {
       g.um = -g.um;
       g.ul = -g.ul;
+      g.mm = -g.mm;
+      g.ml = -g.ml;
     }
-    g.mn = g.r * g.un;
-    g.mm = g.r * g.um;
-    g.ml = g.r * g.ul;
   }
 }
 
@@ -426,14 +432,14 @@ __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int 
 // Minmod-limited slope of one variable towards a face (reconctruct_V3.c:17-43,
 // slopes divided by dist_cc as multiplications) from the delta across the
 // face (d0) and across the opposite face (d1): zero unless the face is active
-// (not a domain boundary) and |d0| > 1e-10; otherwise the slope of smaller
-// magnitude when both have the same sign, else zero.  Written with min / max,
-// without branches; it equals the reference's sm*sp > 0 test except where that
-// product underflows.
+// (not a domain boundary), |d0| > 1e-10 and sm * sp > 0; then the slope of
+// smaller magnitude.  Selects rather than branches.  A NaN product (a domain
+// boundary behind the cell has 1/dist_cc = inf and a zero delta) gives zero,
+// as in the reference.
 __device__ __forceinline__ float minmod_slope(bool active, float d0, float d1, float inv_p, float inv_m) {
-  const float sp = (active && fabsf(d0) > 1e-10f) ? d0 * inv_p : 0.0f;
-  const float sm = -d1 * inv_m;
-  return fmaxf(fminf(sp, sm), 0.0f) + fminf(fmaxf(sp, sm), 0.0f);
+  const float sp = d0 * inv_p, sm = -d1 * inv_m;
+  const float m = fabsf(sm) > fabsf(sp) ? sp : sm;
+  return (active && fabsf(d0) > 1e-10f && sm * sp > 0.0f) ? m : 0.0f;
 }
 
 // Minmod face value of face f of a cell with geometry code gx from its state

@@ -168,21 +168,28 @@ __device__ __forceinline__ void apply_bc(const Phys &ph, int bc, int f, FaceStat
     g.c = sqrt(gamma * (g.p + pinf) / g.r);
   } else if (bc == 3 || bc == 4) {
     // no reference code (bc_reflective / bc_wall are undefined): slip wall
-    // mirrors the normal velocity, no-slip wall reverses it.
+    // mirrors the normal velocity and momentum, no-slip wall reverses them.
+    // The momentum is mirrored as such (not rebuilt as rho * u), so on the
+    // axis-aligned faces the tangential components stay exactly the own
+    // values and the normal one is exactly negated.
     const T nx = T(ph.frames[9 * f + 0]), ny = T(ph.frames[9 * f + 1]), nz = T(ph.frames[9 * f + 2]);
     if (bc == 3) {
       const T un = (g.u * nx + g.v * ny) + g.w * nz;
       g.u = g.u - T(2.0) * un * nx;
       g.v = g.v - T(2.0) * un * ny;
       g.w = g.w - T(2.0) * un * nz;
+      const T mn = (g.vec[1] * nx + g.vec[2] * ny) + g.vec[3] * nz;
+      g.vec[1] = g.vec[1] - T(2.0) * mn * nx;
+      g.vec[2] = g.vec[2] - T(2.0) * mn * ny;
+      g.vec[3] = g.vec[3] - T(2.0) * mn * nz;
     } else {
       g.u = -g.u;
       g.v = -g.v;
       g.w = -g.w;
+      g.vec[1] = -g.vec[1];
+      g.vec[2] = -g.vec[2];
+      g.vec[3] = -g.vec[3];
     }
-    g.vec[1] = g.r * g.u;
-    g.vec[2] = g.r * g.v;
-    g.vec[3] = g.r * g.w;
   }
 }
 

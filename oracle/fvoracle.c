@@ -198,14 +198,19 @@ static void apply_bc(const fvgpu_config *cfg, int bc, const double *frame, fstat
       g->u = g->u - 2.0 * un * frame[0];
       g->v = g->v - 2.0 * un * frame[1];
       g->w = g->w - 2.0 * un * frame[2];
+      /* the momentum mirrored as such: exact on axis-aligned faces */
+      const double mn = (g->vec[1] * frame[0] + g->vec[2] * frame[1]) + g->vec[3] * frame[2];
+      g->vec[1] = g->vec[1] - 2.0 * mn * frame[0];
+      g->vec[2] = g->vec[2] - 2.0 * mn * frame[1];
+      g->vec[3] = g->vec[3] - 2.0 * mn * frame[2];
     } else {
       g->u = -g->u;
       g->v = -g->v;
       g->w = -g->w;
+      g->vec[1] = -g->vec[1];
+      g->vec[2] = -g->vec[2];
+      g->vec[3] = -g->vec[3];
     }
-    g->vec[1] = g->r * g->u;
-    g->vec[2] = g->r * g->v;
-    g->vec[3] = g->r * g->w;
   }
   /* bc == 2 (outflow): the ghost is the own state, bc.c:26-30 */
 }

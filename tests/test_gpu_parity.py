@@ -67,6 +67,26 @@ def test_residual_random_states_amr(periodic, ischeme, ns):
             assert bits_equal(s.sg(), orc.gradcalc(U))
 
 
+@pytest.mark.parametrize("ns", [0, 1])
+def test_wall_boundaries_match_oracle(ns):
+    """Slip (3) and no-slip (4) walls have no reference code; the oracle and
+    the GPU share one definition (velocity and momentum mirrored as such)."""
+    rng = np.random.default_rng(21)
+    c0 = rng.uniform(0.3, 0.7, 3)
+    m = uniform_mesh(3, side_bc=(3, 4, 3, 4, 3, 4))
+    refine_by(m, lambda l, c: ((c - c0[:, None]) ** 2).sum(0) < 0.06, 5)
+    t = m.flatten()
+    U = random_ideal_state(t.ncells, np.random.default_rng(22))
+    cfg = SolverConfig(model=1, ischeme=2, ns=ns, eos=ns, visc=0.01 * ns)
+    orc = Oracle(t, cfg)
+    with solver(t, cfg) as s:
+        assert bits_equal(s.residual(U), orc.residual(U))
+        assert bits_equal(s.sf(), orc.faceinterp(U))
+        s.set_state(U)
+        s.step("ssprk3", dt=1e-4, nsteps=2)
+        assert bits_equal(s.state(), orc.step(U, 1e-4, "ssprk3", 2))
+
+
 @pytest.mark.parametrize("scheme", ["euler", "ssprk2", "ssprk3"])
 @pytest.mark.parametrize("ischeme", [1, 2])
 def test_fixed_dt_steps(scheme, ischeme):
