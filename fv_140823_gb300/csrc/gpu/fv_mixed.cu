@@ -958,6 +958,32 @@ constexpr BrickTasks make_brick_tasks() {
 }
 __device__ const BrickTasks g_brick_tasks = make_brick_tasks();
 
+// The two cells of each face task (viscous runs read their gradients), 12
+// bits each, lower cell first: a brick cell is its Morton index; a cell of a
+// neighbour brick has bit 11 set, the brick side in bits 8-10 and its Morton
+// index within that brick in bits 0-7.
+__host__ __device__ constexpr uint32_t brick_cell_ref(int x, int y, int z) {
+  if (in_brick(x, y, z)) return uint32_t(morton_local(x, y, z));
+  const int side = x < 0 ? 3 : (x >= BX ? 1 : (y < 0 ? 0 : (y >= BY ? 2 : (z < 0 ? 4 : 5))));
+  return 2048u | (uint32_t(side) << 8) | uint32_t(morton_local((x + BX) % BX, (y + BY) % BY, (z + BZ) % BZ));
+}
+struct BrickTaskCells {
+  uint32_t c[kFaces];
+};
+constexpr BrickTaskCells make_brick_task_cells() {
+  BrickTaskCells C{};
+  const BrickTasks T = make_brick_tasks();
+  for (int task = 0; task < kFaces; ++task) {
+    const uint32_t e = T.task[task];
+    const int ti = int(e & 2047u), axis = int((e >> 11) & 3u);
+    const int lx = ti % TX - 2, ly = (ti / TX) % TY - 2, lz = ti / (TX * TY) - 2;
+    C.c[task] = brick_cell_ref(lx, ly, lz) |
+                (brick_cell_ref(lx + (axis == 0), ly + (axis == 1), lz + (axis == 2)) << 12);
+  }
+  return C;
+}
+__device__ const BrickTaskCells g_brick_task_cells = make_brick_task_cells();
+
 // Halo cells of a brick, two layers beyond each side: x sides, then y, then
 // z.  Packed: tile index (11 bits), brick side the cell lies beyond (3),
 // Morton offset of the cell within its own brick (8).
@@ -1040,8 +1066,8 @@ __device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float 
 #ifndef FV_BRICK_MIN_BLOCKS
 #define FV_BRICK_MIN_BLOCKS 5  // 48 registers: 5 blocks per SM measured faster than 4 (217 vs 257 us per stage, 128^3)
 #endif
-template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(MixedConst mc, StageArgs a) {
+template <int MODEL, bool MUSCL, bool NS>
+__global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_brick(MixedConst mc, StageArgs a) {
   __shared__ float tile[kNeqMax][kTile];
   __shared__ float flux[kNeqMax][kFaces];
   __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
@@ -1178,6 +1204,21 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
   };
 
   // B: face tasks -- each face of the brick once
+  // viscous runs: the global index of a face task's cell (brick_cell_ref)
+  // and the viscous normal flux of a face, subtracted as the general kernel
+  // does: (F - FV).n + FH
+  auto cell_of = [&](uint32_t r) -> int {
+    return (r & 2048u) ? s_side[(r >> 8) & 7u] + int(r & 255u) : start + int(r & 255u);
+  };
+  auto sub_viscous = [&](int f, int bc, int clo, int chi, const float lo[kNeqMax], const float hi[kNeqMax],
+                         float Fn[kNeqMax]) {
+    float gl[9], gh[9], FVn[kNeqMax];
+    load_grad9f(a.SG, n, clo, gl);
+    load_grad9f(a.SG, n, chi, gh);
+    viscous_normal(mc, f, bc, lo, hi, gl, gh, FVn);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
+  };
   auto face_tasks = [&](auto edge) {
     constexpr bool EDGE = decltype(edge)::value;
     bool fok = true;
@@ -1201,6 +1242,11 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
         else
           recon_tile(edge, ti + st, eup, fm, -st, own);
         fok &= canonical_flux<MODEL>(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
+        if (NS) {
+          const uint32_t cr = __ldg(&g_brick_task_cells.c[task]);
+          const int cown = cell_of(low_in ? (cr & 4095u) : (cr >> 12));
+          sub_viscous(bside, -1 - s_side[bside], cown, cown, own, own, Fn);
+        }
         if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
@@ -1210,6 +1256,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
         recon_tile(edge, ti, elo, fp, st, lo);
         recon_tile(edge, ti + st, eup, fm, -st, hi);
         fok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
+        if (NS) {
+          const uint32_t cr = __ldg(&g_brick_task_cells.c[task]);
+          sub_viscous(fp, 0, cell_of(cr & 4095u), cell_of(cr >> 12), lo, hi, Fn);
+        }
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
@@ -1230,6 +1280,10 @@ __global__ void __launch_bounds__(kBlock, FV_BRICK_MIN_BLOCKS) k_mixed_brick(Mix
       recon_tile(std::false_type{}, ti, 0u, FP, ST, lo);
       recon_tile(std::false_type{}, ti + ST, 0u, opp_face(FP), -ST, hi);
       fok &= canonical_flux<MODEL, FP>(mc, FP, 0, muscl, lo, hi, Fn);
+      if (NS) {
+        const uint32_t cr = __ldg(&g_brick_task_cells.c[slot]);
+        sub_viscous(FP, 0, cell_of(cr & 4095u), cell_of(cr >> 12), lo, hi, Fn);
+      }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
     };
@@ -1529,9 +1583,9 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   }
   // bricks: candidate starts, then keep those whose six sides resolve
   std::vector<char> is_brick(size_t(n), 0);
-  // viscous runs take the general kernel everywhere: its face evaluations read
-  // both cells' gradients straight from the gradient pass
-  if (!r.force_general && ph.ns != 1) {
+  // bricks for every inviscid run and for viscous runs of model 1 (both
+  // kernels read the cells' gradients straight from the gradient pass)
+  if (!r.force_general && (ph.ns != 1 || ph.model == 1)) {
     for (int64_t i = 0; i + kBlock <= n;) {
       if (brick_interior(m, i)) {
         is_brick[size_t(i)] = 1;
@@ -1656,8 +1710,10 @@ cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const do
 // the kernel instance of the configuration (EOS model, reconstruction order)
 template <int MODEL, bool MUSCL>
 void launch_instance(bool brick, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
-  if (brick)
-    k_mixed_brick<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+  if (brick && mc.ns == 1) {
+    if constexpr (MODEL == 1) k_mixed_brick<MODEL, MUSCL, true><<<grid, kBlock, 0, st>>>(mc, a);
+  } else if (brick)
+    k_mixed_brick<MODEL, MUSCL, false><<<grid, kBlock, 0, st>>>(mc, a);
   else
     k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
 }

@@ -168,7 +168,7 @@ def _mixed_state(case, flags, nsteps, dt):
         return s.state()
 
 
-@pytest.mark.parametrize("name", ["periodic", "sod", "bump", "inflow", "bubble"])
+@pytest.mark.parametrize("name", ["periodic", "sod", "bump", "inflow", "bubble", "tgv", "tgv_walls"])
 def test_brick_kernel_bit_identical_to_general_kernel(name):
     """The brick fast path and the table-driven kernel accumulate every cell's
     residual from the same canonical face fluxes in the same order."""
@@ -181,6 +181,13 @@ def test_brick_kernel_bit_identical_to_general_kernel(name):
         c.scheme = "ssprk3"
     elif name == "bubble":
         c = cases.bubble(base_level=4, extra_levels=1)
+    elif name == "tgv":  # viscous: both kernels subtract the same FP32 viscous flux
+        c = cases.tgv(base_level=5, extra_levels=1)
+    elif name == "tgv_walls":  # viscous next to slip and no-slip walls
+        from fv_140823_gb300.mesh import uniform_mesh
+        g = cases.tgv(base_level=4, extra_levels=0)
+        t = uniform_mesh(4, side_bc=(3, 4, 3, 4, 3, 4)).flatten()
+        c = cases.Case("tgv_walls", t, g.U, g.cfg, cfl=0.5, nsteps=5)
     else:
         from fv_140823_gb300.mesh import uniform_mesh
         t = uniform_mesh(5, side_bc=(2, 2, 2, 1, 2, 2)).flatten()
