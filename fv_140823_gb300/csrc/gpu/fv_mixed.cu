@@ -14,9 +14,9 @@
 // an FP32 copy SNf of the new state that the next step's stages read.  On
 // GB300 FP64 adds and multiplies run at ~1/70 of the FP32 rate (measured:
 // 0.51 against 37 T thread-ops/s), so the stages touch no FP64 value except
-// at the last one: the
-// per-stage increments are small against the state, their FP32 rounding is
-// ~1e-8 of the state per stage, and every add into the state is FP64.
+// at the last one: the per-stage increments are small against the state,
+// their FP32 rounding is ~1e-8 of the state per stage, and every add into
+// the state is FP64.
 //
 // Canonical face fluxes.  Every face flux is defined from the face's lower
 // cell (the one whose +x/+y/+z face it is), with that face's frame; the
@@ -25,12 +25,20 @@
 // without automatic multiply-add contraction, explicit fmaf only), so the
 // scheme is conservative and deterministic however the work is split.
 //
+// Face frames are those of the reference's hexahedral cells (checked at
+// upload), compiled in as signed permutations: rotating the momentum into
+// and out of a face frame is a choice of registers.
+//
 // Two kernels share that definition:
 //   k_mixed_brick    a Morton-aligned 8x8x4 brick of same-level cells whose
 //                    six sides are same-level bricks or domain boundaries:
-//                    brick + 2-deep face halo staged in shared memory, the
-//                    896 faces of the brick evaluated once each by dense
-//                    per-thread face tasks, no neighbour tables read;
+//                    brick + 2-deep face halo staged in shared memory through
+//                    constant index tables, the 896 faces of the brick
+//                    evaluated once each (a brick off the domain boundary:
+//                    each thread its cell's +x, +y, +z faces, then threads
+//                    0-127 the faces on the brick's lower sides), no
+//                    neighbour tables read; viscous runs (model 1) read the
+//                    two cells' gradients of each face;
 //   k_mixed_general  any other run of up to 256 consecutive cells (AMR
 //                    interfaces, 1:4 faces): table-driven, each thread
 //                    computes its + faces and publishes them, the upper cell
