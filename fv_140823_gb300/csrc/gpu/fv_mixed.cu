@@ -332,9 +332,9 @@ __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const f
   if (MODEL == 1) {
     s.e = q[4];
     s.y = 0.0f;
-    const float ke = fmaf(s.ul, s.ul, fmaf(s.um, s.um, s.un * s.un));
-    const float e_int = fmaf(-0.5f, ke, s.e * rinv);
-    s.p = fmaf(s.r * mc.gm1, e_int, -mc.gpinf);
+    // p = (gamma - 1) (E - rho |u|^2 / 2) - gamma pinf, rho |u|^2 as m . u
+    const float ke2 = fmaf(s.ml, s.ul, fmaf(s.mm, s.um, s.mn * s.un));
+    s.p = fmaf(mc.gm1, fmaf(-0.5f, ke2, s.e), -mc.gpinf);
     s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
     return true;
   }
@@ -403,10 +403,15 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   float Fc = Kmn * Kul;
   float F4 = MODEL == 1 ? (Ke + Kp) * Kun : Kmn * Ky;
   if (star) {
+    // star state of star_region_euler.c:3-40 with one reciprocal:
+    // cS = rho_K (S_K - u_K) / (S_K - S*); the energy
+    // cS [(S* - u_K)(S* + p_K / (rho_K (S_K - u_K))) + E_K / rho_K]
+    // = cS (S* - u_K) S* + ((S* - u_K) p_K + (S_K - u_K) E_K) / (S_K - S*)
     const float dK = SK - Kun;
-    const float cS = __fdividef(Kr * dK, SK - S_S);
-    const float us4 = MODEL == 1 ? cS * fmaf(S_S - Kun, S_S + __fdividef(Kp, Kr * dK), __fdividef(Ke, Kr))
-                                    : cS * Ky;
+    const float inv = fast_rcp(SK - S_S);
+    const float cS = (Kr * dK) * inv;
+    const float aK = S_S - Kun;
+    const float us4 = MODEL == 1 ? fmaf(cS * aK, S_S, inv * fmaf(aK, Kp, dK * Ke)) : cS * Ky;
     F0 = fmaf(SK, cS - Kr, F0);
     Fa = fmaf(SK, fmaf(cS, S_S, -Kmn), Fa);
     Fb = fmaf(SK, fmaf(cS, Kum, -Kmm), Fb);
