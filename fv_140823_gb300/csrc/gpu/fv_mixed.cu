@@ -391,33 +391,33 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
   const bool left = r1 || r2;
   const bool star = r2 || r3;
-  const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn, Kmm = left ? L.mm : R.mm;
-  const float Kml = left ? L.ml : R.ml, Kq4 = left ? L.q4 : R.q4;
+  const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn;
   const float Kun = left ? L.un : R.un, Kum = left ? L.um : R.um, Kul = left ? L.ul : R.ul;
   const float Kp = left ? L.p : R.p, Ke = left ? L.e : R.e, Ky = left ? L.y : R.y;
   const float SK = left ? SL : SR;
-  // physical flux in the face frame
-  float F0 = Kmn;
-  float Fa = fmaf(Kmn, Kun, Kp);
-  float Fb = Kmn * Kum;
-  float Fc = Kmn * Kul;
-  float F4 = MODEL == 1 ? (Ke + Kp) * Kun : Kmn * Ky;
+  // F_K + S_K (U*_K - U_K) is the physical flux of the star state U*_K
+  // (star_region_euler.c:3-40): mass flux rho* S*, pressure
+  // p* = p_K + rho_K (S_K - u_K)(S* - u_K), unchanged tangential velocity.
+  // So one flux formula serves both cases, from the upwind state or its star
+  // state, with one reciprocal.
+  float m = Kmn, un = Kun, pp = Kp, ee = Ke;
   if (star) {
-    // star state of star_region_euler.c:3-40 with one reciprocal:
-    // cS = rho_K (S_K - u_K) / (S_K - S*); the energy
-    // cS [(S* - u_K)(S* + p_K / (rho_K (S_K - u_K))) + E_K / rho_K]
-    // = cS (S* - u_K) S* + ((S* - u_K) p_K + (S_K - u_K) E_K) / (S_K - S*)
     const float dK = SK - Kun;
     const float inv = fast_rcp(SK - S_S);
-    const float cS = (Kr * dK) * inv;
+    const float rdK = Kr * dK;
+    const float cS = rdK * inv;  // rho*
     const float aK = S_S - Kun;
-    const float us4 = MODEL == 1 ? fmaf(cS * aK, S_S, inv * fmaf(aK, Kp, dK * Ke)) : cS * Ky;
-    F0 = fmaf(SK, cS - Kr, F0);
-    Fa = fmaf(SK, fmaf(cS, S_S, -Kmn), Fa);
-    Fb = fmaf(SK, fmaf(cS, Kum, -Kmm), Fb);
-    Fc = fmaf(SK, fmaf(cS, Kul, -Kml), Fc);
-    F4 = fmaf(SK, us4 - Kq4, F4);
+    m = cS * S_S;
+    un = S_S;
+    pp = fmaf(rdK, aK, Kp);
+    // E* = rho* [E_K / rho_K + (S* - u_K)(S* + p_K / (rho_K (S_K - u_K)))]
+    if (MODEL == 1) ee = fmaf(cS * aK, S_S, inv * fmaf(aK, Kp, dK * Ke));
   }
+  const float F0 = m;
+  const float Fa = fmaf(m, un, pp);
+  const float Fb = m * Kum;
+  const float Fc = m * Kul;
+  const float F4 = MODEL == 1 ? (ee + pp) * un : m * Ky;
   Fn[0] = F0;
   frame_out<F>(f, Fa, Fb, Fc, Fn);
   Fn[4] = F4;
