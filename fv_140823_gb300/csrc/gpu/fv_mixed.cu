@@ -904,6 +904,12 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
 
+// 4-byte asynchronous global -> shared copy (cp.async.ca)
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+
 // ============================= brick kernel =================================
 
 __host__ __device__ constexpr int tile_index(int x, int y, int z) { return ((z + 2) * TY + (y + 2)) * TX + (x + 2); }
@@ -1122,24 +1128,24 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
     const int v = (t - 168) >> 3, l = (t - 168) & 7;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + int64_t(v) * n + start + 32 * l));
   }
-  // A1: the brick's cells and the halo from the six neighbour bricks
+  // A1: the brick's cells and the halo from the six neighbour bricks, copied
+  // global -> shared asynchronously (cp.async, no register round trip)
   {
     const int ti = int(__ldg(&g_brick_cells.w[2 * t]) & 2047u);
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = v < neq ? __ldg(a.Sin + v * n + c) : 0.0f;
+    for (int v = 0; v < kNeqMax; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
   }
 #pragma unroll
   for (int h = t; h < kHalo; h += kBlock) {
     const uint32_t e = __ldg(&g_brick_halo.h[h]);
     const int base = __ldg(&bdp->side[(e >> 11) & 7u]);
     if (base >= 0) {
-      float q[kNeqMax];
-      global_state(mc, a, base + int(e >> 14), q);
-      const int ti = int(e & 2047u);
+      const int ti = int(e & 2047u), x = base + int(e >> 14);
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) tile[v][ti] = q[v];
+      for (int v = 0; v < kNeqMax; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + x);
     }
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   // A2: ghost values beyond domain-boundary sides (deltavalues.c:9-14): the
   // ghost of the brick cell next to it, in both halo layers
