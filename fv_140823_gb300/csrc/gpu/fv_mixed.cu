@@ -1306,17 +1306,15 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
     };
-#pragma unroll 1
-    for (int k = 0; k < 4; ++k) {
-      int ti = ti_own, slot = k * kBlock + t, axis = k;
-      if (k == 3) {
-        if (slot >= kFaces) break;
-        ti = int(__ldg(&g_brick_tasks.task[slot]) & 2047u);
-        axis = slot < kSlotSideY ? 0 : (slot < kSlotSideZ ? 1 : 2);
-      }
-      if (axis == 0)
+    inner(std::integral_constant<int, 1>{}, ti_own, t);
+    inner(std::integral_constant<int, 2>{}, ti_own, kBlock + t);
+    inner(std::integral_constant<int, 5>{}, ti_own, 2 * kBlock + t);
+    const int slot = 3 * kBlock + t;
+    if (slot < kFaces) {
+      const int ti = int(__ldg(&g_brick_tasks.task[slot]) & 2047u);
+      if (slot < kSlotSideY)
         inner(std::integral_constant<int, 1>{}, ti, slot);
-      else if (axis == 1)
+      else if (slot < kSlotSideZ)
         inner(std::integral_constant<int, 2>{}, ti, slot);
       else
         inner(std::integral_constant<int, 5>{}, ti, slot);
