@@ -1289,10 +1289,11 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
   // +y, +z faces (slots t, 256 + t, 512 + t), then threads 0-127 the faces on
   // the brick's lower sides; face index, stride and frame as compile-time
   // constants (the axis is uniform across each warp).
+  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   auto face_tasks_inner = [&]() {
     bool fok = true;
     const int ti_own = int(__ldg(&g_brick_cells.w[2 * t]) & 2047u);
-    auto inner = [&](auto fpc, int ti, int slot) {
+    auto inner = [&](auto fpc, int ti, int slot, bool own) {
       constexpr int FP = decltype(fpc)::value;
       constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : TX * TY);
       float lo[kNeqMax], hi[kNeqMax], Fn[kNeqMax];
@@ -1305,19 +1306,24 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
+      if (own) {  // the cell's own + face: its first residual terms, in order
+        const float sA = -s_geo[FP][0][2];
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];
+      }
     };
-    inner(std::integral_constant<int, 1>{}, ti_own, t);
-    inner(std::integral_constant<int, 2>{}, ti_own, kBlock + t);
-    inner(std::integral_constant<int, 5>{}, ti_own, 2 * kBlock + t);
+    inner(std::integral_constant<int, 1>{}, ti_own, t, true);
+    inner(std::integral_constant<int, 2>{}, ti_own, kBlock + t, true);
+    inner(std::integral_constant<int, 5>{}, ti_own, 2 * kBlock + t, true);
     const int slot = 3 * kBlock + t;
     if (slot < kFaces) {
       const int ti = int(__ldg(&g_brick_tasks.task[slot]) & 2047u);
       if (slot < kSlotSideY)
-        inner(std::integral_constant<int, 1>{}, ti, slot);
+        inner(std::integral_constant<int, 1>{}, ti, slot, false);
       else if (slot < kSlotSideZ)
-        inner(std::integral_constant<int, 2>{}, ti, slot);
+        inner(std::integral_constant<int, 2>{}, ti, slot, false);
       else
-        inner(std::integral_constant<int, 5>{}, ti, slot);
+        inner(std::integral_constant<int, 5>{}, ti, slot, false);
     }
     return fok;
   };
@@ -1327,7 +1333,6 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
   // C: gather in the fixed face order, RK stage update
   const uint32_t cw0 = __ldg(&g_brick_cells.w[2 * t]), cw1 = __ldg(&g_brick_cells.w[2 * t + 1]);
   const uint32_t be = (cw0 >> 11) & 63u & bmask;
-  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const int sx_m = int(cw1 & 1023u), sy_m = int((cw1 >> 10) & 1023u), sz_m = int(cw1 >> 20);
   // order +x, +y, +z, -x, -y, -z as in the general kernel
   auto add_face = [&](int f, int task, bool plus) {
@@ -1336,9 +1341,11 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * flux[v][task];  // as the general kernel
   };
-  add_face(1, t, true);
-  add_face(2, kBlock + t, true);
-  add_face(5, 2 * kBlock + t, true);
+  if (bmask) {  // a brick off the domain boundary added its + faces already
+    add_face(1, t, true);
+    add_face(2, kBlock + t, true);
+    add_face(5, 2 * kBlock + t, true);
+  }
   add_face(3, sx_m, false);
   add_face(0, sy_m, false);
   add_face(4, sz_m, false);
