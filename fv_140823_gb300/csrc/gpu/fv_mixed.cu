@@ -940,6 +940,12 @@ __host__ __device__ constexpr int morton_x(int t) { return (t & 1) | (((t >> 3) 
 __host__ __device__ constexpr int morton_y(int t) { return ((t >> 1) & 1) | (((t >> 4) & 1) << 1) | (((t >> 7) & 1) << 2); }
 __host__ __device__ constexpr int morton_z(int t) { return ((t >> 2) & 1) | (((t >> 5) & 1) << 1); }
 constexpr int kSlotSideX = 3 * kBlock, kSlotSideY = kSlotSideX + BY * BZ, kSlotSideZ = kSlotSideY + BX * BZ;
+// faces on the brick's -z side: even rows y first, then odd ones, so that
+// each warp's lower cells fall in 32 different banks of the tile
+__host__ __device__ constexpr int brick_zslot(int x, int y) { return (y & 1) * (BX * BY / 2) + (y >> 1) * BX + x; }
+__host__ __device__ constexpr int brick_zslot_y(int r) {
+  return r < BX * BY / 2 ? 2 * (r / BX) : 2 * ((r - BX * BY / 2) / BX) + 1;
+}
 constexpr BrickTasks make_brick_tasks() {
   BrickTasks T{};
   for (int task = 0; task < kFaces; ++task) {
@@ -965,7 +971,7 @@ constexpr BrickTasks make_brick_tasks() {
       const int r = task - kSlotSideZ;
       axis = 2;
       lx = r % BX;
-      ly = r / BX;
+      ly = brick_zslot_y(r);
       lz = -1;
     }
     const int ux = lx + (axis == 0), uy = ly + (axis == 1), uz = lz + (axis == 2);
@@ -1003,41 +1009,43 @@ constexpr BrickTaskCells make_brick_task_cells() {
 }
 __device__ const BrickTaskCells g_brick_task_cells = make_brick_task_cells();
 
-// Halo cells of a brick, two layers beyond each side: x sides, then y, then
-// z.  Packed: tile index (11 bits), brick side the cell lies beyond (3),
-// Morton offset of the cell within its own brick (8).
+// Halo cells of a brick, two layers beyond each side: the x sides (128
+// cells), the y sides (128), the z sides (256).  Within each group the cells
+// are dealt out so that the 32 of every warp fall in 32 different
+// shared-memory banks of the tile (each bank holds exactly 4, 4 and 8 cells
+// of the three groups).  Packed: tile index (11 bits), brick side the cell
+// lies beyond (3), Morton offset of the cell within its own brick (8).
 struct BrickHalo {
   uint32_t h[kHalo];
 };
 constexpr BrickHalo make_brick_halo() {
   BrickHalo H{};
-  for (int h = 0; h < kHalo; ++h) {
-    int hx = 0, hy = 0, hz = 0, side = 0, lx = 0, ly = 0, lz = 0;
-    if (h < 4 * BY * BZ) {
-      const int s = h / (2 * BY * BZ), r = h % (2 * BY * BZ), layer = 1 + r / (BY * BZ), rr = r % (BY * BZ);
-      hy = ly = rr % BY;
-      hz = lz = rr / BY;
-      side = s == 0 ? 3 : 1;
-      hx = s == 0 ? -layer : BX - 1 + layer;
-      lx = s == 0 ? BX - layer : layer - 1;
-    } else if (h < 4 * BY * BZ + 4 * BX * BZ) {
-      const int hh = h - 4 * BY * BZ;
-      const int s = hh / (2 * BX * BZ), r = hh % (2 * BX * BZ), layer = 1 + r / (BX * BZ), rr = r % (BX * BZ);
-      hx = lx = rr % BX;
-      hz = lz = rr / BX;
-      side = s == 0 ? 0 : 2;
-      hy = s == 0 ? -layer : BY - 1 + layer;
-      ly = s == 0 ? BY - layer : layer - 1;
-    } else {
-      const int hh = h - 4 * BY * BZ - 4 * BX * BZ;
-      const int s = hh / (2 * BX * BY), r = hh % (2 * BX * BY), layer = 1 + r / (BX * BY), rr = r % (BX * BY);
-      hx = lx = rr % BX;
-      hy = ly = rr / BX;
-      side = s == 0 ? 4 : 5;
-      hz = s == 0 ? -layer : BZ - 1 + layer;
-      lz = s == 0 ? BZ - layer : layer - 1;
+  int base = 0;
+  for (int g = 0; g < 3; ++g) {
+    int placed[32] = {};
+    const int na = g == 0 ? BY : BX, nb = g == 2 ? BY : BZ;  // extents of the two in-plane axes
+    const int ext = g == 0 ? BX : (g == 1 ? BY : BZ);       // brick extent along the group's axis
+    for (int layer = 0; layer < 4; ++layer) {              // -2, -1, ext, ext + 1
+      const int o = layer < 2 ? layer - 2 : ext + layer - 2;
+      const int side = g == 0 ? (o < 0 ? 3 : 1) : (g == 1 ? (o < 0 ? 0 : 2) : (o < 0 ? 4 : 5));
+      const int lo = o < 0 ? o + ext : o - ext;  // coordinate within the neighbour brick
+      for (int b = 0; b < nb; ++b)
+        for (int a2 = 0; a2 < na; ++a2) {
+          int hx = a2, hy = b, hz = 0, lx = a2, ly = b, lz = 0;
+          if (g == 0) {
+            hx = o; lx = lo; hy = ly = a2; hz = lz = b;
+          } else if (g == 1) {
+            hy = o; ly = lo; hx = lx = a2; hz = lz = b;
+          } else {
+            hz = o; lz = lo; hx = lx = a2; hy = ly = b;
+          }
+          const int ti = tile_index(hx, hy, hz), bank = ti % 32;
+          H.h[base + 32 * placed[bank] + bank] =
+              uint32_t(ti) | (uint32_t(side) << 11) | (uint32_t(morton_local(lx, ly, lz)) << 14);
+          ++placed[bank];
+        }
     }
-    H.h[h] = uint32_t(tile_index(hx, hy, hz)) | (uint32_t(side) << 11) | (uint32_t(morton_local(lx, ly, lz)) << 14);
+    base += 4 * na * nb;
   }
   return H;
 }
@@ -1055,7 +1063,7 @@ constexpr BrickCells make_brick_cells() {
     const int x = morton_x(t), y = morton_y(t), z = morton_z(t);
     const int mx = x > 0 ? morton_local(x - 1, y, z) : kSlotSideX + y + BY * z;
     const int my = y > 0 ? kBlock + morton_local(x, y - 1, z) : kSlotSideY + x + BX * z;
-    const int mz = z > 0 ? 2 * kBlock + morton_local(x, y, z - 1) : kSlotSideZ + x + BX * y;
+    const int mz = z > 0 ? 2 * kBlock + morton_local(x, y, z - 1) : kSlotSideZ + brick_zslot(x, y);
     C.w[2 * t] = uint32_t(tile_index(x, y, z)) | (edge_mask(x, y, z) << 11);
     C.w[2 * t + 1] = uint32_t(mx) | (uint32_t(my) << 10) | (uint32_t(mz) << 20);
   }
