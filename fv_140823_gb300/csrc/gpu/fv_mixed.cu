@@ -1103,7 +1103,6 @@ __global__ void __launch_bounds__(kBlock, NS ? 4 : FV_BRICK_MIN_BLOCKS) k_mixed_
   const BlockDesc *bdp = a.blocks + blockIdx.x;
   const int t = threadIdx.x;
   const int n = a.n;
-  constexpr int neq = kNeqMax;  // models 1 and 3: five conservative variables
   constexpr bool muscl = MUSCL;
   const int start = __ldg(&bdp->start), level = __ldg(&bdp->level);
   const int c = start + t;
@@ -1468,9 +1467,9 @@ bool brick_interior(const fvgpu_mesh_soa *m, int64_t i) {
   return true;
 }
 
-// side f of brick i: the first cell of a same-level brick that supplies all
-// its neighbours, -1-bc for a uniform domain boundary, or INT_MIN
-int brick_side(const fvgpu_mesh_soa *m, int64_t i, int f, const std::vector<char> &is_brick) {
+// side f of brick i: the first cell of a same-level Morton block that
+// supplies all its neighbours, -1-bc for a uniform domain boundary, or INT_MIN
+int brick_side(const fvgpu_mesh_soa *m, int64_t i, int f, const std::vector<char> &is_block) {
   const int64_t n = m->ncells;
   int result = 0;
   bool first = true;
@@ -1486,7 +1485,7 @@ int brick_side(const fvgpu_mesh_soa *m, int64_t i, int f, const std::vector<char
     } else if (code >= 0) {
       const int wx = (nx + BX) % BX, wy = (ny + BY) % BY, wz = (nz + BZ) % BZ;
       const int64_t base = int64_t(code) - host_morton_local(wx, wy, wz);
-      if (base < 0 || base + kBlock > n || !is_brick[size_t(base)]) return INT32_MIN;
+      if (base < 0 || base + kBlock > n || !is_block[size_t(base)]) return INT32_MIN;
       if (m->level[code] != m->level[i]) return INT32_MIN;
       value = int(base);
     } else {
@@ -1613,14 +1612,16 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     }
     geom[size_t(c)] = code;
   }
-  // bricks: candidate starts, then keep those whose six sides resolve
-  std::vector<char> is_brick(size_t(n), 0);
+  // bricks: same-level Morton blocks (candidates), kept when each of their
+  // six sides is a domain boundary or another candidate block, whichever
+  // kernel evaluates that block (its cells only supply the 2-deep halo)
+  std::vector<char> is_block(size_t(n), 0), is_brick(size_t(n), 0);
   // bricks for every inviscid run and for viscous runs of model 1 (both
   // kernels read the cells' gradients straight from the gradient pass)
   if (!r.force_general && (ph.ns != 1 || ph.model == 1)) {
     for (int64_t i = 0; i + kBlock <= n;) {
       if (brick_interior(m, i)) {
-        is_brick[size_t(i)] = 1;
+        is_block[size_t(i)] = 1;
         i += kBlock;
       } else {
         ++i;
@@ -1628,18 +1629,11 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     }
   }
   std::vector<BlockDesc> bricks, general;
-  for (bool changed = true; changed;) {
-    changed = false;
-    for (int64_t i = 0; i < n; ++i) {
-      if (!is_brick[size_t(i)]) continue;
-      for (int f = 0; f < 6; ++f) {
-        if (brick_side(m, i, f, is_brick) == INT32_MIN) {
-          is_brick[size_t(i)] = 0;
-          changed = true;
-          break;
-        }
-      }
-    }
+  for (int64_t i = 0; i < n; ++i) {
+    if (!is_block[size_t(i)]) continue;
+    bool sides = true;
+    for (int f = 0; f < 6 && sides; ++f) sides = brick_side(m, i, f, is_block) != INT32_MIN;
+    is_brick[size_t(i)] = sides ? 1 : 0;
   }
   for (int64_t i = 0; i < n;) {
     if (is_brick[size_t(i)]) {
@@ -1648,7 +1642,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       d.start = int(i);
       d.count = kBlock;
       d.level = m->level[i];
-      for (int f = 0; f < 6; ++f) d.side[f] = brick_side(m, i, f, is_brick);
+      for (int f = 0; f < 6; ++f) d.side[f] = brick_side(m, i, f, is_block);
       bricks.push_back(d);
       i += kBlock;
       continue;
@@ -1688,6 +1682,14 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   r.n = n;
   r.nbricks = int64_t(bricks.size());
   r.ngeneral = int64_t(general.size());
+  if (r.nbricks > 0 && r.ngeneral > 0 && !r.side) {
+    if (cudaStreamCreateWithFlags(&r.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&r.fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&r.join_ev, cudaEventDisableTiming) != cudaSuccess) {
+      snprintf(why, whylen, "stream / event creation failed");
+      return FVGPU_ERR_CUDA;
+    }
+  }
   r.ready = true;
   return FVGPU_OK;
 }
@@ -1698,6 +1700,11 @@ void release_mixed(MixedResources &r) {
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
   }
+  if (r.side) cudaStreamDestroy(r.side);
+  if (r.fork_ev) cudaEventDestroy(r.fork_ev);
+  if (r.join_ev) cudaEventDestroy(r.join_ev);
+  r.side = nullptr;
+  r.fork_ev = r.join_ev = nullptr;
   r.ready = false;
   r.snf_valid = false;
   r.nbricks = r.ngeneral = 0;
@@ -1799,18 +1806,30 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
-    if (r.nbricks > 0) {
-      a.blocks = blocks;
-      marks.mark(FVGPU_KIND_MIXED_STAGE);
-      launch_kernel(ph, true, unsigned(r.nbricks), mc, a, st);
-      cudaError_t e = cudaGetLastError();
+    // bricks and general blocks write disjoint cells: with both present the
+    // general blocks run on the side stream, concurrently
+    const bool fork = r.nbricks > 0 && r.ngeneral > 0 && r.side;
+    marks.mark(FVGPU_KIND_MIXED_STAGE);
+    if (fork) {
+      cudaError_t e = cudaEventRecord(r.fork_ev, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(r.side, r.fork_ev, 0);
       if (e != cudaSuccess) return e;
     }
     if (r.ngeneral > 0) {
       a.blocks = blocks + r.nbricks;
-      marks.mark(FVGPU_KIND_MIXED_STAGE);
-      launch_kernel(ph, false, unsigned(r.ngeneral), mc, a, st);
+      launch_kernel(ph, false, unsigned(r.ngeneral), mc, a, fork ? r.side : st);
       cudaError_t e = cudaGetLastError();
+      if (e == cudaSuccess && fork) e = cudaEventRecord(r.join_ev, r.side);
+      if (e != cudaSuccess) return e;
+    }
+    if (r.nbricks > 0) {
+      a.blocks = blocks;
+      launch_kernel(ph, true, unsigned(r.nbricks), mc, a, st);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (fork) {
+      const cudaError_t e = cudaStreamWaitEvent(st, r.join_ev, 0);
       if (e != cudaSuccess) return e;
     }
   }

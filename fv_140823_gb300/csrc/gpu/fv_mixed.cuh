@@ -21,6 +21,10 @@ struct MixedResources {
   int64_t nbricks = 0;     // brick blocks (structured fast path)
   int64_t ngeneral = 0;    // general blocks
   bool force_general = false;  // FVGPU_FLAG_NO_BRICKS
+  // a stage with both kinds of block runs the general blocks on a second
+  // stream, forked from and joined back into the caller's stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   bool ready = false;
   bool snf_valid = false;  // FP32 copy of the current state is up to date
 };
