@@ -85,7 +85,9 @@ typedef struct fvgpu_config {
   int model;       /* 1 ideal/stiffened gas, 2 barotropic liquid, 3 two-phase mixture */
   int ns;          /* 1 = viscous (Navier-Stokes) fluxes */
   int ischeme;     /* 1 first order, 2 MUSCL / minmod */
-  int iprimtv;     /* must be 0: see DESIGN notes on cons2primtv */
+  int iprimtv;     /* must be 0: MUSCL on the conservative variables
+                      (reconctruct_V3.c, iprimtv == 0); the primitive-variable
+                      branch is not provided */
   int eos;         /* 1 = viscous work term in the energy flux (flux_viscous.c:227) */
   int precision;   /* FVGPU_FP64 or FVGPU_MIXED */
   int device;      /* CUDA device ordinal */
