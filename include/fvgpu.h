@@ -28,7 +28,10 @@
  *   - host buffers are caller-owned; device buffers belong to the context;
  *   - state arrays are structure-of-arrays, U[v * ld + c] for variable v of
  *     cell c (ld >= ncells);
- *   - one context per host thread; each context owns one CUDA stream.
+ *   - one context per host thread; each context owns one CUDA stream.  On
+ *     an AMR mesh a mixed-precision stage forks part of its work to a second
+ *     internal stream and joins it back before the stage ends, so every call
+ *     is still ordered on (and capturable from) the context's stream.
  */
 #ifndef FVGPU_H
 #define FVGPU_H
