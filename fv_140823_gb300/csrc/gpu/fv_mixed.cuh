@@ -18,13 +18,15 @@ struct MixedResources {
   void *buf[11] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t bytes[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   int64_t n = 0;
-  int64_t nbricks = 0;     // brick blocks (structured fast path)
+  int64_t nbricks = 0;     // 8x8x4 brick blocks (structured fast path)
+  int64_t nbricks4 = 0;    // 4x4x4 brick blocks
   int64_t ngeneral = 0;    // general blocks
   bool force_general = false;  // FVGPU_FLAG_NO_BRICKS
-  // a stage with both kinds of block runs the general blocks on a second
-  // stream, forked from and joined back into the caller's stream
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // a stage with more than one kind of block runs the 4x4x4 bricks and the
+  // general blocks on two more streams, forked from and joined back into the
+  // caller's stream
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr};
   bool ready = false;
   bool snf_valid = false;  // FP32 copy of the current state is up to date
 };
