@@ -30,13 +30,14 @@
 // and out of a face frame is a choice of registers.
 //
 // Two kernels share that definition:
-//   k_mixed_brick    a Morton-aligned 8x8x4 brick of same-level cells whose
-//                    six sides are same-level bricks or domain boundaries:
-//                    brick + 2-deep face halo staged in shared memory through
-//                    constant index tables, the 896 faces of the brick
-//                    evaluated once each (a brick off the domain boundary:
-//                    each thread its cell's +x, +y, +z faces, then threads
-//                    0-127 the faces on the brick's lower sides), no
+//   k_mixed_brick    a Morton-aligned 8x8x4 (or, on AMR meshes, 4x4x4)
+//                    brick of same-level cells whose six sides are same-level
+//                    blocks of that shape or domain boundaries: brick +
+//                    2-deep face halo staged in shared memory through
+//                    constant index tables, every face of the brick
+//                    evaluated once (a brick off the domain boundary: each
+//                    thread its cell's +x, +y, +z faces, then the first
+//                    threads the faces on the brick's lower sides), no
 //                    neighbour tables read; viscous runs (model 1) read the
 //                    two cells' gradients of each face;
 //   k_mixed_general  any other run of up to 256 consecutive cells (AMR
@@ -1279,7 +1280,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   };
 
   // B: face tasks -- each face of the brick once
-  // viscous runs: the global index of a face task's cell (brick_cell_ref)
+  // viscous runs: the global index of a face task's cell (S::cell_ref)
   // and the viscous normal flux of a face, subtracted as the general kernel
   // does: (F - FV).n + FH
   auto cell_of = [&](uint32_t r) -> int {
@@ -1342,7 +1343,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     return fok;
   };
   // The same for a brick off the domain boundary: each thread its cell's +x,
-  // +y, +z faces (slots t, 256 + t, 512 + t), then threads 0-127 the faces on
+  // +y, +z faces (slots t, N + t, 2N + t), then the first threads the faces on
   // the brick's lower sides; face index, stride and frame as compile-time
   // constants (the axis is uniform across each warp).
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
