@@ -1345,7 +1345,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   // The same for a brick off the domain boundary: each thread its cell's +x,
   // +y, +z faces (slots t, N + t, 2N + t), then the first threads the faces on
   // the brick's lower sides; face index, stride and frame as compile-time
-  // constants (the axis is uniform across each warp).
+  // constants (the axis is uniform across each warp of an 8x8x4 brick).
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   auto face_tasks_inner = [&]() {
     bool fok = true;
