@@ -144,10 +144,31 @@ struct FS {
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
 
+// Density in the FP32 state vectors.  Model 3 (liquid-gas mixture) stores
+// rho - kRhoOff, kRhoOff the saturation density of the mixture EOS
+// (barotropic_eos.c:41, as an FP32 value): near the liquid density an FP32
+// ulp of rho itself is 6e-5, which the stiff liquid branch of the EOS turns
+// into ~130 Pa of pressure; the offset value keeps the liquid density to
+// ~1e-8 for the FP64 pressure inversion (the gas density, ~1, then carries
+// the 6e-5, worth ~5 Pa).  Differences between cells, and so the
+// reconstruction, are unchanged; model 1 stores rho.
+constexpr float kRhoOffF = 998.1618f;
+constexpr double kRhoOffD = double(kRhoOffF);
+template <int MODEL>
+__device__ __forceinline__ float state_rho(float q0) { return MODEL == 3 ? q0 + kRhoOffF : q0; }
+template <int MODEL>
+__device__ __forceinline__ double state_rho_d(float q0) { return MODEL == 3 ? double(q0) + kRhoOffD : double(q0); }
+__device__ __forceinline__ float state_rho_rt(int model, float q0) { return model == 3 ? q0 + kRhoOffF : q0; }
+// the FP32 state value of variable v from the FP64 state value
+template <int MODEL>
+__device__ __forceinline__ float to_state_f32(int v, double x) {
+  return __double2float_rn(MODEL == 3 && v == 0 ? x - kRhoOffD : x);
+}
+
 // FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
 template <int MODEL>
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
-  s.r = q[0];
+  s.r = state_rho<MODEL>(q[0]);
   const float rinv = fast_rcp(s.r);
   s.u = q[1] * rinv;
   s.v = q[2] * rinv;
@@ -170,7 +191,7 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
     s.y = s.y > mc.yhi ? mc.yhi : s.y;
   }
   double p, c;
-  const bool ok = eos_mixture(double(s.r), double(s.y), p, c);
+  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
   s.p = float(p);
   s.c = float(c);
   s.e = 0.0f;
@@ -313,7 +334,7 @@ __device__ __forceinline__ void frame_out(int f, float a, float b, float c, floa
 
 template <int MODEL, int F = -1>
 __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float q[kNeqMax], bool clip, LS &s) {
-  s.r = q[0];
+  s.r = state_rho<MODEL>(q[0]);
   s.q4 = q[4];
   frame_in<F>(f, q, s.mn, s.mm, s.ml);
   const float rinv = fast_rcp(s.r);
@@ -336,7 +357,7 @@ __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const f
     s.y = s.y > mc.yhi ? mc.yhi : s.y;
   }
   double p, c;
-  const bool ok = eos_mixture(double(s.r), double(s.y), p, c);
+  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
   s.p = float(p);
   s.c = float(c);
   return ok;
@@ -535,7 +556,7 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     for (int v = 0; v < kNeqMax; ++v) {
       const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
       a.SNout[v * n + c] = snew;
-      qn[v] = __double2float_rn(snew);
+      qn[v] = to_state_f32<MODEL>(v, snew);
       a.SNfout[v * n + c] = qn[v];
     }
     return true;
@@ -568,7 +589,7 @@ __device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int
     u[2] = mc.inflow[3] * rinv;
     return;
   }
-  const float rinv = fast_rcp(q[0]);
+  const float rinv = fast_rcp(state_rho_rt(mc.model, q[0]));
   u[0] = q[1] * rinv;
   u[1] = q[2] * rinv;
   u[2] = q[3] * rinv;
@@ -593,7 +614,7 @@ __device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int 
                                                float FVn[kNeqMax]) {
   float ul[3], uh[3];
   {
-    const float rinv = fast_rcp(lo[0]);
+    const float rinv = fast_rcp(state_rho_rt(mc.model, lo[0]));
     ul[0] = lo[1] * rinv;
     ul[1] = lo[2] * rinv;
     ul[2] = lo[3] * rinv;
@@ -601,7 +622,7 @@ __device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int 
   if (bc > 0) {
     ghost_velocity(mc, bc, f, lo, uh);
   } else {
-    const float rinv = fast_rcp(hi[0]);
+    const float rinv = fast_rcp(state_rho_rt(mc.model, hi[0]));
     uh[0] = hi[1] * rinv;
     uh[1] = hi[2] * rinv;
     uh[2] = hi[3] * rinv;
@@ -671,9 +692,10 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
       } else {
         float u[3];
         ghost_velocity(mc, bc, f, q, u);
-        m[0] = q[0] * u[0];
-        m[1] = q[0] * u[1];
-        m[2] = q[0] * u[2];
+        const float rho = state_rho<MODEL>(q[0]);
+        m[0] = rho * u[0];
+        m[1] = rho * u[1];
+        m[2] = rho * u[2];
         if (bc != 3 && bc != 4) {
           m[0] = q[1];
           m[1] = q[2];
@@ -1413,9 +1435,11 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
 }
 
 // FP32 copy of an FP64 state (after an upload or an FP64-path step).
-__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count) {
+// The first n values (the density) are shifted by off (model 3: kRhoOffD).
+__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count, int64_t n,
+                               double off) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-    Sf[i] = __double2float_rn(S[i]);
+    Sf[i] = __double2float_rn(i < n ? S[i] - off : S[i]);
 }
 
 // The same with the CFL spectral radius of the copied state (the mixed
@@ -1430,7 +1454,7 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
       if (v >= mc.neq) break;
-      q[v] = __double2float_rn(S[int64_t(v) * n + c]);
+      q[v] = to_state_f32<MODEL>(v, S[int64_t(v) * n + c]);
       Sf[int64_t(v) * n + c] = q[v];
     }
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
@@ -1769,6 +1793,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
   }
   r.n = n;
+  r.model = ph.model;
   r.nbricks = int64_t(bricks.size());
   r.nbricks4 = int64_t(bricks4.size());
   r.ngeneral = int64_t(general.size());
@@ -1821,7 +1846,8 @@ void mixed_swap_state(MixedResources &r, void *&state) {
 
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
   marks.mark(FVGPU_KIND_MIXED_AUX);
-  k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n);
+  k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n, r.n,
+                                       r.model == 3 ? kRhoOffD : 0.0);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;

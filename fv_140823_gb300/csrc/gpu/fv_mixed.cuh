@@ -18,6 +18,7 @@ struct MixedResources {
   void *buf[11] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t bytes[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   int64_t n = 0;
+  int model = 1;           // EOS model the FP32 state layout follows (model 3: density offset)
   int64_t nbricks = 0;     // 8x8x4 brick blocks (structured fast path)
   int64_t nbricks4 = 0;    // 4x4x4 brick blocks
   int64_t ngeneral = 0;    // general blocks
