@@ -76,6 +76,18 @@ def test_mixture_bubble_model3():
     assert np.all(err[1:4] <= 5e-5), err
 
 
+def test_mixture_bubble_model3_viscous():
+    """Model 3 with viscous fluxes: velocities (face fluxes, ghosts and the
+    Green-Gauss gradients) divide by the density recovered from the FP32
+    state's rho - rho_sat."""
+    c = cases.bubble(base_level=3, extra_levels=2)
+    cfg = SolverConfig(**{**c.cfg.__dict__, "ns": 1, "eos": 0, "visc": 1e-3})
+    c = cases.Case("bubble_viscous", c.tables, c.U, cfg, cfl=0.5, nsteps=5)
+    dt = 2e-7
+    err = rel_l2(run(c, abi.MIXED, 5, dt), run(c, abi.FP64, 5, dt))
+    assert err[0] <= 1e-5 and err[4] <= 1e-5 and np.all(err[1:4] <= 5e-5), err
+
+
 @pytest.mark.parametrize("bc", [2, 3, 4])
 def test_smooth_flow_next_to_domain_boundaries_within_1e6(bc):
     """A cell next to a domain boundary limits its slope on that axis as the
