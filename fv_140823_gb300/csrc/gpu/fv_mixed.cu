@@ -18,36 +18,54 @@
 // their FP32 rounding is ~1e-8 of the state per stage, and every add into
 // the state is FP64.
 //
+// Reconstruction.  minmod-limited MUSCL on the conservative variables
+// (reconctruct_V3.c:17-43).  Where both faces of a cell on an axis have a
+// same-level neighbour, the limited slope is one number per cell, axis and
+// variable, s = minmod(q+ - q, q - q-) (the median of the two differences and
+// zero), and the two face values are q +- k s with k = dist_cf / dist_cc of
+// the level: the reference's slopes toward the two faces differ only through
+// its dead band |d| > 1e-10, which this path drops (it moves a face value by
+// at most k 1e-10).  Every other axis (a 1:4 face, a coarser neighbour, a
+// domain boundary) keeps the reference's per-face form with the dead band.
+//
 // Canonical face fluxes.  Every face flux is defined from the face's lower
-// cell (the one whose +x/+y/+z face it is), with that face's frame; the
-// lower cell's residual gets -A F and the upper cell's +A F.  Whoever
+// cell (the one whose +x/+y/+z face it is), with that face's frame.  Whoever
 // evaluates a face gets the same bits (this translation unit is compiled
 // without automatic multiply-add contraction, explicit fmaf only), so the
-// scheme is conservative and deterministic however the work is split.
+// scheme is conservative and deterministic however the work is split.  A
+// cell's residual is summed axis by axis, x, y, z: R += A (F- - F+) where
+// neither face of the axis is a 1:4 face (a uniform flow cancels exactly),
+// R += (T- - T+) with T the area-weighted sum over the sub-faces otherwise.
 //
 // Face frames are those of the reference's hexahedral cells (checked at
 // upload), compiled in as signed permutations: rotating the momentum into
 // and out of a face frame is a choice of registers.
 //
-// Two kernels share that definition:
+// Two kernels share those definitions:
 //   k_mixed_brick    a Morton-aligned 8x8x4 (or, on AMR meshes, 4x4x4)
 //                    brick of same-level cells whose six sides are same-level
 //                    blocks of that shape or domain boundaries: brick +
 //                    2-deep face halo staged in shared memory through
-//                    constant index tables, every face of the brick
-//                    evaluated once (a brick off the domain boundary: each
-//                    thread its cell's +x, +y, +z faces, then the first
-//                    threads the faces on the brick's lower sides), no
-//                    neighbour tables read; viscous runs (model 1) read the
-//                    two cells' gradients of each face;
+//                    constant index tables; each cell forms its six face
+//                    values once (one slope per axis), the halo cells next to
+//                    the brick the one face value the brick needs; each
+//                    thread then evaluates its cell's +x, +y, +z faces and the
+//                    first threads the faces on the brick's lower sides; no
+//                    neighbour tables are read; viscous runs (model 1) read
+//                    the two cells' gradients of each face;
 //   k_mixed_general  any other run of up to 256 consecutive cells (AMR
 //                    interfaces, 1:4 faces): table-driven, each thread
 //                    computes its + faces and publishes them, the upper cell
 //                    reuses them or recomputes the canonical flux across
 //                    block edges and 1:4 sub-faces.
-// A cell's residual is accumulated in the same face order with the same
-// operations in both kernels, so its result does not depend on which kernel
-// handled it (tests compare the two bit for bit).
+// A cell's result does not depend on which kernel handled it (tests compare
+// the two bit for bit).  Both keep their large shared arrays in dynamic
+// shared memory, opted in per kernel above the 48 KiB default.
+//
+// Model 3 (two-phase mixture) keeps the density as two FP32 words, rho -
+// rho_sat and its rounding remainder: differences between cells, face
+// values and the FP64 pressure inversion see the density to ~1e-14 of the
+// liquid value, while the FP32 flux arithmetic uses its FP32 rounding.
 //
 // Geometry comes from per-level tables (octree-regular meshes): a packed
 // per-cell code (level + face relations) replaces the FP64 face tables.
@@ -68,11 +86,12 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kMaxLevel = 18;
 constexpr int kRelSame = 0, kRelFiner = 1, kRelCoarser = 2, kRelBoundary = 3;
-constexpr int kGeoStride = 4;  // per (level, face, relation): dcf, 1/dcc, area, pad
+constexpr int kGeoStride = 4;  // per (level, face, relation): dcf, 1/dcc, area, k = dcf/dcc
 constexpr int kGeoEntries = (kMaxLevel + 1) * 6 * 4;
 
 struct GeoTables {
   float face[kGeoEntries * kGeoStride];
+  float axis_area[(kMaxLevel + 1) * 3];  // area of a single-neighbour face normal to the axis
   float sub_area[(kMaxLevel + 1) * 6];
   float vol[kMaxLevel + 1];
   float inv_vol[kMaxLevel + 1];
@@ -80,12 +99,19 @@ struct GeoTables {
 };
 
 __host__ __device__ constexpr int geo_index(int level, int f, int rel) { return ((level * 6 + f) * 4 + rel); }
-// + faces: normals +x (1), +y (2), +z (5); their slot in the flux table
-__device__ __forceinline__ int plus_slot(int f) { return f == 1 ? 0 : (f == 2 ? 1 : 2); }
-// residual accumulation order (both kernels): +x, +y, +z, -x, -y, -z
-__device__ __forceinline__ int face_of_iter(int it) {
-  return it == 0 ? 1 : it == 1 ? 2 : it == 2 ? 5 : it == 3 ? 3 : it == 4 ? 0 : 4;
-}
+// faces of an axis: + faces +x (1), +y (2), +z (5); - faces -x (3), -y (0), -z (4)
+__host__ __device__ constexpr int plus_face(int a) { return a == 0 ? 1 : (a == 1 ? 2 : 5); }
+__host__ __device__ constexpr int minus_face(int a) { return a == 0 ? 3 : (a == 1 ? 0 : 4); }
+__host__ __device__ constexpr int axis_of_face(int f) { return (f == 1 || f == 3) ? 0 : ((f == 0 || f == 2) ? 1 : 2); }
+
+// Number of FP32 words of the state vector: model 3 adds the low words of
+// the density and of the gas partial density (rows 5 and 6).
+template <int MODEL>
+constexpr int kNv = MODEL == 3 ? 7 : 5;
+constexpr int kNvMax = 7;
+// the low word of variable v (model 3: density -> 5, rho Y -> 6), else -1
+template <int MODEL>
+__host__ __device__ constexpr int lo_word(int v) { return MODEL == 3 ? (v == 0 ? 5 : (v == 4 ? 6 : -1)) : -1; }
 
 // FP32 constants, converted once on the host.
 struct MixedConst {
@@ -94,7 +120,7 @@ struct MixedConst {
   float ylo, yhi;  // mass-fraction clip (facercnstr.c:43-44)
   float visc;      // dynamic viscosity (flux_viscous.c, turb = 0)
   int ns, eos;     // viscous fluxes on; energy work term on
-  float inflow[kNeqMax];
+  float inflow[kNvMax];  // conservative inflow ghost in FP32 state form
   int model, neq, ischeme, pad;
 };
 
@@ -114,15 +140,15 @@ struct StageArgs {
   const int32_t *hang_nbr;  // [nhang][4]
   const GeoTables *geo;
   const BlockDesc *blocks;
-  const float *SNf;         // [neq][n] FP32 copy of the step-start state
-  const float *Sin;         // [neq][n] FP32 stage-input state SNf + Din (SNf at the first stage)
-  const float *Din;         // [neq][n] stage-input increment (null: zero)
-  float *Dout;              // [neq][n]
-  float *Sout;              // [neq][n] non-last stages: the next stage's input SNf + Dout
+  const float *SNf;         // [nv][n] FP32 copy of the step-start state
+  const float *Sin;         // [nv][n] FP32 stage-input state SNf + Din (SNf at the first stage)
+  const float *Din;         // [5][n] stage-input increment (null: zero)
+  float *Dout;              // [5][n]
+  float *Sout;              // [nv][n] non-last stages: the next stage's input SNf + Dout
   const float *SG;          // [9][n] viscous runs: momentum gradients of Sin (ux uy uz vx ... wz)
   const double *SN;         // [neq][n] step-start state (last stage)
   double *SNout;            // [neq][n] last stage: SN + D
-  float *SNfout;            // [neq][n] last stage: FP32 copy of SNout
+  float *SNfout;            // [nv][n] last stage: FP32 copy of SNout
   const double *dt;
   double *lambda;           // last stage: CFL radius of the new state
   int irk;
@@ -136,120 +162,179 @@ __device__ __forceinline__ const float *geo_face(const GeoTables *G, int level, 
   return G->face + geo_index(level, f, rel) * kGeoStride;
 }
 
-struct FS {
-  float r, u, v, w, e, p, c, y;
-  float q[kNeqMax];
-};
-
-__device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
+// Hardware approximations (one special-function instruction each): relative
+// error ~2^-22, far below the FP32 rounding the rest of the flux carries.
+__device__ __forceinline__ float fast_rcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float fast_sqrt(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// rounding error of s = a + b (Knuth's two-sum, exact in round-to-nearest)
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  const float bb = s - a;
+  return (a - (s - bb)) + (b - bb);
+}
 
 // Density in the FP32 state vectors.  Model 3 (liquid-gas mixture) stores
-// rho - kRhoOff, kRhoOff the saturation density of the mixture EOS
-// (barotropic_eos.c:41, as an FP32 value): near the liquid density an FP32
-// ulp of rho itself is 6e-5, which the stiff liquid branch of the EOS turns
-// into ~130 Pa of pressure; the offset value keeps the liquid density to
-// ~1e-8 for the FP64 pressure inversion (the gas density, ~1, then carries
-// the 6e-5, worth ~5 Pa).  Differences between cells, and so the
-// reconstruction, are unchanged; model 1 stores rho.
+// rho - kRhoOff in word 0 and the remainder rho - kRhoOff - word0 in word 5,
+// kRhoOff the saturation density of the mixture EOS (barotropic_eos.c:41, as
+// an FP32 value): near the liquid density an FP32 ulp of rho itself is 6e-5,
+// which the stiff liquid branch turns into ~130 Pa, and the gas density (~1)
+// stored as rho - kRhoOff carries the ulp of ~1000 (~5 Pa of gas pressure);
+// the two words together hold rho to ~1e-14 of 1000.  The gas partial
+// density rho Y gets a low word too (word 4 + word 6): a bubbly liquid's
+// pressure moves by ~3e7 Pa per kg/m^3 of rho Y, so an FP32 rounding of rho
+// Y ~ 3e-3 alone is worth ~0.006 Pa.  Model 1 stores its five variables.
 constexpr float kRhoOffF = 998.1618f;
 constexpr double kRhoOffD = double(kRhoOffF);
 template <int MODEL>
-__device__ __forceinline__ float state_rho(float q0) { return MODEL == 3 ? q0 + kRhoOffF : q0; }
+__device__ __forceinline__ float state_rho(const float *q) { return MODEL == 3 ? q[0] + kRhoOffF : q[0]; }
+// the density as FP64: model 3 from both words (exact sum of the three terms)
 template <int MODEL>
-__device__ __forceinline__ double state_rho_d(float q0) { return MODEL == 3 ? double(q0) + kRhoOffD : double(q0); }
+__device__ __forceinline__ double state_rho_d(const float *q) {
+  if constexpr (MODEL == 3) return (kRhoOffD + double(q[0])) + double(q[5]);
+  return double(q[0]);
+}
 __device__ __forceinline__ float state_rho_rt(int model, float q0) { return model == 3 ? q0 + kRhoOffF : q0; }
-// the FP32 state value of variable v from the FP64 state value
+// FP32 state words of an FP64 state: v < 5 variable v (density shifted for
+// model 3); model 3 word 5 = rounding remainder of word 0, else 0
 template <int MODEL>
-__device__ __forceinline__ float to_state_f32(int v, double x) {
-  return __double2float_rn(MODEL == 3 && v == 0 ? x - kRhoOffD : x);
-}
-
-// FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
-template <int MODEL>
-__device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
-  s.r = state_rho<MODEL>(q[0]);
-  const float rinv = fast_rcp(s.r);
-  s.u = q[1] * rinv;
-  s.v = q[2] * rinv;
-  s.w = q[3] * rinv;
+__device__ __forceinline__ void to_state_f32(const double x[kNeqMax], float q[kNvMax]) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) s.q[v] = q[v];
-  if (MODEL == 1) {
-    s.e = q[4];
-    const float ke = fmaf(s.w, s.w, fmaf(s.v, s.v, s.u * s.u));
-    const float e_int = fmaf(-0.5f, ke, s.e * rinv);
-    s.p = fmaf(s.r * mc.gm1, e_int, -mc.gpinf);
-    s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
-    s.y = 0.0f;
-    return true;
-  }
-  // model 3: mass fraction in FP32, pressure inversion in FP64
-  s.y = q[4] * rinv;
-  if (clip) {
-    s.y = s.y < mc.ylo ? mc.ylo : s.y;
-    s.y = s.y > mc.yhi ? mc.yhi : s.y;
-  }
-  double p, c;
-  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
-  s.p = float(p);
-  s.c = float(c);
-  s.e = 0.0f;
-  return ok;
+  for (int v = 0; v < kNeqMax; ++v) q[v] = __double2float_rn(MODEL == 3 && v == 0 ? x[0] - kRhoOffD : x[v]);
+  q[5] = MODEL == 3 ? __double2float_rn((x[0] - kRhoOffD) - double(q[0])) : 0.0f;  // both subtractions exact
+  q[6] = MODEL == 3 ? __double2float_rn(x[4] - double(q[4])) : 0.0f;
 }
 
-// Boundary ghost (bc.c:19-49) from the own face state.
+// d = a - b on the state words; model 3: the density difference with the
+// low words (accurate to the rounding of the difference itself)
 template <int MODEL>
-__device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
-  if (bc == 1) {
-    mixed_face_state<MODEL>(mc, mc.inflow, false, g);
-  } else if (bc == 3 || bc == 4) {
-    // velocity and momentum mirrored as such (the momentum is not rebuilt as
-    // rho * u): exact on the axis-aligned faces, as in the FP64 path
-    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
-    if (bc == 3) {
-      const float un = fmaf(g.w, nz, fmaf(g.v, ny, g.u * nx));
-      g.u = fmaf(-2.0f * un, nx, g.u);
-      g.v = fmaf(-2.0f * un, ny, g.v);
-      g.w = fmaf(-2.0f * un, nz, g.w);
-      const float mn = fmaf(g.q[3], nz, fmaf(g.q[2], ny, g.q[1] * nx));
-      g.q[1] = fmaf(-2.0f * mn, nx, g.q[1]);
-      g.q[2] = fmaf(-2.0f * mn, ny, g.q[2]);
-      g.q[3] = fmaf(-2.0f * mn, nz, g.q[3]);
-    } else {
-      g.u = -g.u;
-      g.v = -g.v;
-      g.w = -g.w;
-      g.q[1] = -g.q[1];
-      g.q[2] = -g.q[2];
-      g.q[3] = -g.q[3];
+__device__ __forceinline__ void state_diff(const float a[kNvMax], const float b[kNvMax], float d[kNeqMax]) {
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) d[v] = a[v] - b[v];
+  if constexpr (MODEL == 3) {
+    d[0] = d[0] + (a[5] - b[5]);
+    d[4] = d[4] + (a[6] - b[6]);
+  }
+}
+// out = q + c s per variable (one fused multiply-add); model 3: the density
+// word with its rounding carried into the low word
+template <int MODEL>
+__device__ __forceinline__ void add_slope(const float q[kNvMax], float c, const float s[kNeqMax], float out[kNvMax]) {
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) out[v] = fmaf(c, s[v], q[v]);
+  out[5] = q[5];
+  out[6] = q[6];
+  if constexpr (MODEL == 3) {
+#pragma unroll
+    for (int v = 0; v < kNeqMax; v += 4) {  // the density and rho Y
+      const int lo = lo_word<MODEL>(v);
+      const float p = c * s[v];
+      out[v] = q[v] + p;
+      out[lo] = q[lo] + two_sum_err(q[v], p, out[v]);
     }
   }
 }
 
-// value across a boundary face: the own state, or its ghost (deltavalues.c:9-14)
+// The two-phase mixture EOS of barotropic_eos.c:32-129 (the pressure root of
+// a quadratic, liquid sound speed with a fallback) written on the gas
+// partial density ry = rho Y instead of the mass fraction: the reference's
+// products rho Y and rho (1 - Y) become ry and rho - ry.  The pressure of a
+// bubbly liquid is stiff in the liquid partial density (dp ~ c_liq^2 d(rho -
+// rho Y)), and forming Y = rho Y / rho in FP32 and multiplying it back by rho
+// loses ~1e-7 of rho Y relative to rho: ~0.5 Pa at Y ~ 3e-6.  From the state
+// words directly the inversion sees both partial densities to FP64 rounding
+// of FP32 data.  FP64 throughout; false when neither branch has a real root.
+__device__ __forceinline__ bool eos_mixture_partial(double r, double ry, double &p_out, double &c_out) {
+  const double R_G = 286.0, T_ref = 293.15, r_sat = 998.1618, p_sat = 2340.0;
+  const double c_liq = 1482.5, c_mixture = 1.0;
+  const double rg = ry * R_G * T_ref, rl = r - ry;
+  double c2 = c_liq * c_liq;
+  double b = c2 * r_sat - p_sat - rg - rl * c2;
+  double d = (p_sat - c2 * r_sat) * rg;
+  double disc = b * b - 4.0 * d;
+  double ct = c_liq;
+  if (!(disc >= 0.0)) {
+    ct = c_mixture;
+    c2 = c_mixture * c_mixture;
+    b = c2 * r_sat - p_sat - rg - rl * c2;
+    d = (p_sat - c2 * r_sat) * rg;
+    disc = b * b - 4.0 * d;
+    if (!(disc >= 0.0)) {
+      p_out = __longlong_as_double(0x7ff8000000000000ll);
+      c_out = ct;
+      return false;
+    }
+  }
+  p_out = 0.5 * (-b + sqrt(disc));  // the larger root
+  c_out = ct;
+  return true;
+}
+
+// FP32 face state in the Cartesian frame (facevalues.c:113-142): the CFL
+// radius.
+struct FS {
+  float r, u, v, w, p, c;
+};
 template <int MODEL>
-__device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float own[kNeqMax],
-                                               float nb[kNeqMax]) {
+__device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, FS &s) {
+  s.r = MODEL == 3 ? float(state_rho_d<MODEL>(q)) : q[0];
+  const float rinv = fast_rcp(s.r);
+  s.u = q[1] * rinv;
+  s.v = q[2] * rinv;
+  s.w = q[3] * rinv;
+  if (MODEL == 1) {
+    const float msq = fmaf(q[3], q[3], fmaf(q[2], q[2], q[1] * q[1]));
+    s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, rinv, q[4]), -mc.gpinf);
+    s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * rinv);
+    return true;
+  }
+  double p, c;
+  const bool ok = eos_mixture_partial(state_rho_d<MODEL>(q), double(q[4]) + double(q[6]), p, c);
+  s.p = float(p);
+  s.c = float(c);
+  return ok;
+}
+
+// Value across a boundary face (deltavalues.c:9-14; bc.c:19-49): the own
+// state (transmissive), the inflow state, or the own state with the momentum
+// mirrored as such (slip wall: normal component; no-slip wall: all of it),
+// which on the axis-aligned faces is exact, as in the FP64 path.
+template <int MODEL>
+__device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float own[kNvMax],
+                                               float nb[kNvMax]) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
-  if (bc == 1 || bc == 3 || bc == 4) {
-    FS g;
-    mixed_face_state<MODEL>(mc, own, false, g);
-    mixed_ghost<MODEL>(mc, bc, f, g);
+  for (int v = 0; v < kNvMax; ++v) nb[v] = own[v];
+  if (bc == 1) {
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
+    for (int v = 0; v < kNvMax; ++v) nb[v] = mc.inflow[v];
+  } else if (bc == 3) {
+    const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
+    const float mn = fmaf(own[3], nz, fmaf(own[2], ny, own[1] * nx));
+    nb[1] = fmaf(-2.0f * mn, nx, own[1]);
+    nb[2] = fmaf(-2.0f * mn, ny, own[2]);
+    nb[3] = fmaf(-2.0f * mn, nz, own[3]);
+  } else if (bc == 4) {
+    nb[1] = -own[1];
+    nb[2] = -own[2];
+    nb[3] = -own[3];
   }
 }
 
 // Face-local state: the momentum rotated into the face frame (normal n,
-// tangents t1, t2), its velocities, pressure and sound speed.  The mixed
-// path requires orthonormal frames (checked at upload), so the kinetic energy
-// and the stress contraction n.(p I).n = p are frame invariant.
+// tangents t1, t2), the normal velocity, pressure and sound speed.  The mixed
+// path requires orthonormal frames (checked at upload), so |m|^2 and the
+// stress contraction n.(p I).n = p are frame invariant; tangential velocities
+// are formed only for the upwind state the HLLC flux takes.
 struct LS {
-  float r, mn, mm, ml, q4;  // density, local momentum, fifth conservative variable
-  float un, um, ul;         // local velocity
-  float p, c, e, y;
+  float r, rinv, mn, mm, ml;  // density, its reciprocal, local momentum
+  float un;                   // normal velocity
+  float p, c, e, y;           // pressure, sound speed, energy (model 1), mass fraction (model 3)
 };
 
 // Face frames of the reference's hexahedral cells (tagvector.c:40-53 on
@@ -275,7 +360,7 @@ __host__ __device__ constexpr int frame_row(int f, int k) {
 __host__ __device__ constexpr bool frame_neg(int f, int r) { return std_frame(f, 3 * r + frame_col(f, r)) < 0.0f; }
 
 template <int F, int R>
-__device__ __forceinline__ float frame_in_row(const float q[kNeqMax]) {
+__device__ __forceinline__ float frame_in_row(const float *q) {
   constexpr int k = frame_col(F, R);
   constexpr bool neg = frame_neg(F, R);
   return neg ? -q[1 + k] : q[1 + k];
@@ -288,7 +373,7 @@ __device__ __forceinline__ float frame_out_col(float a, float b, float c) {
   return neg ? -x : x;
 }
 template <int F>
-__device__ __forceinline__ void frame_in_f(const float q[kNeqMax], float &mn, float &mm, float &ml) {
+__device__ __forceinline__ void frame_in_f(const float *q, float &mn, float &mm, float &ml) {
   mn = frame_in_row<F, 0>(q);
   mm = frame_in_row<F, 1>(q);
   ml = frame_in_row<F, 2>(q);
@@ -301,7 +386,7 @@ __device__ __forceinline__ void frame_out_f(float a, float b, float c, float out
 }
 // momentum into the frame of face F (F < 0: face f, known at run time)
 template <int F>
-__device__ __forceinline__ void frame_in(int f, const float q[kNeqMax], float &mn, float &mm, float &ml) {
+__device__ __forceinline__ void frame_in(int f, const float *q, float &mn, float &mm, float &ml) {
   if constexpr (F >= 0) {
     frame_in_f<F>(q, mn, mm, ml);
   } else {
@@ -333,31 +418,36 @@ __device__ __forceinline__ void frame_out(int f, float a, float b, float c, floa
 }
 
 template <int MODEL, int F = -1>
-__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float q[kNeqMax], bool clip, LS &s) {
-  s.r = state_rho<MODEL>(q[0]);
-  s.q4 = q[4];
+__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float *q, bool clip, LS &s) {
   frame_in<F>(f, q, s.mn, s.mm, s.ml);
-  const float rinv = fast_rcp(s.r);
-  s.un = s.mn * rinv;
-  s.um = s.mm * rinv;
-  s.ul = s.ml * rinv;
   if (MODEL == 1) {
+    s.r = q[0];
+    s.rinv = fast_rcp(s.r);
+    s.un = s.mn * s.rinv;
     s.e = q[4];
     s.y = 0.0f;
-    // p = (gamma - 1) (E - rho |u|^2 / 2) - gamma pinf, rho |u|^2 as m . u
-    const float ke2 = fmaf(s.ml, s.ul, fmaf(s.mm, s.um, s.mn * s.un));
-    s.p = fmaf(mc.gm1, fmaf(-0.5f, ke2, s.e), -mc.gpinf);
-    s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
+    // p = (gamma - 1) (E - |m|^2 / (2 rho)) - gamma pinf, c^2 = gamma (p + pinf) / rho
+    const float msq = fmaf(s.ml, s.ml, fmaf(s.mm, s.mm, s.mn * s.mn));
+    s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, s.rinv, s.e), -mc.gpinf);
+    s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * s.rinv);
     return true;
   }
+  // model 3: the FP64 pressure inversion on the density from both state
+  // words and the gas partial density rho Y (clipped as facercnstr.c:43-44
+  // clips Y)
+  const double r64 = state_rho_d<MODEL>(q);
+  s.r = float(r64);
+  s.rinv = fast_rcp(s.r);
+  s.un = s.mn * s.rinv;
   s.e = 0.0f;
-  s.y = q[4] * rinv;
+  double ry = double(q[4]) + double(q[6]);
   if (clip) {
-    s.y = s.y < mc.ylo ? mc.ylo : s.y;
-    s.y = s.y > mc.yhi ? mc.yhi : s.y;
+    ry = ry < double(mc.ylo) * r64 ? double(mc.ylo) * r64 : ry;
+    ry = ry > double(mc.yhi) * r64 ? double(mc.yhi) * r64 : ry;
   }
+  s.y = float(ry) * s.rinv;
   double p, c;
-  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
+  const bool ok = eos_mixture_partial(r64, ry, p, c);
   s.p = float(p);
   s.c = float(c);
   return ok;
@@ -374,8 +464,6 @@ __device__ __forceinline__ void local_ghost(const MixedConst &mc, int bc, int f,
     g.un = -g.un;
     g.mn = -g.mn;
     if (bc == 4) {
-      g.um = -g.um;
-      g.ul = -g.ul;
       g.mm = -g.mm;
       g.ml = -g.ml;
     }
@@ -393,7 +481,7 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   const float SL = fminf(L.un - L.c, R.un - R.c);
   const float num = fmaf(SR, R.mn, fmaf(-SL, L.mn, fmaf(L.mn, L.un, L.p) - fmaf(R.mn, R.un, R.p)));
   const float den = fmaf(SR, R.r, fmaf(-SL, L.r, L.mn - R.mn));
-  float S_S = __fdividef(num, den);
+  float S_S = num * fast_rcp(den);
   const bool ok = !isnan(S_S);
   if (bc == 3) S_S = 0.0f;
   // region selection in the order of hllc_euler.c:18-50
@@ -403,9 +491,9 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
   const bool left = r1 || r2;
   const bool star = r2 || r3;
-  const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn;
-  const float Kun = left ? L.un : R.un, Kum = left ? L.um : R.um, Kul = left ? L.ul : R.ul;
+  const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn, Kun = left ? L.un : R.un;
   const float Kp = left ? L.p : R.p, Ke = left ? L.e : R.e, Ky = left ? L.y : R.y;
+  const float Krinv = left ? L.rinv : R.rinv, Kmm = left ? L.mm : R.mm, Kml = left ? L.ml : R.ml;
   const float SK = left ? SL : SR;
   // F_K + S_K (U*_K - U_K) is the physical flux of the star state U*_K
   // (star_region_euler.c:3-40): mass flux rho* S*, pressure
@@ -427,8 +515,8 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   }
   const float F0 = m;
   const float Fa = fmaf(m, un, pp);
-  const float Fb = m * Kum;
-  const float Fc = m * Kul;
+  const float Fb = m * (Kmm * Krinv);
+  const float Fc = m * (Kml * Krinv);
   const float F4 = MODEL == 1 ? (ee + pp) * un : m * Ky;
   Fn[0] = F0;
   frame_out<F>(f, Fa, Fb, Fc, Fn);
@@ -439,9 +527,8 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
 // Canonical flux of a face from the lower / upper face values (bc > 0: a
 // domain-boundary face, the upper side is the ghost of the lower one).
 template <int MODEL, int F = -1>
-__device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int bc, bool clip,
-                                               const float lo[kNeqMax], const float hi[kNeqMax],
-                                               float Fn[kNeqMax]) {
+__device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int bc, bool clip, const float *lo,
+                                               const float *hi, float Fn[kNeqMax]) {
   LS Ls, Rs;
   bool ok = local_state<MODEL, F>(mc, f, lo, clip, Ls);
   if (bc > 0) {
@@ -454,32 +541,79 @@ __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int 
   return ok;
 }
 
-// Minmod-limited slope of one variable towards a face (reconctruct_V3.c:17-43,
-// slopes divided by dist_cc as multiplications) from the delta across the
-// face (d0) and across the opposite face (d1): zero unless the face is active
-// (not a domain boundary), |d0| > 1e-10 and sm * sp > 0; then the slope of
-// smaller magnitude.  Selects rather than branches.  A NaN product (a domain
-// boundary behind the cell has 1/dist_cc = inf and a zero delta) gives zero,
-// as in the reference.
+// ============================ reconstruction ================================
+
+// minmod of a and b: the one of smaller magnitude when both have the same
+// sign, else zero -- the median of a, b and 0 (four min/max operations)
+__device__ __forceinline__ float minmod(float a, float b) { return fmaxf(fminf(a, b), fminf(fmaxf(a, b), 0.0f)); }
+
+// Face values of a cell on an axis whose two neighbours have the cell's
+// level: s = minmod(q+ - q, q - q-), face+ = q + k s, face- = q - k s.
+// WHICH: 1 only face+, -1 only face-, 0 both.
+template <int MODEL, int WHICH = 0>
+__device__ __forceinline__ void axis_faces(const float q[kNvMax], const float nbp[kNvMax], const float nbm[kNvMax],
+                                           float k, float fp[kNvMax], float fm[kNvMax]) {
+  float dp[kNeqMax], dm[kNeqMax], s[kNeqMax];
+  state_diff<MODEL>(nbp, q, dp);
+  state_diff<MODEL>(q, nbm, dm);
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) s[v] = minmod(dp[v], dm[v]);
+  if (WHICH >= 0) add_slope<MODEL>(q, k, s, fp);
+  if (WHICH <= 0) add_slope<MODEL>(q, -k, s, fm);
+}
+
+// The reference's per-face limited slope (reconctruct_V3.c:17-43, slopes
+// divided by dist_cc as multiplications) from the delta across the face (d0)
+// and across the opposite face (d1): zero unless the face is active (not a
+// domain boundary), |d0| > 1e-10 and sm * sp > 0; then the slope of smaller
+// magnitude.  A NaN product (a domain boundary behind the cell has 1/dist_cc
+// = inf and a zero delta) gives zero, as in the reference.
 __device__ __forceinline__ float minmod_slope(bool active, float d0, float d1, float inv_p, float inv_m) {
   const float sp = d0 * inv_p, sm = -d1 * inv_m;
   const float m = fabsf(sm) > fabsf(sp) ? sp : sm;
   return (active && fabsf(d0) > 1e-10f && sm * sp > 0.0f) ? m : 0.0f;
 }
 
-// Minmod face value of face f of a cell with geometry code gx from its state
-// and the deltas across f (d0) and across the opposite face (d1).
-__device__ __forceinline__ void recon_face(const GeoTables *geo, int32_t gx, int f, const float qx[kNeqMax],
-                                           const float d0[kNeqMax], const float d1[kNeqMax],
-                                           float out[kNeqMax]) {
-  const int lev = level_of(gx);
-  const int rf = rel_of(gx, f), ro = rel_of(gx, opp_face(f));
-  const float *gf = geo_face(geo, lev, f, rf);
-  const float dcf = gf[0], inv_p = gf[1];
-  const float inv_m = geo_face(geo, lev, opp_face(f), ro)[1];
+// Face value of a face of a cell in the reference's per-face form: values
+// across the face (nbf) and across the opposite face (nbo), the face's
+// dist_cf and 1/dist_cc (inv_p) and the opposite face's 1/dist_cc (inv_m).
+template <int MODEL>
+__device__ __forceinline__ void face_general(const float q[kNvMax], const float nbf[kNvMax], const float nbo[kNvMax],
+                                             bool active, float dcf, float inv_p, float inv_m, float out[kNvMax]) {
+  float d0[kNeqMax], d1[kNeqMax], s[kNeqMax];
+  state_diff<MODEL>(nbf, q, d0);
+  state_diff<MODEL>(nbo, q, d1);
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v)
-    out[v] = fmaf(dcf, minmod_slope(rf != kRelBoundary, d0[v], d1[v], inv_p, inv_m), qx[v]);
+  for (int v = 0; v < kNeqMax; ++v) s[v] = minmod_slope(active, d0[v], d1[v], inv_p, inv_m);
+  add_slope<MODEL>(q, dcf, s, out);
+}
+
+// Both face values of a cell with geometry code gx on axis ax from the values
+// across its + and - faces: the shared slope where both neighbours have the
+// cell's level, the per-face form otherwise.  WHICH as in axis_faces.
+template <int MODEL, bool MUSCL, int WHICH = 0>
+__device__ __forceinline__ void cell_axis_faces(const GeoTables *geo, int32_t gx, int ax, const float q[kNvMax],
+                                                const float nbp[kNvMax], const float nbm[kNvMax], float fp[kNvMax],
+                                                float fm[kNvMax]) {
+  if (!MUSCL) {
+#pragma unroll
+    for (int v = 0; v < kNvMax; ++v) {
+      if (WHICH >= 0) fp[v] = q[v];
+      if (WHICH <= 0) fm[v] = q[v];
+    }
+    return;
+  }
+  const int lev = level_of(gx);
+  const int f1 = plus_face(ax), f0 = minus_face(ax);
+  const int r1 = rel_of(gx, f1), r0 = rel_of(gx, f0);
+  const float *g1 = geo_face(geo, lev, f1, r1);
+  if (r1 == kRelSame && r0 == kRelSame) {
+    axis_faces<MODEL, WHICH>(q, nbp, nbm, g1[3], fp, fm);
+    return;
+  }
+  const float *g0 = geo_face(geo, lev, f0, r0);
+  if (WHICH >= 0) face_general<MODEL>(q, nbp, nbm, r1 != kRelBoundary, g1[0], g1[1], g0[1], fp);
+  if (WHICH <= 0) face_general<MODEL>(q, nbm, nbp, r0 != kRelBoundary, g0[0], g0[1], g1[1], fm);
 }
 
 template <int NT = kBlock>  // threads of the block
@@ -499,10 +633,10 @@ __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
 // CFL spectral radius of one cell (definition in fvgpu.h), FP32, with the
 // area of face f from area(f) and 1 / (2 V).
 template <int MODEL, class AreaFn>
-__device__ __forceinline__ float cell_lambda_with(const MixedConst &mc, const float q[kNeqMax], AreaFn area,
+__device__ __forceinline__ float cell_lambda_with(const MixedConst &mc, const float q[kNvMax], AreaFn area,
                                                   float inv2vol) {
   FS s;
-  mixed_face_state<MODEL>(mc, q, false, s);
+  mixed_face_state<MODEL>(mc, q, s);
   float acc = 0.0f;
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
@@ -514,11 +648,11 @@ __device__ __forceinline__ float cell_lambda_with(const MixedConst &mc, const fl
 
 template <int MODEL>
 __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTables *geo, int32_t g,
-                                               const float q[kNeqMax]) {
+                                               const float q[kNvMax]) {
   const int lev = level_of(g);
   return cell_lambda_with<MODEL>(
       mc, q,
-      [&](int f) {
+      [geo, g, lev](int f) {
         const int rel = rel_of(g, f);
         return rel == kRelFiner ? 4.0f * geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
       },
@@ -526,10 +660,10 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
 }
 
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
-// CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
+// CFL radius at the last stage (qn receives the new FP32 state words).
 template <int MODEL>
-__device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageArgs &a, int c, float dtv,
-                                             const float R[kNeqMax], bool ok, float qn[kNeqMax]) {
+__device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dtv, const float R[kNeqMax], bool ok,
+                                             float qn[kNvMax]) {
   const int n = a.n;
   bool finite = true;
 #pragma unroll
@@ -552,38 +686,46 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     }
   }
   if (a.last) {
+    double snew[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
-      a.SNout[v * n + c] = snew;
-      qn[v] = to_state_f32<MODEL>(v, snew);
-      a.SNfout[v * n + c] = qn[v];
+      snew[v] = __ldg(a.SN + v * n + c) + double(dn[v]);
+      a.SNout[v * n + c] = snew[v];
     }
+    to_state_f32<MODEL>(snew, qn);
+#pragma unroll
+    for (int v = 0; v < kNv<MODEL>; ++v) a.SNfout[v * n + c] = qn[v];
     return true;
   }
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     a.Dout[v * n + c] = dn[v];
-    a.Sout[v * n + c] = __ldg(a.SNf + v * n + c) + dn[v];  // the value the next stage would form
+    const float sn = __ldg(a.SNf + v * n + c);
+    const float x = sn + dn[v];  // the value the next stage would form
+    a.Sout[v * n + c] = x;
+    if (lo_word<MODEL>(v) >= 0) {
+      const int lo = lo_word<MODEL>(v);
+      a.Sout[lo * n + c] = __ldg(a.SNf + lo * n + c) + two_sum_err(sn, dn[v], x);
+    }
   }
   return false;
 }
 
 // stage state of any cell from global memory (SNf + D, written by the
 // previous stage)
-__device__ __forceinline__ void global_state(const MixedConst &mc, const StageArgs &a, int x, float q[kNeqMax]) {
+template <int MODEL>
+__device__ __forceinline__ void global_state(const StageArgs &a, int x, float q[kNvMax]) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) q[v] = v < mc.neq ? __ldg(a.Sin + v * a.n + x) : 0.0f;
+  for (int v = 0; v < kNvMax; ++v) q[v] = v < kNv<MODEL> ? __ldg(a.Sin + v * a.n + x) : 0.0f;
 }
 
 // ============================ viscous terms =================================
 
 // Cartesian velocity of the ghost across a boundary face f (bc.c:19-49) from
 // the own face values q.
-__device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float q[kNeqMax],
-                                               float u[3]) {
+__device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float *q, float u[3]) {
   if (bc == 1) {
-    const float rinv = fast_rcp(mc.inflow[0]);
+    const float rinv = fast_rcp(state_rho_rt(mc.model, mc.inflow[0]));
     u[0] = mc.inflow[1] * rinv;
     u[1] = mc.inflow[2] * rinv;
     u[2] = mc.inflow[3] * rinv;
@@ -609,8 +751,8 @@ __device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int
 // FV . n of one face (flux_viscous.c:57-232 with turb = 0) from the face
 // values of both sides (bc > 0: a boundary face, the other side is the
 // ghost of lo) and the momentum gradients of both cells, FP32.
-__device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int bc, const float lo[kNeqMax],
-                                               const float hi[kNeqMax], const float gl[9], const float gh[9],
+__device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int bc, const float *lo,
+                                               const float *hi, const float gl[9], const float gh[9],
                                                float FVn[kNeqMax]) {
   float ul[3], uh[3];
   {
@@ -656,6 +798,23 @@ __device__ __forceinline__ void load_grad9f(const float *__restrict__ SG, int n,
   for (int i = 0; i < 9; ++i) g[i] = __ldg(SG + i * n + c);
 }
 
+// (F - FV).n of a face: the canonical flux minus the viscous normal flux,
+// with the gradients of the face's lower and upper cells clo / chi
+template <int MODEL, int F = -1>
+__device__ __forceinline__ bool face_flux(const MixedConst &mc, const StageArgs &a, int f, int bc, bool clip,
+                                          const float *lo, const float *hi, int clo, int chi, float Fn[kNeqMax]) {
+  const bool ok = canonical_flux<MODEL, F>(mc, f, bc, clip, lo, hi, Fn);
+  if (mc.ns == 1) {
+    float gl[9], gh[9], FVn[kNeqMax];
+    load_grad9f(a.SG, a.n, clo, gl);
+    load_grad9f(a.SG, a.n, chi, gh);
+    viscous_normal(mc, f, bc, lo, hi, gl, gh, FVn);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
+  }
+  return ok;
+}
+
 // Green-Gauss momentum gradients of the stage-input state (gradcalc.c:9-47,
 // rows of rho u, rho v, rho w), FP32, one cell per thread.
 template <int MODEL>
@@ -663,9 +822,8 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
   const int c = blockIdx.x * kBlock + threadIdx.x;
   const int n = a.n;
   if (c >= n) return;
-  float q[kNeqMax];
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) q[v] = __ldg(a.Sin + v * n + c);
+  float q[kNvMax];
+  global_state<MODEL>(a, c, q);
   const int32_t g = __ldg(a.geom + c);
   const int lev = level_of(g);
   const float inv_vol = a.geo->inv_vol[lev];
@@ -692,7 +850,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
       } else {
         float u[3];
         ghost_velocity(mc, bc, f, q, u);
-        const float rho = state_rho<MODEL>(q[0]);
+        const float rho = state_rho<MODEL>(q);
         m[0] = rho * u[0];
         m[1] = rho * u[1];
         m[2] = rho * u[2];
@@ -722,65 +880,109 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
 
 // ============================ general kernel ================================
 
+// Shared memory of the general kernel: the block's stage states st[nv][256],
+// its cells' six face values sf[6][nv][256] and per axis the published +
+// face fluxes fpub[3][5][256].
+template <int MODEL>
+constexpr size_t general_smem_bytes() {
+  return sizeof(float) * kBlock * (7 * kNv<MODEL> + 3 * kNeqMax);
+}
+
 template <int MODEL>
 struct Block {
+  static constexpr int NV = kNv<MODEL>;
   const StageArgs &a;
   const MixedConst &mc;
   int c0, cnt;
   const float (*st)[kBlock];
-  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock])
-      : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_) {}
+  const float (*sf)[NV][kBlock];
+  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock],
+                   const float (*sf_)[NV][kBlock])
+      : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_), sf(sf_) {}
   __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(cnt); }
-  __device__ __forceinline__ void state(int x, float q[kNeqMax]) const {
+  __device__ __forceinline__ void state(int x, float q[kNvMax]) const {
     if (in_block(x)) {
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) q[v] = st[v][x - c0];
+      for (int v = 0; v < kNvMax; ++v) q[v] = v < NV ? st[v][x - c0] : 0.0f;
       return;
     }
-    global_state(mc, a, x, q);
+    global_state<MODEL>(a, x, q);
   }
   // value across face f of cell x (deltavalues.c): single neighbour, mean of
   // the four fine ones, or the boundary ghost
-  __device__ __forceinline__ void across(int x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
+  __device__ __forceinline__ void across(int x, int f, const float own[kNvMax], float nb[kNvMax]) const {
     const int32_t code = __ldg(a.nbr + f * a.n + x);
     if (code >= 0) {
       state(code, nb);
     } else if (is_hanging(code)) {
       const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-      float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      float acc[kNvMax] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
       for (int s = 0; s < 4; ++s) {
-        float q[kNeqMax];
+        float q[kNvMax];
         state(__ldg(k + s), q);
+        if constexpr (MODEL == 3) {  // paired words summed with the rounding carried into the low word
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
+          for (int v = 0; v < kNeqMax; ++v) {
+            const int lo = lo_word<MODEL>(v);
+            if (lo >= 0) {
+              const float sv = acc[v] + q[v];
+              acc[lo] = acc[lo] + (two_sum_err(acc[v], q[v], sv) + q[lo]);
+              acc[v] = sv;
+            } else {
+              acc[v] += q[v];
+            }
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
+        }
       }
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
+      for (int v = 0; v < kNvMax; ++v) nb[v] = 0.25f * acc[v];
     } else {
       boundary_value<MODEL>(mc, -1 - code, f, own, nb);
     }
   }
-  // face value of face f of any cell (used across block edges)
-  __device__ __forceinline__ void recon_any(int x, int f, float out[kNeqMax]) const {
-    float qx[kNeqMax], nbp[kNeqMax], nbm[kNeqMax], d0[kNeqMax], d1[kNeqMax];
-    state(x, qx);
-    across(x, f, qx, nbp);
-    across(x, opp_face(f), qx, nbm);
+  // face value of face f of cell x: the block's table when x is in the
+  // block, else recomputed from global memory (across block edges)
+  template <bool MUSCL>
+  __device__ __forceinline__ void face_value(int x, int f, float out[kNvMax]) const {
+    if (in_block(x)) {
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      d0[v] = nbp[v] - qx[v];
-      d1[v] = nbm[v] - qx[v];
+      for (int v = 0; v < kNvMax; ++v) out[v] = v < NV ? sf[f][v][x - c0] : 0.0f;
+      return;
     }
-    recon_face(a.geo, __ldg(a.geom + x), f, qx, d0, d1, out);
+    float q[kNvMax];
+    state(x, q);
+    if (!MUSCL) {
+#pragma unroll
+      for (int v = 0; v < kNvMax; ++v) out[v] = q[v];
+      return;
+    }
+    const int ax = axis_of_face(f);
+    float nbp[kNvMax], nbm[kNvMax], unused[kNvMax];
+    across(x, plus_face(ax), q, nbp);
+    across(x, minus_face(ax), q, nbm);
+    const int32_t gx = __ldg(a.geom + x);
+    if (f == plus_face(ax))
+      cell_axis_faces<MODEL, true, 1>(a.geo, gx, ax, q, nbp, nbm, out, unused);
+    else
+      cell_axis_faces<MODEL, true, -1>(a.geo, gx, ax, q, nbp, nbm, unused, out);
   }
 };
 
+// dynamic shared memory of the kernels (16-byte aligned)
+extern __shared__ __align__(16) float g_mixed_smem[];
+
+// model 3 (FP64 pressure inversion, six state words) runs two blocks per SM
+// with up to 128 registers, model 1 four with 64; neither spills
 template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageArgs a) {
-  __shared__ float st[kNeqMax][kBlock];
-  __shared__ float sf[6][kNeqMax][kBlock];
-  __shared__ float fp[3][kNeqMax][kBlock];
+__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(MixedConst mc, StageArgs a) {
+  constexpr int NV = kNv<MODEL>;
+  float(*st)[kBlock] = reinterpret_cast<float(*)[kBlock]>(g_mixed_smem);
+  float(*sf)[NV][kBlock] = reinterpret_cast<float(*)[NV][kBlock]>(g_mixed_smem + NV * kBlock);
+  float(*fpub)[kNeqMax][kBlock] = reinterpret_cast<float(*)[kNeqMax][kBlock]>(g_mixed_smem + 7 * NV * kBlock);
   __shared__ float s_dt;
   const BlockDesc bd = a.blocks[blockIdx.x];
   const int t = threadIdx.x;
@@ -788,16 +990,14 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   const int c = c0 + t;
   const int n = a.n;
   const bool active = t < bd.count;
-  constexpr int neq = kNeqMax;  // models 1 and 3: five conservative variables
-  constexpr bool muscl = MUSCL;
-  Block<MODEL> blk(a, mc, c0, bd.count, st);
+  const Block<MODEL> blk(a, mc, c0, bd.count, st, sf);
 
   // A: own stage state
-  float q[kNeqMax];
+  float q[kNvMax];
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) {
-    q[v] = (active && v < neq) ? __ldg(a.Sin + v * n + c) : 0.0f;
-    st[v][t] = q[v];
+  for (int v = 0; v < kNvMax; ++v) {
+    q[v] = (active && v < NV) ? __ldg(a.Sin + v * n + c) : 0.0f;
+    if (v < NV) st[v][t] = q[v];
   }
   int32_t nb[6];
   int32_t g = 0;
@@ -807,113 +1007,124 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   if (t == 0) s_dt = __double2float_rn(*a.dt);
   __syncthreads();
 
-  // B: own face values
+  // B: own face values, axis by axis
   if (active) {
-    if (muscl) {
-      float dl[6][kNeqMax];
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        float nbv[kNeqMax];
-        blk.across(c, f, q, nbv);
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) dl[f][v] = nbv[v] - q[v];
+    for (int ax = 0; ax < 3; ++ax) {
+      float nbp[kNvMax], nbm[kNvMax], fpv[kNvMax], fmv[kNvMax];
+      if (MUSCL) {
+        blk.across(c, plus_face(ax), q, nbp);
+        blk.across(c, minus_face(ax), q, nbm);
       }
+      cell_axis_faces<MODEL, MUSCL>(a.geo, g, ax, q, nbp, nbm, fpv, fmv);
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        float o[kNeqMax];
-        recon_face(a.geo, g, f, q, dl[f], dl[opp_face(f)], o);
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = o[v];
+      for (int v = 0; v < NV; ++v) {
+        sf[plus_face(ax)][v][t] = fpv[v];
+        sf[minus_face(ax)][v][t] = fmv[v];
       }
-    } else {
-#pragma unroll
-      for (int f = 0; f < 6; ++f)
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = q[v];
     }
   }
   __syncthreads();
 
-  // C: fluxes, + faces (publish), barrier, - faces
-  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  bool ok = true;
   const int lev = level_of(g);
-#pragma unroll 1
-  for (int it = 0; it < 6; ++it) {
-    if (it == 3) __syncthreads();
-    if (!active) continue;
-    const int f = face_of_iter(it);
-    const bool plus = it < 3;
-    const int fo = opp_face(f);
-    const int32_t code = nb[f];
-    const bool boundary = is_boundary(code);
-    const bool hanging = is_hanging(code);
-    const int rel = rel_of(g, f);
-    const int nsub = hanging ? 4 : 1;
-    const int32_t *hk = hanging ? a.hang_nbr + 4 * hang_index(code) : nullptr;
-    const float A = hanging ? a.geo->sub_area[lev * 6 + f] : geo_face(a.geo, lev, f, rel)[2];
-#pragma unroll 1
-    for (int s = 0; s < nsub; ++s) {
-      const int other = boundary ? -1 : (hanging ? __ldg(hk + s) : code);
-      float Fn[kNeqMax];
-      // the - side reads a published flux when the lower cell is in the block
-      // and its + face carries a single neighbour (this cell)
-      const bool published = !plus && !boundary && (hanging || rel == kRelSame) && blk.in_block(other);
-      if (published) {
-        const int tl = other - c0;
+  bool ok = true;
+  // C1: + faces.  fpub[ax][.][t] receives the flux of a single-neighbour +
+  // face (read by the upper cell when it is in the block) or, for a boundary
+  // or 1:4 face, its contribution T+ (read back by this thread only).
+  if (active) {
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
+    for (int ax = 0; ax < 3; ++ax) {
+      const int f = plus_face(ax), fo = minus_face(ax);
+      const int32_t code = nb[f];
+      float own[kNvMax], Fn[kNeqMax], T[kNeqMax];
+#pragma unroll
+      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? sf[f][v][t] : 0.0f;
+      if (is_boundary(code)) {
+        ok &= face_flux<MODEL>(mc, a, f, -1 - code, MUSCL, own, own, c, c, T);
+      } else if (is_hanging(code)) {
+        const int32_t *hk = a.hang_nbr + 4 * hang_index(code);
+        const float A = a.geo->sub_area[lev * 6 + f];
+#pragma unroll 1
+        for (int s = 0; s < 4; ++s) {
+          const int other = __ldg(hk + s);
+          float hi[kNvMax];
+          blk.template face_value<MUSCL>(other, fo, hi);
+          ok &= face_flux<MODEL>(mc, a, f, 0, MUSCL, own, hi, c, other, Fn);
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) T[v] = s == 0 ? A * Fn[v] : T[v] + A * Fn[v];
+        }
       } else {
-        float own[kNeqMax], oth[kNeqMax];
+        float hi[kNvMax];
+        blk.template face_value<MUSCL>(code, fo, hi);
+        ok &= face_flux<MODEL>(mc, a, f, 0, MUSCL, own, hi, c, code, T);
+      }
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) {
-          own[v] = sf[f][v][t];
-          oth[v] = own[v];
-        }
-        if (!boundary) {
-          if (blk.in_block(other)) {
+      for (int v = 0; v < kNeqMax; ++v) fpub[ax][v][t] = T[v];
+    }
+  }
+  __syncthreads();
+
+  // C2: - faces (published fluxes reused) and the residual, axis by axis
+  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (active) {
 #pragma unroll
-            for (int v = 0; v < kNeqMax; ++v) oth[v] = sf[fo][v][other - c0];
-          } else if (muscl) {
-            blk.recon_any(other, fo, oth);
+    for (int ax = 0; ax < 3; ++ax) {
+      const int f = minus_face(ax), fo = plus_face(ax);
+      const int32_t code = nb[f];
+      float own[kNvMax], Tm[kNeqMax], Fn[kNeqMax];
+#pragma unroll
+      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? sf[f][v][t] : 0.0f;
+      const bool hang_m = is_hanging(code), hang_p = is_hanging(nb[fo]);
+      if (is_boundary(code)) {
+        // the cell's own boundary face in its own frame; canonical orientation is -1 times that
+        ok &= face_flux<MODEL>(mc, a, f, -1 - code, MUSCL, own, own, c, c, Fn);
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) Tm[v] = -Fn[v];
+      } else if (hang_m) {
+        const int32_t *hk = a.hang_nbr + 4 * hang_index(code);
+        const float A = a.geo->sub_area[lev * 6 + f];
+#pragma unroll 1
+        for (int s = 0; s < 4; ++s) {
+          const int other = __ldg(hk + s);
+          if (blk.in_block(other)) {  // the fine cell's + face has this cell alone: published
+#pragma unroll
+            for (int v = 0; v < kNeqMax; ++v) Fn[v] = fpub[ax][v][other - c0];
           } else {
-            blk.state(other, oth);
+            float lo[kNvMax];
+            blk.template face_value<MUSCL>(other, fo, lo);
+            ok &= face_flux<MODEL>(mc, a, fo, 0, MUSCL, lo, own, other, c, Fn);
           }
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) Tm[v] = s == 0 ? A * Fn[v] : Tm[v] + A * Fn[v];
         }
-        // canonical orientation: lower side first, frame of the lower cell's + face
-        const bool own_low = plus || boundary;
-        float lo[kNeqMax], hi[kNeqMax];
+      } else if (rel_of(g, f) == kRelSame && blk.in_block(code)) {
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) Tm[v] = fpub[ax][v][code - c0];
+      } else {
+        float lo[kNvMax];
+        blk.template face_value<MUSCL>(code, fo, lo);
+        ok &= face_flux<MODEL>(mc, a, fo, 0, MUSCL, lo, own, code, c, Tm);
+      }
+      const float A = a.geo->axis_area[lev * 3 + ax];
+      if (!hang_m && !hang_p) {
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, Tm[v] - fpub[ax][v][t], R[v]);
+      } else {
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) {
-          lo[v] = own_low ? own[v] : oth[v];
-          hi[v] = own_low ? oth[v] : own[v];
-        }
-        ok &= canonical_flux<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
-        if (mc.ns == 1) {  // (F - FV).n + FH
-          float gl[9], gh[9], FVn[kNeqMax];
-          const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
-          load_grad9f(a.SG, n, clo, gl);
-          load_grad9f(a.SG, n, chi, gh);
-          viscous_normal(mc, own_low ? f : fo, boundary ? -1 - code : 0, lo, hi, gl, gh, FVn);
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
-        }
-        if (plus && !boundary && !hanging) {
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
+          const float tp = hang_p ? fpub[ax][v][t] : A * fpub[ax][v][t];
+          const float tm = hang_m ? Tm[v] : A * Tm[v];
+          R[v] = R[v] + (tm - tp);
         }
       }
-      const float sA = (plus || boundary) ? -A : A;
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];  // separate roundings: equal and opposite face fluxes cancel exactly
     }
   }
 
   float lam = 0.0f;
   if (active) {
-    float qn[kNeqMax];
-    const float dtv = s_dt * a.geo->inv_vol[level_of(g)];
-    if (stage_update<MODEL>(mc, a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
+    float qn[kNvMax];
+    const float dtv = s_dt * a.geo->inv_vol[lev];
+    if (stage_update<MODEL>(a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
   }
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
@@ -940,6 +1151,9 @@ __host__ __device__ constexpr int morton_z(int t) { return ((t >> 2) & 1) | (((t
 // so that the 32 Morton-ordered lanes of a warp read 32 different banks.
 //   Brick8  8x8x4 (256 cells): uniform regions;
 //   Brick4  4x4x4 (64 cells): the smaller same-level blocks of AMR meshes.
+// Face-value slots (the values a thread hands to another): the brick cells'
+// -x, -y, -z face values (axis * N + t), then the halo cells next to the
+// brick (layer 1), side by side in the order -x, +x, -y, +y, -z, +z.
 template <int BX_, int BY_, int BZ_, int PAD_>
 struct BrickShape {
   static constexpr int BX = BX_, BY = BY_, BZ = BZ_, N = BX_ * BY_ * BZ_;
@@ -948,12 +1162,16 @@ struct BrickShape {
   static constexpr int kTile = P * TZ;
   static constexpr int kFaces = (BX + 1) * BY * BZ + BX * (BY + 1) * BZ + BX * BY * (BZ + 1);
   static constexpr int kHalo = 2 * (2 * BY * BZ + 2 * BX * BZ + 2 * BX * BY);
+  static constexpr int kHalo1 = 2 * (BY * BZ + BX * BZ + BX * BY);
+  static constexpr int kSides = BY * BZ + BX * BZ + BX * BY;
+  static constexpr int kFvSlots = 3 * N + kHalo1;
   // flux slots: the +x, +y, +z faces of the N cells (axis * N + t), then
   // the faces on the brick's -x, -y, -z sides
   static constexpr int kSlotSideX = 3 * N, kSlotSideY = kSlotSideX + BY * BZ, kSlotSideZ = kSlotSideY + BX * BZ;
-  // blocks per SM the launch bounds ask for: 48 registers at five 256-thread
-  // blocks (measured faster than four), four for viscous runs (64 registers)
-  static constexpr int kMinBlocks = 5 * 256 / N, kMinBlocksNS = 4 * 256 / N;
+  // blocks per SM the launch bounds ask for (registers per thread): inviscid
+  // model 1 48 (five 256-thread blocks) or 64 (64-thread blocks); viscous
+  // model 1 64; model 3 (FP64 pressure inversion) 80.  None spills.
+  static constexpr int kMinBlocks = N == 256 ? 5 : 16, kMinBlocksNS = 4 * 256 / N, kMinBlocks3 = 3 * 256 / N;
   __host__ __device__ static constexpr int tile_index(int x, int y, int z) {
     return (z + 2) * P + (y + 2) * TX + (x + 2);
   }
@@ -974,6 +1192,16 @@ struct BrickShape {
   __host__ __device__ static constexpr int zslot_y(int r) {
     return r < BX * BY / 2 ? 2 * (r / BX) : 2 * ((r - BX * BY / 2) / BX) + 1;
   }
+  // layer-1 halo cell beyond brick side `side` at in-plane position (i, j):
+  // (y, z) for the x sides, (x, z) for the y sides, (x, y) for the z sides
+  __host__ __device__ static constexpr int halo1_index(int side, int i, int j) {
+    return side == 3   ? i + BY * j
+           : side == 1 ? BY * BZ + i + BY * j
+           : side == 0 ? 2 * BY * BZ + i + BX * j
+           : side == 2 ? 2 * BY * BZ + BX * BZ + i + BX * j
+           : side == 4 ? 2 * BY * BZ + 2 * BX * BZ + i + BX * j
+                       : 2 * BY * BZ + 2 * BX * BZ + BX * BY + i + BX * j;
+  }
   // a cell of the brick or of a neighbour brick (viscous runs read the
   // gradients of a face's two cells), 12 bits: a brick cell is its Morton
   // index; a cell of a neighbour brick has bit 11 set, the brick side in
@@ -983,60 +1211,49 @@ struct BrickShape {
     const int side = x < 0 ? 3 : (x >= BX ? 1 : (y < 0 ? 0 : (y >= BY ? 2 : (z < 0 ? 4 : 5))));
     return 2048u | (uint32_t(side) << 8) | uint32_t(morton_local((x + BX) % BX, (y + BY) % BY, (z + BZ) % BZ));
   }
-  static_assert(kTile <= 2048 && kFaces <= 1024 && kSlotSideZ + BX * BY == kFaces && N <= 256 && BY % 2 == 0,
+  // dynamic shared memory: the tile (stage states, later the face fluxes)
+  // and the face-value slots
+  template <int NV>
+  static constexpr size_t smem_bytes() { return sizeof(float) * NV * (kTile + kFvSlots); }
+  static_assert(kTile <= 2048 && kFvSlots <= 1024 && kFaces <= 1024 && kSlotSideZ + BX * BY == kFaces &&
+                    N <= 256 && BY % 2 == 0 && kNeqMax * kFaces <= 5 * kTile,
                 "brick table fields");
 };
 using Brick8 = BrickShape<8, 8, 4, 0>;
 using Brick4 = BrickShape<4, 4, 4, 4>;
 
-// Face tasks of a brick, in flux-slot order (Morton lanes of a warp then
-// read tile cells in distinct shared-memory banks).  Packed: tile index of
-// the lower cell (11 bits), axis (2), lower / upper cell inside the brick
-// (1 + 1), edge masks of the lower and upper cells (6 + 6).
+// lower cell (brick coordinates) and axis of flux slot `slot`
 template <class S>
-struct BrickTasks {
-  uint32_t task[S::kFaces];
-};
-template <class S>
-constexpr BrickTasks<S> make_brick_tasks() {
-  BrickTasks<S> T{};
-  for (int task = 0; task < S::kFaces; ++task) {
-    int axis = 0, lx = 0, ly = 0, lz = 0;
-    if (task < S::kSlotSideX) {
-      axis = task / S::N;
-      const int t = task % S::N;
-      lx = morton_x(t);
-      ly = morton_y(t);
-      lz = morton_z(t);
-    } else if (task < S::kSlotSideY) {
-      const int r = task - S::kSlotSideX;
-      lx = -1;
-      ly = r % S::BY;
-      lz = r / S::BY;
-    } else if (task < S::kSlotSideZ) {
-      const int r = task - S::kSlotSideY;
-      axis = 1;
-      lx = r % S::BX;
-      ly = -1;
-      lz = r / S::BX;
-    } else {
-      const int r = task - S::kSlotSideZ;
-      axis = 2;
-      lx = r % S::BX;
-      ly = S::zslot_y(r);
-      lz = -1;
-    }
-    const int ux = lx + (axis == 0), uy = ly + (axis == 1), uz = lz + (axis == 2);
-    T.task[task] = uint32_t(S::tile_index(lx, ly, lz)) | (uint32_t(axis) << 11) |
-                   (uint32_t(S::in_brick(lx, ly, lz)) << 13) | (uint32_t(S::in_brick(ux, uy, uz)) << 14) |
-                   (S::edge_mask(lx, ly, lz) << 15) | (S::edge_mask(ux, uy, uz) << 21);
+__host__ __device__ constexpr void slot_lower_cell(int slot, int &axis, int &lx, int &ly, int &lz) {
+  axis = 0;
+  if (slot < S::kSlotSideX) {
+    axis = slot / S::N;
+    const int t = slot % S::N;
+    lx = morton_x(t);
+    ly = morton_y(t);
+    lz = morton_z(t);
+  } else if (slot < S::kSlotSideY) {
+    const int r = slot - S::kSlotSideX;
+    lx = -1;
+    ly = r % S::BY;
+    lz = r / S::BY;
+  } else if (slot < S::kSlotSideZ) {
+    const int r = slot - S::kSlotSideY;
+    axis = 1;
+    lx = r % S::BX;
+    ly = -1;
+    lz = r / S::BX;
+  } else {
+    const int r = slot - S::kSlotSideZ;
+    axis = 2;
+    lx = r % S::BX;
+    ly = S::zslot_y(r);
+    lz = -1;
   }
-  return T;
 }
-template <class S>
-__device__ const BrickTasks<S> g_brick_tasks = make_brick_tasks<S>();
 
-// The two cells of each face task (S::cell_ref), 12 bits each, lower first.
+// The two cells of each flux slot (S::cell_ref), 12 bits each, lower first
+// (viscous runs).
 template <class S>
 struct BrickTaskCells {
   uint32_t c[S::kFaces];
@@ -1044,12 +1261,10 @@ struct BrickTaskCells {
 template <class S>
 constexpr BrickTaskCells<S> make_brick_task_cells() {
   BrickTaskCells<S> C{};
-  const BrickTasks<S> T = make_brick_tasks<S>();
-  for (int task = 0; task < S::kFaces; ++task) {
-    const uint32_t e = T.task[task];
-    const int ti = int(e & 2047u), axis = int((e >> 11) & 3u);
-    const int lz = ti / S::P - 2, rem = ti % S::P, ly = rem / S::TX - 2, lx = rem % S::TX - 2;
-    C.c[task] = S::cell_ref(lx, ly, lz) | (S::cell_ref(lx + (axis == 0), ly + (axis == 1), lz + (axis == 2)) << 12);
+  for (int slot = 0; slot < S::kFaces; ++slot) {
+    int axis = 0, lx = 0, ly = 0, lz = 0;
+    slot_lower_cell<S>(slot, axis, lx, ly, lz);
+    C.c[slot] = S::cell_ref(lx, ly, lz) | (S::cell_ref(lx + (axis == 0), ly + (axis == 1), lz + (axis == 2)) << 12);
   }
   return C;
 }
@@ -1116,37 +1331,105 @@ constexpr BrickHalo<S> make_brick_halo() {
 template <class S>
 __device__ const BrickHalo<S> g_brick_halo = make_brick_halo<S>();
 
-// Brick cells in Morton order.  Word 0: tile index (11 bits), edge mask (6);
-// word 1: flux slots of the cell's -x, -y, -z faces (10 bits each).  The +x,
-// +y, +z faces are slots t, N + t, 2N + t.
+// Brick cells in Morton order, three words each.  Word 0: tile index (11
+// bits), edge mask (6); word 1: flux slots of the cell's -x, -y, -z faces (10
+// bits each; the +x, +y, +z faces are slots t, N + t, 2N + t); word 2:
+// face-value slots of the upper cells across the +x, +y, +z faces (their
+// - face values).
 template <class S>
 struct BrickCells {
-  uint32_t w[2 * S::N];
+  uint32_t w[3 * S::N];
 };
 template <class S>
 constexpr BrickCells<S> make_brick_cells() {
   BrickCells<S> C{};
-  for (int t = 0; t < S::N; ++t) {
+  constexpr int N = S::N;
+  for (int t = 0; t < N; ++t) {
     const int x = morton_x(t), y = morton_y(t), z = morton_z(t);
     const int mx = x > 0 ? morton_local(x - 1, y, z) : S::kSlotSideX + y + S::BY * z;
-    const int my = y > 0 ? S::N + morton_local(x, y - 1, z) : S::kSlotSideY + x + S::BX * z;
-    const int mz = z > 0 ? 2 * S::N + morton_local(x, y, z - 1) : S::kSlotSideZ + S::zslot(x, y);
-    C.w[2 * t] = uint32_t(S::tile_index(x, y, z)) | (S::edge_mask(x, y, z) << 11);
-    C.w[2 * t + 1] = uint32_t(mx) | (uint32_t(my) << 10) | (uint32_t(mz) << 20);
+    const int my = y > 0 ? N + morton_local(x, y - 1, z) : S::kSlotSideY + x + S::BX * z;
+    const int mz = z > 0 ? 2 * N + morton_local(x, y, z - 1) : S::kSlotSideZ + S::zslot(x, y);
+    const int px = x < S::BX - 1 ? morton_local(x + 1, y, z) : 3 * N + S::halo1_index(1, y, z);
+    const int py = y < S::BY - 1 ? N + morton_local(x, y + 1, z) : 3 * N + S::halo1_index(2, x, z);
+    const int pz = z < S::BZ - 1 ? 2 * N + morton_local(x, y, z + 1) : 3 * N + S::halo1_index(5, x, y);
+    C.w[3 * t] = uint32_t(S::tile_index(x, y, z)) | (S::edge_mask(x, y, z) << 11);
+    C.w[3 * t + 1] = uint32_t(mx) | (uint32_t(my) << 10) | (uint32_t(mz) << 20);
+    C.w[3 * t + 2] = uint32_t(px) | (uint32_t(py) << 10) | (uint32_t(pz) << 20);
   }
   return C;
 }
 template <class S>
 __device__ const BrickCells<S> g_brick_cells = make_brick_cells<S>();
 
+// Layer-1 halo cells in face-value slot order.  Packed: tile index (11
+// bits), axis (2), upper side (1: the cell's - face value is needed, else
+// its + face value), brick side (3).
+template <class S>
+struct BrickHalo1 {
+  uint32_t h[S::kHalo1];
+};
+template <class S>
+constexpr BrickHalo1<S> make_brick_halo1() {
+  BrickHalo1<S> H{};
+  const int sides[6] = {3, 1, 0, 2, 4, 5};
+  for (int k = 0; k < 6; ++k) {
+    const int side = sides[k];
+    const int axis = (side == 1 || side == 3) ? 0 : ((side == 0 || side == 2) ? 1 : 2);
+    const bool upper = side == 1 || side == 2 || side == 5;
+    const int ni = axis == 0 ? S::BY : S::BX, nj = axis == 2 ? S::BY : S::BZ;
+    const int o = upper ? (axis == 0 ? S::BX : (axis == 1 ? S::BY : S::BZ)) : -1;
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni; ++i) {
+        const int x = axis == 0 ? o : i, y = axis == 0 ? i : (axis == 1 ? o : j), z = axis == 2 ? o : j;
+        H.h[S::halo1_index(side, i, j)] = uint32_t(S::tile_index(x, y, z)) | (uint32_t(axis) << 11) |
+                                          (uint32_t(upper) << 13) | (uint32_t(side) << 14);
+      }
+  }
+  return H;
+}
+template <class S>
+__device__ const BrickHalo1<S> g_brick_halo1 = make_brick_halo1<S>();
+
+// Faces on the brick's lower sides, in flux-slot order (slot 3N + j).
+// Packed: face-value slot of the lower (halo) cell's + face value (10 bits),
+// of the upper (brick) cell's - face value (10), axis (2).
+template <class S>
+struct BrickSides {
+  uint32_t s[S::kSides];
+};
+template <class S>
+constexpr BrickSides<S> make_brick_sides() {
+  BrickSides<S> T{};
+  constexpr int N = S::N;
+  for (int j = 0; j < S::kSides; ++j) {
+    int axis = 0, lx = 0, ly = 0, lz = 0;
+    slot_lower_cell<S>(3 * N + j, axis, lx, ly, lz);
+    int lo = 0, hi = 0;
+    if (axis == 0) {
+      lo = 3 * N + S::halo1_index(3, ly, lz);
+      hi = morton_local(0, ly, lz);
+    } else if (axis == 1) {
+      lo = 3 * N + S::halo1_index(0, lx, lz);
+      hi = N + morton_local(lx, 0, lz);
+    } else {
+      lo = 3 * N + S::halo1_index(4, lx, ly);
+      hi = 2 * N + morton_local(lx, ly, 0);
+    }
+    T.s[j] = uint32_t(lo) | (uint32_t(hi) << 10) | (uint32_t(axis) << 20);
+  }
+  return T;
+}
+template <class S>
+__device__ const BrickSides<S> g_brick_sides = make_brick_sides<S>();
+
 // CFL radius of a brick cell: the frames are axis-aligned (checked at
 // upload), so |u.n| on face f is the magnitude of one velocity component --
 // the same value cell_lambda_with forms from the frame, without it.
 template <int MODEL>
-__device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float q[kNeqMax], uint32_t be,
+__device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float q[kNvMax], uint32_t be,
                                               const float (*geo)[2][4], float inv2vol) {
   FS s;
-  mixed_face_state<MODEL>(mc, q, false, s);
+  mixed_face_state<MODEL>(mc, q, s);
   const float au = fabsf(s.u), av = fabsf(s.v), aw = fabsf(s.w);
   float acc = 0.0f;
 #pragma unroll
@@ -1158,20 +1441,24 @@ __device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float 
 }
 
 template <int MODEL, bool MUSCL, bool NS, class S>
-__global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
+__global__ void __launch_bounds__(S::N, MODEL == 3 ? S::kMinBlocks3 : (NS ? S::kMinBlocksNS : S::kMinBlocks))
     k_mixed_brick(MixedConst mc, StageArgs a) {
-  constexpr int BX = S::BX, BY = S::BY, BZ = S::BZ, TX = S::TX, NB = S::N;
-  constexpr int kTile = S::kTile, kFaces = S::kFaces, kHalo = S::kHalo;
-  constexpr int kSlotSideY = S::kSlotSideY, kSlotSideZ = S::kSlotSideZ;
-  __shared__ float tile[kNeqMax][kTile];
-  __shared__ float flux[kNeqMax][kFaces];
-  __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area
+  constexpr int NV = kNv<MODEL>;
+  constexpr int TX = S::TX, NB = S::N;
+  constexpr int kTile = S::kTile, kFaces = S::kFaces, kHalo = S::kHalo, kHalo1 = S::kHalo1;
+  constexpr int kSides = S::kSides, kFvSlots = S::kFvSlots;
+  // the tile holds the stage state of the brick and its halo until every
+  // face value is formed, then the face fluxes [5][kFaces]
+  float(*tile)[kTile] = reinterpret_cast<float(*)[kTile]>(g_mixed_smem);
+  float(*fvb)[kFvSlots] = reinterpret_cast<float(*)[kFvSlots]>(g_mixed_smem + NV * kTile);  // face values handed on
+  float(*flux)[kFaces] = reinterpret_cast<float(*)[kFaces]>(g_mixed_smem);
+  __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area, k
+  __shared__ float s_area[3];       // face area per axis
   __shared__ float s_dtv, s_inv2vol;  // dt / V and 1 / (2 V) of the brick's level
   __shared__ int s_side[6];  // brick sides (indexed at run time: kept out of local memory)
   const BlockDesc *bdp = a.blocks + blockIdx.x;
   const int t = threadIdx.x;
   const int n = a.n;
-  constexpr bool muscl = MUSCL;
   const int start = __ldg(&bdp->start), level = __ldg(&bdp->level);
   const int c = start + t;
   uint32_t bmask = 0;  // sides of the brick on the domain boundary
@@ -1182,10 +1469,10 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   if (t < 12) {
     const int f = t >> 1, r = t & 1;
     const float *gf = geo_face(a.geo, level, f, r ? kRelBoundary : kRelSame);
-    s_geo[f][r][0] = gf[0];
-    s_geo[f][r][1] = gf[1];
-    s_geo[f][r][2] = gf[2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s_geo[f][r][k] = gf[k];
   }
+  if (t >= 12 && t < 15) s_area[t - 12] = a.geo->axis_area[level * 3 + (t - 12)];
   if (t == 0) {
     s_dtv = __double2float_rn(*a.dt) * a.geo->inv_vol[level];
     s_inv2vol = a.geo->inv2vol[level];
@@ -1207,255 +1494,247 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + int64_t(v) * n + start + 32 * l));
   }
   static_assert(kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes");
-  // A1: the brick's cells and the halo from the six neighbour bricks, copied
+  // 1: the brick's cells and the halo from the six neighbour bricks, copied
   // global -> shared asynchronously (cp.async, no register round trip)
-  {
-    const int ti = int(__ldg(&g_brick_cells<S>.w[2 * t]) & 2047u);
+  const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[3 * t]);
+  const int ti = int(cw0 & 2047u);
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
-  }
+  for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
 #pragma unroll
   for (int h = t; h < kHalo; h += NB) {
     const uint32_t e = __ldg(&g_brick_halo<S>.h[h]);
     const int base = __ldg(&bdp->side[(e >> 11) & 7u]);
     if (base >= 0) {
-      const int ti = int(e & 2047u), x = base + int(e >> 14);
+      const int hti = int(e & 2047u), x = base + int(e >> 14);
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + x);
+      for (int v = 0; v < NV; ++v) cp_async4(&tile[v][hti], a.Sin + v * n + x);
     }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
-  // A2: ghost values beyond domain-boundary sides (deltavalues.c:9-14): the
+  // ghost values beyond domain-boundary sides (deltavalues.c:9-14): the
   // ghost of the brick cell next to it, in both halo layers
   if (bmask) {
 #pragma unroll 1
-    for (int h = t; h < 2 * (BY * BZ + BX * BZ + BX * BY); h += NB) {
-      int side, bx, by, bz, sx = 0, sy = 0, sz = 0;
-      if (h < 2 * BY * BZ) {
-        side = h < BY * BZ ? 3 : 1;
-        const int rr = h % (BY * BZ);
-        by = rr % BY;
-        bz = rr / BY;
-        bx = side == 3 ? 0 : BX - 1;
-        sx = side == 3 ? -1 : 1;
-      } else if (h < 2 * BY * BZ + 2 * BX * BZ) {
-        const int hh = h - 2 * BY * BZ;
-        side = hh < BX * BZ ? 0 : 2;
-        const int rr = hh % (BX * BZ);
-        bx = rr % BX;
-        bz = rr / BX;
-        by = side == 0 ? 0 : BY - 1;
-        sy = side == 0 ? -1 : 1;
-      } else {
-        const int hh = h - 2 * BY * BZ - 2 * BX * BZ;
-        side = hh < BX * BY ? 4 : 5;
-        const int rr = hh % (BX * BY);
-        bx = rr % BX;
-        by = rr / BX;
-        bz = side == 4 ? 0 : BZ - 1;
-        sz = side == 4 ? -1 : 1;
-      }
-      if ((bmask >> side) & 1u) {
-        float own[kNeqMax], gv[kNeqMax];
-        const int ti_own = S::tile_index(bx, by, bz);
+    for (int h = t; h < kHalo1; h += NB) {
+      const uint32_t e = __ldg(&g_brick_halo1<S>.h[h]);
+      const int side = int((e >> 14) & 7u);
+      if (!((bmask >> side) & 1u)) continue;
+      const int ax = int((e >> 11) & 3u);
+      const int st = ax == 0 ? 1 : (ax == 1 ? TX : S::P);
+      const int sg = ((e >> 13) & 1u) ? st : -st;  // outward step
+      const int h1 = int(e & 2047u), own_ti = h1 - sg;
+      float own[kNvMax], gv[kNvMax];
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) own[v] = tile[v][ti_own];
-        boundary_value<MODEL>(mc, -1 - s_side[side], side, own, gv);
-        const int t1 = S::tile_index(bx + sx, by + sy, bz + sz), t2 = S::tile_index(bx + 2 * sx, by + 2 * sy, bz + 2 * sz);
+      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? tile[v][own_ti] : 0.0f;
+      boundary_value<MODEL>(mc, -1 - s_side[side], side, own, gv);
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) {
-          tile[v][t1] = gv[v];
-          tile[v][t2] = gv[v];
-        }
+      for (int v = 0; v < NV; ++v) {
+        tile[v][h1] = gv[v];
+        tile[v][h1 + sg] = gv[v];
       }
     }
     __syncthreads();  // bmask is uniform across the block
   }
 
-  // face value of the face g of the tile cell at ti (edge mask e), with the
-  // values across g at ti + dg and across the opposite face at ti - dg.
-  // EDGE: the brick has a side on the domain boundary.
-  auto recon_tile = [&](auto edge, int ti, uint32_t e, int g, int dg, float out[kNeqMax]) {
-    constexpr bool EDGE = decltype(edge)::value;
-    float qp[kNeqMax];
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) qp[v] = tile[v][ti];
-    if (!muscl) {
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) out[v] = qp[v];
-      return;
-    }
-    int rg = 0, ro = 0;
-    if (EDGE) {
-      const uint32_t be = e & bmask;
-      rg = (be >> g) & 1u;
-      ro = (be >> opp_face(g)) & 1u;
-    }
-    const float dcf = s_geo[g][rg][0], inv_p = s_geo[g][rg][1], inv_m = s_geo[opp_face(g)][ro][1];
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      const float d0 = tile[v][ti + dg] - qp[v];
-      const float d1 = tile[v][ti - dg] - qp[v];
-      out[v] = fmaf(dcf, minmod_slope(!rg, d0, d1, inv_p, inv_m), qp[v]);
-    }
-  };
-
-  // B: face tasks -- each face of the brick once
-  // viscous runs: the global index of a face task's cell (S::cell_ref)
-  // and the viscous normal flux of a face, subtracted as the general kernel
-  // does: (F - FV).n + FH
+  const uint32_t cw2 = __ldg(&g_brick_cells<S>.w[3 * t + 2]);
   auto cell_of = [&](uint32_t r) -> int {
     return (r & 2048u) ? s_side[(r >> 8) & 7u] + int(r & 255u) : start + int(r & 255u);
   };
-  auto sub_viscous = [&](int f, int bc, int clo, int chi, const float lo[kNeqMax], const float hi[kNeqMax],
-                         float Fn[kNeqMax]) {
-    float gl[9], gh[9], FVn[kNeqMax];
-    load_grad9f(a.SG, n, clo, gl);
-    load_grad9f(a.SG, n, chi, gh);
-    viscous_normal(mc, f, bc, lo, hi, gl, gh, FVn);
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
-  };
-  auto face_tasks = [&](auto edge) {
+  bool ok = true;
+  const uint32_t be = (cw0 >> 11) & 63u & bmask;
+  // 2-3 for a brick off the domain boundary (EDGE false) or on it
+  auto body = [&](auto edge) {
     constexpr bool EDGE = decltype(edge)::value;
-    bool fok = true;
-#pragma unroll 1
-    for (int task = t; task < kFaces; task += NB) {
-      const uint32_t e = __ldg(&g_brick_tasks<S>.task[task]);
-      const int ti = int(e & 2047u);
-      const int axis = int((e >> 11) & 3u);
-      const bool low_in = (e >> 13) & 1u, up_in = (e >> 14) & 1u;
-      const uint32_t elo = (e >> 15) & 63u, eup = (e >> 21) & 63u;
-      const int st = axis == 0 ? 1 : (axis == 1 ? TX : S::P);
-      const int fp = axis == 0 ? 1 : (axis == 1 ? 2 : 5);
-      const int fm = opp_face(fp);
-      float Fn[kNeqMax];
-      const int bside = low_in ? fp : fm;
-      if (EDGE && !(low_in && up_in) && s_side[bside] < 0) {
-        // the brick cell's own domain-boundary face, own frame (residual_faces_AMR.c:196-209)
-        float own[kNeqMax];
-        if (low_in)
-          recon_tile(edge, ti, elo, fp, st, own);
-        else
-          recon_tile(edge, ti + st, eup, fm, -st, own);
-        fok &= canonical_flux<MODEL>(mc, bside, -1 - s_side[bside], muscl, own, own, Fn);
-        if (NS) {
-          const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[task]);
-          const int cown = cell_of(low_in ? (cr & 4095u) : (cr >> 12));
-          sub_viscous(bside, -1 - s_side[bside], cown, cown, own, own, Fn);
-        }
-        if (!low_in) {  // stored as the +-face flux of the lower cell that is not there
+    // 2: face values.  Own cell: all six (one slope per axis); the + face
+    // values stay in registers, the - face values go to the slots.
+    float q[kNvMax];
 #pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
-        }
+    for (int v = 0; v < kNvMax; ++v) q[v] = v < NV ? tile[v][ti] : 0.0f;
+    float fpv[3][kNvMax];
+    auto own_axis = [&](auto axc) {
+      constexpr int AX = decltype(axc)::value;
+      constexpr int FP = plus_face(AX), FM = minus_face(AX);
+      constexpr int ST = AX == 0 ? 1 : (AX == 1 ? TX : S::P);
+      float nbp[kNvMax], nbm[kNvMax], fm[kNvMax];
+#pragma unroll
+      for (int v = 0; v < kNvMax; ++v) {
+        nbp[v] = v < NV ? tile[v][ti + ST] : 0.0f;
+        nbm[v] = v < NV ? tile[v][ti - ST] : 0.0f;
+      }
+      if (!MUSCL) {
+#pragma unroll
+        for (int v = 0; v < kNvMax; ++v) fpv[AX][v] = fm[v] = q[v];
+      } else if (EDGE && (be & ((1u << FP) | (1u << FM)))) {
+        const int rp = (be >> FP) & 1u, rm = (be >> FM) & 1u;
+        face_general<MODEL>(q, nbp, nbm, !rp, s_geo[FP][rp][0], s_geo[FP][rp][1], s_geo[FM][rm][1], fpv[AX]);
+        face_general<MODEL>(q, nbm, nbp, !rm, s_geo[FM][rm][0], s_geo[FM][rm][1], s_geo[FP][rp][1], fm);
       } else {
-        float lo[kNeqMax], hi[kNeqMax];
-        recon_tile(edge, ti, elo, fp, st, lo);
-        recon_tile(edge, ti + st, eup, fm, -st, hi);
-        fok &= canonical_flux<MODEL>(mc, fp, 0, muscl, lo, hi, Fn);
-        if (NS) {
-          const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[task]);
-          sub_viscous(fp, 0, cell_of(cr & 4095u), cell_of(cr >> 12), lo, hi, Fn);
-        }
+        axis_faces<MODEL>(q, nbp, nbm, s_geo[FP][0][3], fpv[AX], fm);
       }
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) flux[v][task] = Fn[v];
+      for (int v = 0; v < NV; ++v) fvb[v][AX * NB + t] = fm[v];
+    };
+    own_axis(std::integral_constant<int, 0>{});
+    own_axis(std::integral_constant<int, 1>{});
+    own_axis(std::integral_constant<int, 2>{});
+    // layer-1 halo cells: the one face value the brick needs
+#pragma unroll
+    for (int h = t; h < kHalo1; h += NB) {
+      const uint32_t e = __ldg(&g_brick_halo1<S>.h[h]);
+      if (!EDGE || !((bmask >> ((e >> 14) & 7u)) & 1u)) {
+        const int hti = int(e & 2047u), ax = int((e >> 11) & 3u);
+        const bool upper = (e >> 13) & 1u;
+        const int st = ax == 0 ? 1 : (ax == 1 ? TX : S::P);
+        float qh[kNvMax], nbp[kNvMax], nbm[kNvMax], out[kNvMax];
+#pragma unroll
+        for (int v = 0; v < kNvMax; ++v) {
+          qh[v] = v < NV ? tile[v][hti] : 0.0f;
+          nbp[v] = v < NV ? tile[v][hti + st] : 0.0f;
+          nbm[v] = v < NV ? tile[v][hti - st] : 0.0f;
+        }
+        if (!MUSCL) {
+#pragma unroll
+          for (int v = 0; v < kNvMax; ++v) out[v] = qh[v];
+        } else {
+          const float k = s_geo[plus_face(ax)][0][3];
+          if (upper)
+            axis_faces<MODEL, -1>(qh, nbp, nbm, k, out, out);
+          else
+            axis_faces<MODEL, 1>(qh, nbp, nbm, k, out, out);
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) fvb[v][3 * NB + h] = out[v];
+      }
     }
-    return fok;
-  };
-  // The same for a brick off the domain boundary: each thread its cell's +x,
-  // +y, +z faces (slots t, N + t, 2N + t), then the first threads the faces on
-  // the brick's lower sides; face index, stride and frame as compile-time
-  // constants (the axis is uniform across each warp of an 8x8x4 brick).
-  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  auto face_tasks_inner = [&]() {
-    bool fok = true;
-    const int ti_own = int(__ldg(&g_brick_cells<S>.w[2 * t]) & 2047u);
-    auto inner = [&](auto fpc, int ti, int slot, bool own) {
-      constexpr int FP = decltype(fpc)::value;
-      constexpr int ST = FP == 1 ? 1 : (FP == 2 ? TX : S::P);
-      float lo[kNeqMax], hi[kNeqMax], Fn[kNeqMax];
-      recon_tile(std::false_type{}, ti, 0u, FP, ST, lo);
-      recon_tile(std::false_type{}, ti + ST, 0u, opp_face(FP), -ST, hi);
-      fok &= canonical_flux<MODEL, FP>(mc, FP, 0, muscl, lo, hi, Fn);
-      if (NS) {
-        const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[slot]);
-        sub_viscous(FP, 0, cell_of(cr & 4095u), cell_of(cr >> 12), lo, hi, Fn);
+    __syncthreads();  // the tile is read for the last time above; it now takes the fluxes
+
+    // 3: fluxes of the own + faces and of the faces on the brick's lower sides
+    auto own_flux = [&](auto axc) {
+      constexpr int AX = decltype(axc)::value;
+      constexpr int FP = plus_face(AX);
+      float Fn[kNeqMax];
+      const int slot = AX * NB + t;
+      if (EDGE && ((be >> FP) & 1u)) {  // the cell's own domain-boundary face (residual_faces_AMR.c:196-209)
+        ok &= face_flux<MODEL, FP>(mc, a, FP, -1 - s_side[FP], MUSCL, fpv[AX], fpv[AX], c, c, Fn);
+      } else {
+        float hi[kNvMax];
+        const int hs = int((cw2 >> (10 * AX)) & 1023u);
+#pragma unroll
+        for (int v = 0; v < kNvMax; ++v) hi[v] = v < NV ? fvb[v][hs] : 0.0f;
+        int clo = c, chi = c;
+        if (NS) {
+          const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[slot]);
+          clo = cell_of(cr & 4095u);
+          chi = cell_of(cr >> 12);
+        }
+        ok &= face_flux<MODEL, FP>(mc, a, FP, 0, MUSCL, fpv[AX], hi, clo, chi, Fn);
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
-      if (own) {  // the cell's own + face: its first residual terms, in order
-        const float sA = -s_geo[FP][0][2];
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];
-      }
     };
-    inner(std::integral_constant<int, 1>{}, ti_own, t, true);
-    inner(std::integral_constant<int, 2>{}, ti_own, NB + t, true);
-    inner(std::integral_constant<int, 5>{}, ti_own, 2 * NB + t, true);
-    const int slot = 3 * NB + t;
-    if (slot < kFaces) {
-      const int ti = int(__ldg(&g_brick_tasks<S>.task[slot]) & 2047u);
-      if (slot < kSlotSideY)
-        inner(std::integral_constant<int, 1>{}, ti, slot, false);
-      else if (slot < kSlotSideZ)
-        inner(std::integral_constant<int, 2>{}, ti, slot, false);
-      else
-        inner(std::integral_constant<int, 5>{}, ti, slot, false);
+    own_flux(std::integral_constant<int, 0>{});
+    own_flux(std::integral_constant<int, 1>{});
+    own_flux(std::integral_constant<int, 2>{});
+#pragma unroll 1
+    for (int j = t; j < kSides; j += NB) {
+      const uint32_t e = __ldg(&g_brick_sides<S>.s[j]);
+      const int ax = int((e >> 20) & 3u);
+      const int fm = minus_face(ax);
+      float Fn[kNeqMax], lo[kNvMax], hi[kNvMax];
+      const int los = int(e & 1023u), his = int((e >> 10) & 1023u);
+#pragma unroll
+      for (int v = 0; v < kNvMax; ++v) hi[v] = v < NV ? fvb[v][his] : 0.0f;
+      if (EDGE && ((bmask >> fm) & 1u)) {
+        // the brick cell's own domain-boundary face, own frame, stored as the
+        // + face flux of the lower cell that is not there
+        const int cown = start + his % NB;
+        ok &= face_flux<MODEL>(mc, a, fm, -1 - s_side[fm], MUSCL, hi, hi, cown, cown, Fn);
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
+      } else {
+#pragma unroll
+        for (int v = 0; v < kNvMax; ++v) lo[v] = v < NV ? fvb[v][los] : 0.0f;
+        int clo = c, chi = c;
+        if (NS) {
+          const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[3 * NB + j]);
+          clo = cell_of(cr & 4095u);
+          chi = cell_of(cr >> 12);
+        }
+        if (ax == 0)
+          ok &= face_flux<MODEL, 1>(mc, a, 1, 0, MUSCL, lo, hi, clo, chi, Fn);
+        else if (ax == 1)
+          ok &= face_flux<MODEL, 2>(mc, a, 2, 0, MUSCL, lo, hi, clo, chi, Fn);
+        else
+          ok &= face_flux<MODEL, 5>(mc, a, 5, 0, MUSCL, lo, hi, clo, chi, Fn);
+      }
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) flux[v][3 * NB + j] = Fn[v];
     }
-    return fok;
   };
-  const bool ok = bmask ? face_tasks(std::true_type{}) : face_tasks_inner();
+  if (bmask)
+    body(std::true_type{});
+  else
+    body(std::false_type{});
   __syncthreads();
 
-  // C: gather in the fixed face order, RK stage update
-  const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[2 * t]), cw1 = __ldg(&g_brick_cells<S>.w[2 * t + 1]);
-  const uint32_t be = (cw0 >> 11) & 63u & bmask;
-  const int sx_m = int(cw1 & 1023u), sy_m = int((cw1 >> 10) & 1023u), sz_m = int(cw1 >> 20);
-  // order +x, +y, +z, -x, -y, -z as in the general kernel
-  auto add_face = [&](int f, int task, bool plus) {
-    const float A = s_geo[f][(be >> f) & 1u][2];
-    const float sA = plus ? -A : A;
+  // 4: residual axis by axis, x, y, z: R += A (F- - F+), then the RK stage update
+  const uint32_t cw1 = __ldg(&g_brick_cells<S>.w[3 * t + 1]);
+  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * flux[v][task];  // as the general kernel
-  };
-  if (bmask) {  // a brick off the domain boundary added its + faces already
-    add_face(1, t, true);
-    add_face(2, NB + t, true);
-    add_face(5, 2 * NB + t, true);
+  for (int ax = 0; ax < 3; ++ax) {
+    const int sm = int((cw1 >> (10 * ax)) & 1023u), sp = ax * NB + t;
+    const float A = s_area[ax];
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, flux[v][sm] - flux[v][sp], R[v]);
   }
-  add_face(3, sx_m, false);
-  add_face(0, sy_m, false);
-  add_face(4, sz_m, false);
-  float qn[kNeqMax], lam = 0.0f;
-  if (stage_update<MODEL>(mc, a, c, s_dtv, R, ok, qn) && a.lambda)
+  float qn[kNvMax], lam = 0.0f;
+  if (stage_update<MODEL>(a, c, s_dtv, R, ok, qn) && a.lambda)
     lam = brick_lambda<MODEL>(mc, qn, be, s_geo, s_inv2vol);
   if (a.last && a.lambda) block_max_lambda_f<NB>(lam, a.lambda);
 }
 
-// FP32 copy of an FP64 state (after an upload or an FP64-path step).
-// The first n values (the density) are shifted by off (model 3: kRhoOffD).
-__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count, int64_t n,
-                               double off) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-    Sf[i] = __double2float_rn(i < n ? S[i] - off : S[i]);
+// FP32 state words of an FP64 state (after an upload or an FP64-path
+// step), one cell per thread: the neq variables (model 3: the density
+// shifted by kRhoOffD, plus the low words of the density and of rho Y in
+// rows 5 and 6).
+template <int MODEL>
+__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t n, int neq) {
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
+    double x[kNeqMax];
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) x[v] = v < neq ? S[v * n + c] : 0.0;
+    float q[kNvMax];
+    to_state_f32<MODEL>(x, q);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v)
+      if (v < neq) Sf[v * n + c] = q[v];
+    if (MODEL == 3) {
+      Sf[5 * n + c] = q[5];
+      Sf[6 * n + c] = q[6];
+    }
+  }
 }
 
 // The same with the CFL spectral radius of the copied state (the mixed
-// path's first CFL time step after an upload): one cell per thread.
+// path's first CFL time step after an upload).
 template <int MODEL>
 __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, const int32_t *__restrict__ geom,
                                                                 const GeoTables *geo, const double *__restrict__ S,
                                                                 float *__restrict__ Sf, int n, double *lambda) {
   float lam = 0.0f;
   for (int c = blockIdx.x * kBlock + threadIdx.x; c < n; c += gridDim.x * kBlock) {
-    float q[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    double x[kNeqMax];
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      if (v >= mc.neq) break;
-      q[v] = to_state_f32<MODEL>(v, S[int64_t(v) * n + c]);
-      Sf[int64_t(v) * n + c] = q[v];
+    for (int v = 0; v < kNeqMax; ++v) x[v] = v < mc.neq ? S[int64_t(v) * n + c] : 0.0;
+    float q[kNvMax];
+    to_state_f32<MODEL>(x, q);
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v)
+      if (v < mc.neq) Sf[int64_t(v) * n + c] = q[v];
+    if (MODEL == 3) {
+      Sf[int64_t(5) * n + c] = q[5];
+      Sf[int64_t(6) * n + c] = q[6];
     }
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
@@ -1472,7 +1751,11 @@ MixedConst make_const(const Phys &ph) {
   mc.gpinf = float(ph.gamma * ph.pinf);
   mc.ylo = float(ph.ymin / 1000.0);
   mc.yhi = float(1.0 - ph.ymin / 1000.0);
-  for (int v = 0; v < kNeqMax; ++v) mc.inflow[v] = float(ph.inflow[v]);
+  // the inflow ghost in FP32 state form (the library accepts inflow
+  // boundaries for model 1 only, whose state form is the plain state)
+  for (int v = 0; v < kNeqMax; ++v)
+    mc.inflow[v] = float(ph.model == 3 && v == 0 ? ph.inflow[0] - kRhoOffD : ph.inflow[v]);
+  mc.inflow[5] = 0.0f;
   mc.model = ph.model;
   mc.neq = ph.neq;
   mc.ischeme = ph.ischeme;
@@ -1601,6 +1884,8 @@ bool brick_sides_resolve(const fvgpu_mesh_soa *m, int64_t i, const std::vector<c
 
 }  // namespace
 
+cudaError_t allow_smem_model(int model, bool muscl);  // defined with the launches below
+
 bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
   if (ph.model != 1 && ph.model != 3) {
     snprintf(why, whylen, "the mixed path implements models 1 and 3");
@@ -1633,6 +1918,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   GeoTables gt;
   memset(&gt, 0, sizeof gt);
   std::vector<char> seen(kGeoEntries, 0), seen_sub((kMaxLevel + 1) * 6, 0), seen_vol(kMaxLevel + 1, 0);
+  std::vector<char> seen_axis((kMaxLevel + 1) * 3, 0);
   std::vector<int32_t> geom(size_t(n), 0);
   for (int64_t c = 0; c < n; ++c) {
     const int lev = m->level[c];
@@ -1696,6 +1982,8 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       const float dcf = float(m->dcf[i]);
       const float inv_dcc = m->dcc[i] > 0.0 ? float(1.0 / m->dcc[i]) : __builtin_inff();
       const float area = rel == kRelFiner ? 0.0f : float(m->area[i]);
+      // the slope factor dist_cf / dist_cc of a face between two same-level cells
+      const float kf = rel == kRelSame ? float(m->dcf[i] / m->dcc[i]) : 0.0f;
       const int gi = geo_index(lev, f, rel);
       float *e = gt.face + gi * kGeoStride;
       if (!seen[gi]) {
@@ -1703,13 +1991,39 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         e[0] = dcf;
         e[1] = inv_dcc;
         e[2] = area;
-      } else if (e[0] != dcf || !(e[1] == inv_dcc) || e[2] != area) {
+        e[3] = kf;
+      } else if (e[0] != dcf || !(e[1] == inv_dcc) || e[2] != area || e[3] != kf) {
         snprintf(why, whylen, "the mixed path needs octree-regular geometry (cell %lld face %d)", (long long)c, f);
         return FVGPU_ERR_UNSUPPORTED;
+      }
+      // one area per level and axis for the single-neighbour faces (the
+      // residual sums A (F- - F+) per axis)
+      if (rel != kRelFiner) {
+        const int ai = lev * 3 + axis_of_face(f);
+        if (!seen_axis[ai]) {
+          seen_axis[ai] = 1;
+          gt.axis_area[ai] = area;
+        } else if (gt.axis_area[ai] != area) {
+          snprintf(why, whylen, "the mixed path needs equal areas of a cell's single-neighbour faces on an axis "
+                                "(cell %lld face %d)", (long long)c, f);
+          return FVGPU_ERR_UNSUPPORTED;
+        }
       }
     }
     geom[size_t(c)] = code;
   }
+  // the shared slope of a cell on an axis takes k from its + face: the two
+  // same-level faces of an axis have the same dist_cf and dist_cc
+  for (int lev = 0; lev <= kMaxLevel; ++lev)
+    for (int ax = 0; ax < 3; ++ax) {
+      const int ip = geo_index(lev, plus_face(ax), kRelSame), im = geo_index(lev, minus_face(ax), kRelSame);
+      if (!seen[ip] || !seen[im]) continue;
+      const float *ep = gt.face + ip * kGeoStride, *em = gt.face + im * kGeoStride;
+      if (ep[0] != em[0] || ep[1] != em[1] || ep[3] != em[3]) {
+        snprintf(why, whylen, "the mixed path needs the same cell spacing on both sides of an axis (level %d)", lev);
+        return FVGPU_ERR_UNSUPPORTED;
+      }
+    }
   // bricks: same-level Morton blocks (candidates), kept when each of their
   // six sides is a domain boundary or another candidate block of the same
   // shape, whichever kernel evaluates that block (its cells only supply the
@@ -1770,10 +2084,15 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     d.count = cnt;
     general.push_back(d);
   }
+  const int nv = ph.model == 3 ? kNv<3> : kNv<1>;  // FP32 state words per cell
   std::vector<BlockDesc> all(bricks);
   all.insert(all.end(), bricks4.begin(), bricks4.end());
   all.insert(all.end(), general.begin(), general.end());
   cudaError_t e;
+  if ((e = allow_smem_model(ph.model, ph.ischeme == 2)) != cudaSuccess) {
+    snprintf(why, whylen, "shared-memory opt-in of the mixed kernels: %s", cudaGetErrorString(e));
+    return FVGPU_ERR_CUDA;
+  }
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = alloc_slot(r, kBufTables, sizeof(GeoTables))) != cudaSuccess ||
@@ -1784,10 +2103,10 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       (e = alloc_slot(r, kBufD1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNf, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX1, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX2, sizeof(float) * nv * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufSG, ph.ns == 1 ? sizeof(float) * 9 * n : 16)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
@@ -1846,8 +2165,11 @@ void mixed_swap_state(MixedResources &r, void *&state) {
 
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
   marks.mark(FVGPU_KIND_MIXED_AUX);
-  k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n, r.n,
-                                       r.model == 3 ? kRhoOffD : 0.0);
+  float *Sf = static_cast<float *>(r.buf[kBufSNf]);
+  if (r.model == 3)
+    k_state_to_f32<3><<<1024, 256, 0, st>>>(S, Sf, r.n, neq);
+  else
+    k_state_to_f32<1><<<1024, 256, 0, st>>>(S, Sf, r.n, neq);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;
@@ -1873,14 +2195,43 @@ cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const do
 // the kernel instance of the configuration (EOS model, reconstruction order)
 template <int MODEL, bool MUSCL, class S>
 void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
+  constexpr size_t smem = S::template smem_bytes<kNv<MODEL>>();
   if (mc.ns == 1) {
-    if constexpr (MODEL == 1) k_mixed_brick<MODEL, MUSCL, true, S><<<grid, S::N, 0, st>>>(mc, a);
+    if constexpr (MODEL == 1) k_mixed_brick<MODEL, MUSCL, true, S><<<grid, S::N, smem, st>>>(mc, a);
   } else {
-    k_mixed_brick<MODEL, MUSCL, false, S><<<grid, S::N, 0, st>>>(mc, a);
+    k_mixed_brick<MODEL, MUSCL, false, S><<<grid, S::N, smem, st>>>(mc, a);
   }
 }
 
 enum BlockKind { kKindGeneral = 0, kKindBrick8 = 1, kKindBrick4 = 2 };
+
+// Dynamic shared memory above the 48 KiB default needs a per-kernel opt-in
+// (cudaFuncAttributeMaxDynamicSharedMemorySize); set it for every stage
+// kernel of the model before any launch or stream capture.
+template <class K>
+cudaError_t allow_smem(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(reinterpret_cast<const void *>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(bytes));
+}
+template <int MODEL, bool MUSCL>
+cudaError_t allow_smem_instance() {
+  cudaError_t e = allow_smem(k_mixed_general<MODEL, MUSCL>, general_smem_bytes<MODEL>());
+  if (e == cudaSuccess)
+    e = allow_smem(k_mixed_brick<MODEL, MUSCL, false, Brick8>, Brick8::template smem_bytes<kNv<MODEL>>());
+  if (e == cudaSuccess)
+    e = allow_smem(k_mixed_brick<MODEL, MUSCL, false, Brick4>, Brick4::template smem_bytes<kNv<MODEL>>());
+  if constexpr (MODEL == 1) {
+    if (e == cudaSuccess)
+      e = allow_smem(k_mixed_brick<MODEL, MUSCL, true, Brick8>, Brick8::template smem_bytes<kNv<MODEL>>());
+    if (e == cudaSuccess)
+      e = allow_smem(k_mixed_brick<MODEL, MUSCL, true, Brick4>, Brick4::template smem_bytes<kNv<MODEL>>());
+  }
+  return e;
+}
+cudaError_t allow_smem_model(int model, bool muscl) {
+  if (model == 1) return muscl ? allow_smem_instance<1, true>() : allow_smem_instance<1, false>();
+  return muscl ? allow_smem_instance<3, true>() : allow_smem_instance<3, false>();
+}
 
 template <int MODEL, bool MUSCL>
 void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
@@ -1889,7 +2240,7 @@ void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageA
   else if (kind == kKindBrick4)
     launch_brick<MODEL, MUSCL, Brick4>(grid, mc, a, st);
   else
-    k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+    k_mixed_general<MODEL, MUSCL><<<grid, kBlock, general_smem_bytes<MODEL>(), st>>>(mc, a);
 }
 
 void launch_kernel(const Phys &ph, int kind, unsigned grid, const MixedConst &mc, const StageArgs &a,
