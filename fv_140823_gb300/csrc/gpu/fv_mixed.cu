@@ -41,31 +41,20 @@
 // upload), compiled in as signed permutations: rotating the momentum into
 // and out of a face frame is a choice of registers.
 //
-// Two kernels share those definitions:
-//   k_mixed_brick    a Morton-aligned 8x8x4 (or, on AMR meshes, 4x4x4)
-//                    brick of same-level cells whose six sides are same-level
-//                    blocks of that shape or domain boundaries: brick +
-//                    2-deep face halo staged in shared memory through
-//                    constant index tables; each cell forms its six face
-//                    values once (one slope per axis), the halo cells next to
-//                    the brick the one face value the brick needs; each
-//                    thread then evaluates its cell's +x, +y, +z faces and the
-//                    first threads the faces on the brick's lower sides; no
-//                    neighbour tables are read; viscous runs (model 1) read
-//                    the two cells' gradients of each face;
-//   k_mixed_general  any other run of up to 256 consecutive cells (AMR
-//                    interfaces, 1:4 faces): table-driven, each thread
-//                    computes its + faces and publishes them, the upper cell
-//                    reuses them or recomputes the canonical flux across
-//                    block edges and 1:4 sub-faces.
-// A cell's result does not depend on which kernel handled it (tests compare
-// the two bit for bit).  Both keep their large shared arrays in dynamic
-// shared memory, opted in per kernel above the 48 KiB default.
-//
-// Model 3 (two-phase mixture) keeps the density as two FP32 words, rho -
-// rho_sat and its rounding remainder: differences between cells, face
-// values and the FP64 pressure inversion see the density to ~1e-14 of the
-// liquid value, while the FP32 flux arithmetic uses its FP32 rounding.
+// The kernel, k_mixed_brick, serves model-1 meshes that are Morton-aligned
+// 8x8x4 bricks of same-level cells throughout (uniform octrees: the 128^3
+// periodic case, the Sod tube), one brick per 256-thread block: the brick
+// and its 2-deep face halo are staged in shared memory through constant
+// index tables; each cell forms its six face values once (one slope per
+// axis) and the halo cells next to the brick the one face value the brick
+// needs; each thread then evaluates its cell's +x, +y, +z faces and the
+// first threads the faces on the brick's lower sides; no neighbour tables
+// are read; viscous runs read the two cells' gradients of each face.  Its
+// tile and face-value slots live in dynamic shared memory (opted in above
+// the 48 KiB default).  Every other mesh (AMR, model 3, FVGPU_FLAG_NO_BRICKS)
+// runs the table-driven family of fv_mixed_amr.cu; the family is chosen
+// once per mesh, so a context's results do not depend on how its cells are
+// split into blocks.
 //
 // Geometry comes from per-level tables (octree-regular meshes): a packed
 // per-cell code (level + face relations) replaces the FP64 face tables.
@@ -104,14 +93,12 @@ __host__ __device__ constexpr int plus_face(int a) { return a == 0 ? 1 : (a == 1
 __host__ __device__ constexpr int minus_face(int a) { return a == 0 ? 3 : (a == 1 ? 0 : 4); }
 __host__ __device__ constexpr int axis_of_face(int f) { return (f == 1 || f == 3) ? 0 : ((f == 0 || f == 2) ? 1 : 2); }
 
-// Number of FP32 words of the state vector: model 3 adds the low words of
-// the density and of the gas partial density (rows 5 and 6).
+// FP32 words of the state vector: the five conservative variables of
+// model 1 (this file serves model 1; model 3 runs in fv_mixed_amr.cu).
 template <int MODEL>
-constexpr int kNv = MODEL == 3 ? 7 : 5;
-constexpr int kNvMax = 7;
-// the low word of variable v (model 3: density -> 5, rho Y -> 6), else -1
-template <int MODEL>
-__host__ __device__ constexpr int lo_word(int v) { return MODEL == 3 ? (v == 0 ? 5 : (v == 4 ? 6 : -1)) : -1; }
+constexpr int kNv = 5;
+constexpr int kNvMax = 5;
+static_assert(kNvMax == kNeqMax, "model 1 state words");
 
 // FP32 constants, converted once on the host.
 struct MixedConst {
@@ -174,106 +161,27 @@ __device__ __forceinline__ float fast_sqrt(float x) {
   asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
-// rounding error of s = a + b (Knuth's two-sum, exact in round-to-nearest)
-__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
-  const float bb = s - a;
-  return (a - (s - bb)) + (b - bb);
-}
-
-// Density in the FP32 state vectors.  Model 3 (liquid-gas mixture) stores
-// rho - kRhoOff in word 0 and the remainder rho - kRhoOff - word0 in word 5,
-// kRhoOff the saturation density of the mixture EOS (barotropic_eos.c:41, as
-// an FP32 value): near the liquid density an FP32 ulp of rho itself is 6e-5,
-// which the stiff liquid branch turns into ~130 Pa, and the gas density (~1)
-// stored as rho - kRhoOff carries the ulp of ~1000 (~5 Pa of gas pressure);
-// the two words together hold rho to ~1e-14 of 1000.  The gas partial
-// density rho Y gets a low word too (word 4 + word 6): a bubbly liquid's
-// pressure moves by ~3e7 Pa per kg/m^3 of rho Y, so an FP32 rounding of rho
-// Y ~ 3e-3 alone is worth ~0.006 Pa.  Model 1 stores its five variables.
-constexpr float kRhoOffF = 998.1618f;
-constexpr double kRhoOffD = double(kRhoOffF);
 template <int MODEL>
-__device__ __forceinline__ float state_rho(const float *q) { return MODEL == 3 ? q[0] + kRhoOffF : q[0]; }
-// the density as FP64: model 3 from both words (exact sum of the three terms)
-template <int MODEL>
-__device__ __forceinline__ double state_rho_d(const float *q) {
-  if constexpr (MODEL == 3) return (kRhoOffD + double(q[0])) + double(q[5]);
-  return double(q[0]);
-}
-__device__ __forceinline__ float state_rho_rt(int model, float q0) { return model == 3 ? q0 + kRhoOffF : q0; }
-// FP32 state words of an FP64 state: v < 5 variable v (density shifted for
-// model 3); model 3 word 5 = rounding remainder of word 0, else 0
+__device__ __forceinline__ float state_rho(const float *q) { return q[0]; }
+__device__ __forceinline__ float state_rho_rt(int, float q0) { return q0; }
+// FP32 state words of an FP64 state
 template <int MODEL>
 __device__ __forceinline__ void to_state_f32(const double x[kNeqMax], float q[kNvMax]) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) q[v] = __double2float_rn(MODEL == 3 && v == 0 ? x[0] - kRhoOffD : x[v]);
-  q[5] = MODEL == 3 ? __double2float_rn((x[0] - kRhoOffD) - double(q[0])) : 0.0f;  // both subtractions exact
-  q[6] = MODEL == 3 ? __double2float_rn(x[4] - double(q[4])) : 0.0f;
+  for (int v = 0; v < kNeqMax; ++v) q[v] = __double2float_rn(x[v]);
 }
 
-// d = a - b on the state words; model 3: the density difference with the
-// low words (accurate to the rounding of the difference itself)
+// d = a - b on the state words
 template <int MODEL>
 __device__ __forceinline__ void state_diff(const float a[kNvMax], const float b[kNvMax], float d[kNeqMax]) {
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) d[v] = a[v] - b[v];
-  if constexpr (MODEL == 3) {
-    d[0] = d[0] + (a[5] - b[5]);
-    d[4] = d[4] + (a[6] - b[6]);
-  }
 }
-// out = q + c s per variable (one fused multiply-add); model 3: the density
-// word with its rounding carried into the low word
+// out = q + c s per variable (one fused multiply-add)
 template <int MODEL>
 __device__ __forceinline__ void add_slope(const float q[kNvMax], float c, const float s[kNeqMax], float out[kNvMax]) {
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) out[v] = fmaf(c, s[v], q[v]);
-  out[5] = q[5];
-  out[6] = q[6];
-  if constexpr (MODEL == 3) {
-#pragma unroll
-    for (int v = 0; v < kNeqMax; v += 4) {  // the density and rho Y
-      const int lo = lo_word<MODEL>(v);
-      const float p = c * s[v];
-      out[v] = q[v] + p;
-      out[lo] = q[lo] + two_sum_err(q[v], p, out[v]);
-    }
-  }
-}
-
-// The two-phase mixture EOS of barotropic_eos.c:32-129 (the pressure root of
-// a quadratic, liquid sound speed with a fallback) written on the gas
-// partial density ry = rho Y instead of the mass fraction: the reference's
-// products rho Y and rho (1 - Y) become ry and rho - ry.  The pressure of a
-// bubbly liquid is stiff in the liquid partial density (dp ~ c_liq^2 d(rho -
-// rho Y)), and forming Y = rho Y / rho in FP32 and multiplying it back by rho
-// loses ~1e-7 of rho Y relative to rho: ~0.5 Pa at Y ~ 3e-6.  From the state
-// words directly the inversion sees both partial densities to FP64 rounding
-// of FP32 data.  FP64 throughout; false when neither branch has a real root.
-__device__ __forceinline__ bool eos_mixture_partial(double r, double ry, double &p_out, double &c_out) {
-  const double R_G = 286.0, T_ref = 293.15, r_sat = 998.1618, p_sat = 2340.0;
-  const double c_liq = 1482.5, c_mixture = 1.0;
-  const double rg = ry * R_G * T_ref, rl = r - ry;
-  double c2 = c_liq * c_liq;
-  double b = c2 * r_sat - p_sat - rg - rl * c2;
-  double d = (p_sat - c2 * r_sat) * rg;
-  double disc = b * b - 4.0 * d;
-  double ct = c_liq;
-  if (!(disc >= 0.0)) {
-    ct = c_mixture;
-    c2 = c_mixture * c_mixture;
-    b = c2 * r_sat - p_sat - rg - rl * c2;
-    d = (p_sat - c2 * r_sat) * rg;
-    disc = b * b - 4.0 * d;
-    if (!(disc >= 0.0)) {
-      p_out = __longlong_as_double(0x7ff8000000000000ll);
-      c_out = ct;
-      return false;
-    }
-  }
-  p_out = 0.5 * (-b + sqrt(disc));  // the larger root
-  c_out = ct;
-  return true;
 }
 
 // FP32 face state in the Cartesian frame (facevalues.c:113-142): the CFL
@@ -283,22 +191,15 @@ struct FS {
 };
 template <int MODEL>
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, FS &s) {
-  s.r = MODEL == 3 ? float(state_rho_d<MODEL>(q)) : q[0];
+  s.r = q[0];
   const float rinv = fast_rcp(s.r);
   s.u = q[1] * rinv;
   s.v = q[2] * rinv;
   s.w = q[3] * rinv;
-  if (MODEL == 1) {
-    const float msq = fmaf(q[3], q[3], fmaf(q[2], q[2], q[1] * q[1]));
-    s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, rinv, q[4]), -mc.gpinf);
-    s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * rinv);
-    return true;
-  }
-  double p, c;
-  const bool ok = eos_mixture_partial(state_rho_d<MODEL>(q), double(q[4]) + double(q[6]), p, c);
-  s.p = float(p);
-  s.c = float(c);
-  return ok;
+  const float msq = fmaf(q[3], q[3], fmaf(q[2], q[2], q[1] * q[1]));
+  s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, rinv, q[4]), -mc.gpinf);
+  s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * rinv);
+  return true;
 }
 
 // Value across a boundary face (deltavalues.c:9-14; bc.c:19-49): the own
@@ -334,7 +235,7 @@ __device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int
 struct LS {
   float r, rinv, mn, mm, ml;  // density, its reciprocal, local momentum
   float un;                   // normal velocity
-  float p, c, e, y;           // pressure, sound speed, energy (model 1), mass fraction (model 3)
+  float p, c, e, y;           // pressure, sound speed, energy, (unused) mass fraction
 };
 
 // Face frames of the reference's hexahedral cells (tagvector.c:40-53 on
@@ -418,39 +319,19 @@ __device__ __forceinline__ void frame_out(int f, float a, float b, float c, floa
 }
 
 template <int MODEL, int F = -1>
-__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float *q, bool clip, LS &s) {
+__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float *q, bool, LS &s) {
+  static_assert(MODEL == 1, "model 1 face states");
   frame_in<F>(f, q, s.mn, s.mm, s.ml);
-  if (MODEL == 1) {
-    s.r = q[0];
-    s.rinv = fast_rcp(s.r);
-    s.un = s.mn * s.rinv;
-    s.e = q[4];
-    s.y = 0.0f;
-    // p = (gamma - 1) (E - |m|^2 / (2 rho)) - gamma pinf, c^2 = gamma (p + pinf) / rho
-    const float msq = fmaf(s.ml, s.ml, fmaf(s.mm, s.mm, s.mn * s.mn));
-    s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, s.rinv, s.e), -mc.gpinf);
-    s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * s.rinv);
-    return true;
-  }
-  // model 3: the FP64 pressure inversion on the density from both state
-  // words and the gas partial density rho Y (clipped as facercnstr.c:43-44
-  // clips Y)
-  const double r64 = state_rho_d<MODEL>(q);
-  s.r = float(r64);
+  s.r = q[0];
   s.rinv = fast_rcp(s.r);
   s.un = s.mn * s.rinv;
-  s.e = 0.0f;
-  double ry = double(q[4]) + double(q[6]);
-  if (clip) {
-    ry = ry < double(mc.ylo) * r64 ? double(mc.ylo) * r64 : ry;
-    ry = ry > double(mc.yhi) * r64 ? double(mc.yhi) * r64 : ry;
-  }
-  s.y = float(ry) * s.rinv;
-  double p, c;
-  const bool ok = eos_mixture_partial(r64, ry, p, c);
-  s.p = float(p);
-  s.c = float(c);
-  return ok;
+  s.e = q[4];
+  s.y = 0.0f;
+  // p = (gamma - 1) (E - |m|^2 / (2 rho)) - gamma pinf, c^2 = gamma (p + pinf) / rho
+  const float msq = fmaf(s.ml, s.ml, fmaf(s.mm, s.mm, s.mn * s.mn));
+  s.p = fmaf(mc.gm1, fmaf(-0.5f * msq, s.rinv, s.e), -mc.gpinf);
+  s.c = fast_sqrt(fmaf(mc.gamma, s.p, mc.gpinf) * s.rinv);
+  return true;
 }
 
 // Ghost of a boundary face in the face-local frame (bc.c:19-49): inflow
@@ -588,34 +469,6 @@ __device__ __forceinline__ void face_general(const float q[kNvMax], const float 
   add_slope<MODEL>(q, dcf, s, out);
 }
 
-// Both face values of a cell with geometry code gx on axis ax from the values
-// across its + and - faces: the shared slope where both neighbours have the
-// cell's level, the per-face form otherwise.  WHICH as in axis_faces.
-template <int MODEL, bool MUSCL, int WHICH = 0>
-__device__ __forceinline__ void cell_axis_faces(const GeoTables *geo, int32_t gx, int ax, const float q[kNvMax],
-                                                const float nbp[kNvMax], const float nbm[kNvMax], float fp[kNvMax],
-                                                float fm[kNvMax]) {
-  if (!MUSCL) {
-#pragma unroll
-    for (int v = 0; v < kNvMax; ++v) {
-      if (WHICH >= 0) fp[v] = q[v];
-      if (WHICH <= 0) fm[v] = q[v];
-    }
-    return;
-  }
-  const int lev = level_of(gx);
-  const int f1 = plus_face(ax), f0 = minus_face(ax);
-  const int r1 = rel_of(gx, f1), r0 = rel_of(gx, f0);
-  const float *g1 = geo_face(geo, lev, f1, r1);
-  if (r1 == kRelSame && r0 == kRelSame) {
-    axis_faces<MODEL, WHICH>(q, nbp, nbm, g1[3], fp, fm);
-    return;
-  }
-  const float *g0 = geo_face(geo, lev, f0, r0);
-  if (WHICH >= 0) face_general<MODEL>(q, nbp, nbm, r1 != kRelBoundary, g1[0], g1[1], g0[1], fp);
-  if (WHICH <= 0) face_general<MODEL>(q, nbm, nbp, r0 != kRelBoundary, g0[0], g0[1], g1[1], fm);
-}
-
 template <int NT = kBlock>  // threads of the block
 __device__ __forceinline__ void block_max_lambda_f(float lam, double *out) {
   __shared__ float red[NT / 32];
@@ -703,10 +556,6 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
     const float sn = __ldg(a.SNf + v * n + c);
     const float x = sn + dn[v];  // the value the next stage would form
     a.Sout[v * n + c] = x;
-    if (lo_word<MODEL>(v) >= 0) {
-      const int lo = lo_word<MODEL>(v);
-      a.Sout[lo * n + c] = __ldg(a.SNf + lo * n + c) + two_sum_err(sn, dn[v], x);
-    }
   }
   return false;
 }
@@ -878,256 +727,8 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
   for (int i = 0; i < 9; ++i) SGout[i * n + c] = gr[i];
 }
 
-// ============================ general kernel ================================
-
-// Shared memory of the general kernel: the block's stage states st[nv][256],
-// its cells' six face values sf[6][nv][256] and per axis the published +
-// face fluxes fpub[3][5][256].
-template <int MODEL>
-constexpr size_t general_smem_bytes() {
-  return sizeof(float) * kBlock * (7 * kNv<MODEL> + 3 * kNeqMax);
-}
-
-template <int MODEL>
-struct Block {
-  static constexpr int NV = kNv<MODEL>;
-  const StageArgs &a;
-  const MixedConst &mc;
-  int c0, cnt;
-  const float (*st)[kBlock];
-  const float (*sf)[NV][kBlock];
-  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock],
-                   const float (*sf_)[NV][kBlock])
-      : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_), sf(sf_) {}
-  __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(cnt); }
-  __device__ __forceinline__ void state(int x, float q[kNvMax]) const {
-    if (in_block(x)) {
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) q[v] = v < NV ? st[v][x - c0] : 0.0f;
-      return;
-    }
-    global_state<MODEL>(a, x, q);
-  }
-  // value across face f of cell x (deltavalues.c): single neighbour, mean of
-  // the four fine ones, or the boundary ghost
-  __device__ __forceinline__ void across(int x, int f, const float own[kNvMax], float nb[kNvMax]) const {
-    const int32_t code = __ldg(a.nbr + f * a.n + x);
-    if (code >= 0) {
-      state(code, nb);
-    } else if (is_hanging(code)) {
-      const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-      float acc[kNvMax] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-      for (int s = 0; s < 4; ++s) {
-        float q[kNvMax];
-        state(__ldg(k + s), q);
-        if constexpr (MODEL == 3) {  // paired words summed with the rounding carried into the low word
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) {
-            const int lo = lo_word<MODEL>(v);
-            if (lo >= 0) {
-              const float sv = acc[v] + q[v];
-              acc[lo] = acc[lo] + (two_sum_err(acc[v], q[v], sv) + q[lo]);
-              acc[v] = sv;
-            } else {
-              acc[v] += q[v];
-            }
-          }
-        } else {
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
-        }
-      }
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) nb[v] = 0.25f * acc[v];
-    } else {
-      boundary_value<MODEL>(mc, -1 - code, f, own, nb);
-    }
-  }
-  // face value of face f of cell x: the block's table when x is in the
-  // block, else recomputed from global memory (across block edges)
-  template <bool MUSCL>
-  __device__ __forceinline__ void face_value(int x, int f, float out[kNvMax]) const {
-    if (in_block(x)) {
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) out[v] = v < NV ? sf[f][v][x - c0] : 0.0f;
-      return;
-    }
-    float q[kNvMax];
-    state(x, q);
-    if (!MUSCL) {
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) out[v] = q[v];
-      return;
-    }
-    const int ax = axis_of_face(f);
-    float nbp[kNvMax], nbm[kNvMax], unused[kNvMax];
-    across(x, plus_face(ax), q, nbp);
-    across(x, minus_face(ax), q, nbm);
-    const int32_t gx = __ldg(a.geom + x);
-    if (f == plus_face(ax))
-      cell_axis_faces<MODEL, true, 1>(a.geo, gx, ax, q, nbp, nbm, out, unused);
-    else
-      cell_axis_faces<MODEL, true, -1>(a.geo, gx, ax, q, nbp, nbm, unused, out);
-  }
-};
-
 // dynamic shared memory of the kernels (16-byte aligned)
 extern __shared__ __align__(16) float g_mixed_smem[];
-
-// model 3 (FP64 pressure inversion, six state words) runs two blocks per SM
-// with up to 128 registers, model 1 four with 64; neither spills
-template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(MixedConst mc, StageArgs a) {
-  constexpr int NV = kNv<MODEL>;
-  float(*st)[kBlock] = reinterpret_cast<float(*)[kBlock]>(g_mixed_smem);
-  float(*sf)[NV][kBlock] = reinterpret_cast<float(*)[NV][kBlock]>(g_mixed_smem + NV * kBlock);
-  float(*fpub)[kNeqMax][kBlock] = reinterpret_cast<float(*)[kNeqMax][kBlock]>(g_mixed_smem + 7 * NV * kBlock);
-  __shared__ float s_dt;
-  const BlockDesc bd = a.blocks[blockIdx.x];
-  const int t = threadIdx.x;
-  const int c0 = bd.start;
-  const int c = c0 + t;
-  const int n = a.n;
-  const bool active = t < bd.count;
-  const Block<MODEL> blk(a, mc, c0, bd.count, st, sf);
-
-  // A: own stage state
-  float q[kNvMax];
-#pragma unroll
-  for (int v = 0; v < kNvMax; ++v) {
-    q[v] = (active && v < NV) ? __ldg(a.Sin + v * n + c) : 0.0f;
-    if (v < NV) st[v][t] = q[v];
-  }
-  int32_t nb[6];
-  int32_t g = 0;
-#pragma unroll
-  for (int f = 0; f < 6; ++f) nb[f] = active ? __ldg(a.nbr + f * n + c) : -3;
-  if (active) g = __ldg(a.geom + c);
-  if (t == 0) s_dt = __double2float_rn(*a.dt);
-  __syncthreads();
-
-  // B: own face values, axis by axis
-  if (active) {
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      float nbp[kNvMax], nbm[kNvMax], fpv[kNvMax], fmv[kNvMax];
-      if (MUSCL) {
-        blk.across(c, plus_face(ax), q, nbp);
-        blk.across(c, minus_face(ax), q, nbm);
-      }
-      cell_axis_faces<MODEL, MUSCL>(a.geo, g, ax, q, nbp, nbm, fpv, fmv);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        sf[plus_face(ax)][v][t] = fpv[v];
-        sf[minus_face(ax)][v][t] = fmv[v];
-      }
-    }
-  }
-  __syncthreads();
-
-  const int lev = level_of(g);
-  bool ok = true;
-  // C1: + faces.  fpub[ax][.][t] receives the flux of a single-neighbour +
-  // face (read by the upper cell when it is in the block) or, for a boundary
-  // or 1:4 face, its contribution T+ (read back by this thread only).
-  if (active) {
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const int f = plus_face(ax), fo = minus_face(ax);
-      const int32_t code = nb[f];
-      float own[kNvMax], Fn[kNeqMax], T[kNeqMax];
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? sf[f][v][t] : 0.0f;
-      if (is_boundary(code)) {
-        ok &= face_flux<MODEL>(mc, a, f, -1 - code, MUSCL, own, own, c, c, T);
-      } else if (is_hanging(code)) {
-        const int32_t *hk = a.hang_nbr + 4 * hang_index(code);
-        const float A = a.geo->sub_area[lev * 6 + f];
-#pragma unroll 1
-        for (int s = 0; s < 4; ++s) {
-          const int other = __ldg(hk + s);
-          float hi[kNvMax];
-          blk.template face_value<MUSCL>(other, fo, hi);
-          ok &= face_flux<MODEL>(mc, a, f, 0, MUSCL, own, hi, c, other, Fn);
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) T[v] = s == 0 ? A * Fn[v] : T[v] + A * Fn[v];
-        }
-      } else {
-        float hi[kNvMax];
-        blk.template face_value<MUSCL>(code, fo, hi);
-        ok &= face_flux<MODEL>(mc, a, f, 0, MUSCL, own, hi, c, code, T);
-      }
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) fpub[ax][v][t] = T[v];
-    }
-  }
-  __syncthreads();
-
-  // C2: - faces (published fluxes reused) and the residual, axis by axis
-  float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  if (active) {
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const int f = minus_face(ax), fo = plus_face(ax);
-      const int32_t code = nb[f];
-      float own[kNvMax], Tm[kNeqMax], Fn[kNeqMax];
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? sf[f][v][t] : 0.0f;
-      const bool hang_m = is_hanging(code), hang_p = is_hanging(nb[fo]);
-      if (is_boundary(code)) {
-        // the cell's own boundary face in its own frame; canonical orientation is -1 times that
-        ok &= face_flux<MODEL>(mc, a, f, -1 - code, MUSCL, own, own, c, c, Fn);
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) Tm[v] = -Fn[v];
-      } else if (hang_m) {
-        const int32_t *hk = a.hang_nbr + 4 * hang_index(code);
-        const float A = a.geo->sub_area[lev * 6 + f];
-#pragma unroll 1
-        for (int s = 0; s < 4; ++s) {
-          const int other = __ldg(hk + s);
-          if (blk.in_block(other)) {  // the fine cell's + face has this cell alone: published
-#pragma unroll
-            for (int v = 0; v < kNeqMax; ++v) Fn[v] = fpub[ax][v][other - c0];
-          } else {
-            float lo[kNvMax];
-            blk.template face_value<MUSCL>(other, fo, lo);
-            ok &= face_flux<MODEL>(mc, a, fo, 0, MUSCL, lo, own, other, c, Fn);
-          }
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) Tm[v] = s == 0 ? A * Fn[v] : Tm[v] + A * Fn[v];
-        }
-      } else if (rel_of(g, f) == kRelSame && blk.in_block(code)) {
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) Tm[v] = fpub[ax][v][code - c0];
-      } else {
-        float lo[kNvMax];
-        blk.template face_value<MUSCL>(code, fo, lo);
-        ok &= face_flux<MODEL>(mc, a, fo, 0, MUSCL, lo, own, code, c, Tm);
-      }
-      const float A = a.geo->axis_area[lev * 3 + ax];
-      if (!hang_m && !hang_p) {
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, Tm[v] - fpub[ax][v][t], R[v]);
-      } else {
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) {
-          const float tp = hang_p ? fpub[ax][v][t] : A * fpub[ax][v][t];
-          const float tm = hang_m ? Tm[v] : A * Tm[v];
-          R[v] = R[v] + (tm - tp);
-        }
-      }
-    }
-  }
-
-  float lam = 0.0f;
-  if (active) {
-    float qn[kNvMax];
-    const float dtv = s_dt * a.geo->inv_vol[lev];
-    if (stage_update<MODEL>(a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
-  }
-  if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
-}
 
 // 4-byte asynchronous global -> shared copy (cp.async.ca)
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
@@ -1150,7 +751,6 @@ __host__ __device__ constexpr int morton_z(int t) { return ((t >> 2) & 1) | (((t
 // (BX + 4) x (BY + 4) x (BZ + 4) cells whose z-plane stride is padded by PAD
 // so that the 32 Morton-ordered lanes of a warp read 32 different banks.
 //   Brick8  8x8x4 (256 cells): uniform regions;
-//   Brick4  4x4x4 (64 cells): the smaller same-level blocks of AMR meshes.
 // Face-value slots (the values a thread hands to another): the brick cells'
 // -x, -y, -z face values (axis * N + t), then the halo cells next to the
 // brick (layer 1), side by side in the order -x, +x, -y, +y, -z, +z.
@@ -1168,10 +768,9 @@ struct BrickShape {
   // flux slots: the +x, +y, +z faces of the N cells (axis * N + t), then
   // the faces on the brick's -x, -y, -z sides
   static constexpr int kSlotSideX = 3 * N, kSlotSideY = kSlotSideX + BY * BZ, kSlotSideZ = kSlotSideY + BX * BZ;
-  // blocks per SM the launch bounds ask for (registers per thread): inviscid
-  // model 1 48 (five 256-thread blocks) or 64 (64-thread blocks); viscous
-  // model 1 64; model 3 (FP64 pressure inversion) 80.  None spills.
-  static constexpr int kMinBlocks = N == 256 ? 5 : 16, kMinBlocksNS = 4 * 256 / N, kMinBlocks3 = 3 * 256 / N;
+  // blocks per SM the launch bounds ask for: inviscid 48 registers (five
+  // 256-thread blocks), viscous 64 (four).  Neither spills.
+  static constexpr int kMinBlocks = 5 * 256 / N, kMinBlocksNS = 4 * 256 / N;
   __host__ __device__ static constexpr int tile_index(int x, int y, int z) {
     return (z + 2) * P + (y + 2) * TX + (x + 2);
   }
@@ -1220,7 +819,6 @@ struct BrickShape {
                 "brick table fields");
 };
 using Brick8 = BrickShape<8, 8, 4, 0>;
-using Brick4 = BrickShape<4, 4, 4, 4>;
 
 // lower cell (brick coordinates) and axis of flux slot `slot`
 template <class S>
@@ -1441,7 +1039,7 @@ __device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float 
 }
 
 template <int MODEL, bool MUSCL, bool NS, class S>
-__global__ void __launch_bounds__(S::N, MODEL == 3 ? S::kMinBlocks3 : (NS ? S::kMinBlocksNS : S::kMinBlocks))
+__global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     k_mixed_brick(MixedConst mc, StageArgs a) {
   constexpr int NV = kNv<MODEL>;
   constexpr int TX = S::TX, NB = S::N;
@@ -1695,9 +1293,7 @@ __global__ void __launch_bounds__(S::N, MODEL == 3 ? S::kMinBlocks3 : (NS ? S::k
 }
 
 // FP32 state words of an FP64 state (after an upload or an FP64-path
-// step), one cell per thread: the neq variables (model 3: the density
-// shifted by kRhoOffD, plus the low words of the density and of rho Y in
-// rows 5 and 6).
+// step), one cell per thread.
 template <int MODEL>
 __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t n, int neq) {
   for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
@@ -1709,10 +1305,6 @@ __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v)
       if (v < neq) Sf[v * n + c] = q[v];
-    if (MODEL == 3) {
-      Sf[5 * n + c] = q[5];
-      Sf[6 * n + c] = q[6];
-    }
   }
 }
 
@@ -1732,10 +1324,6 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v)
       if (v < mc.neq) Sf[int64_t(v) * n + c] = q[v];
-    if (MODEL == 3) {
-      Sf[int64_t(5) * n + c] = q[5];
-      Sf[int64_t(6) * n + c] = q[6];
-    }
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
   block_max_lambda_f(lam, lambda);
@@ -1751,11 +1339,7 @@ MixedConst make_const(const Phys &ph) {
   mc.gpinf = float(ph.gamma * ph.pinf);
   mc.ylo = float(ph.ymin / 1000.0);
   mc.yhi = float(1.0 - ph.ymin / 1000.0);
-  // the inflow ghost in FP32 state form (the library accepts inflow
-  // boundaries for model 1 only, whose state form is the plain state)
-  for (int v = 0; v < kNeqMax; ++v)
-    mc.inflow[v] = float(ph.model == 3 && v == 0 ? ph.inflow[0] - kRhoOffD : ph.inflow[v]);
-  mc.inflow[5] = 0.0f;
+  for (int v = 0; v < kNeqMax; ++v) mc.inflow[v] = float(ph.inflow[v]);
   mc.model = ph.model;
   mc.neq = ph.neq;
   mc.ischeme = ph.ischeme;
@@ -1882,9 +1466,18 @@ bool brick_sides_resolve(const fvgpu_mesh_soa *m, int64_t i, const std::vector<c
   return true;
 }
 
-}  // namespace
+// every cell of a model-1 mesh lies in an 8x8x4 brick whose six sides are
+// bricks or domain boundaries
+bool all_cells_in_bricks(const fvgpu_mesh_soa *m, std::vector<char> &is_block8) {
+  const int64_t n = m->ncells;
+  if (n % Brick8::N != 0) return false;
+  find_blocks<Brick8>(m, is_block8);
+  for (int64_t i = 0; i < n; i += Brick8::N)
+    if (!is_block8[size_t(i)] || !brick_sides_resolve<Brick8>(m, i, is_block8)) return false;
+  return true;
+}
 
-cudaError_t allow_smem_model(int model, bool muscl);  // defined with the launches below
+}  // namespace
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
   if (ph.model != 1 && ph.model != 3) {
@@ -1893,6 +1486,11 @@ bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
   }
   return true;
 }
+
+// The kernel family of a mesh: the brick kernel of this file for model 1 in
+// 8x8x4 bricks throughout, the table-driven family (fv_mixed_amr.cu)
+// otherwise.
+cudaError_t allow_smem_brick(bool muscl, bool ns);  // with the launches below
 
 int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen) {
   r.ready = false;
@@ -1906,6 +1504,12 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     snprintf(why, whylen, "the mixed path needs the per-cell level array");
     return FVGPU_ERR_UNSUPPORTED;
   }
+  std::vector<char> is_block8(size_t(m->ncells), 0);
+  if (ph.model != 1 || r.force_general || !all_cells_in_bricks(m, is_block8)) {
+    r.family = 1;
+    return amr::mixed_prepare_host(r, ph, m, why, whylen);
+  }
+  r.family = 0;
   // fluxes are evaluated in the face frames of the reference's hexahedral
   // cells, compiled in as signed permutations
   for (int f = 0; f < 6; ++f)
@@ -2024,89 +1628,35 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         return FVGPU_ERR_UNSUPPORTED;
       }
     }
-  // bricks: same-level Morton blocks (candidates), kept when each of their
-  // six sides is a domain boundary or another candidate block of the same
-  // shape, whichever kernel evaluates that block (its cells only supply the
-  // 2-deep halo).  8x8x4 bricks first; 4x4x4 bricks only on meshes where the
-  // 8x8x4 ones cover under 5 % of the cells.  Where both exist, carving 4x4x4
-  // blocks out of the general runs fragments them, and the general kernel's
-  // cost per cell rises more than the bricks save (measured on the two-phase
-  // bubble: 30 % fewer general cells, 4 % more general-kernel time).
-  std::vector<char> is_block8(size_t(n), 0), is_brick8(size_t(n), 0), in_brick8(size_t(n), 0);
-  std::vector<char> is_block4(size_t(n), 0), is_brick4(size_t(n), 0);
-  // bricks for every inviscid run and for viscous runs of model 1 (both
-  // kernels read the cells' gradients straight from the gradient pass)
-  if (!r.force_general && (ph.ns != 1 || ph.model == 1)) {
-    find_blocks<Brick8>(m, is_block8);
-    for (int64_t i = 0; i < n; ++i)
-      if (is_block8[size_t(i)] && brick_sides_resolve<Brick8>(m, i, is_block8)) {
-        is_brick8[size_t(i)] = 1;
-        for (int t = 0; t < Brick8::N; ++t) in_brick8[size_t(i + t)] = 1;
-      }
-    int64_t covered8 = 0;
-    for (int64_t i = 0; i < n; ++i) covered8 += in_brick8[size_t(i)];
-    if (covered8 * 20 < n) {
-      find_blocks<Brick4>(m, is_block4);
-      for (int64_t i = 0; i < n; ++i)
-        if (is_block4[size_t(i)] && !in_brick8[size_t(i)] && brick_sides_resolve<Brick4>(m, i, is_block4))
-          is_brick4[size_t(i)] = 1;
-    }
-  }
-  std::vector<BlockDesc> bricks, bricks4, general;
-  auto brick_desc = [&](int64_t i, int count, auto side_of) {
+  std::vector<BlockDesc> bricks;
+  for (int64_t i = 0; i < n; i += Brick8::N) {
     BlockDesc d;
     memset(&d, 0, sizeof d);
     d.start = int(i);
-    d.count = count;
+    d.count = Brick8::N;
     d.level = m->level[i];
-    for (int f = 0; f < 6; ++f) d.side[f] = side_of(f);
-    return d;
-  };
-  for (int64_t i = 0; i < n;) {
-    if (is_brick8[size_t(i)]) {
-      bricks.push_back(brick_desc(i, Brick8::N, [&](int f) { return brick_side<Brick8>(m, i, f, is_block8); }));
-      i += Brick8::N;
-      continue;
-    }
-    if (is_brick4[size_t(i)]) {
-      bricks4.push_back(brick_desc(i, Brick4::N, [&](int f) { return brick_side<Brick4>(m, i, f, is_block4); }));
-      i += Brick4::N;
-      continue;
-    }
-    BlockDesc d;
-    memset(&d, 0, sizeof d);
-    d.start = int(i);
-    int cnt = 0;
-    while (i < n && cnt < kBlock && !is_brick8[size_t(i)] && !is_brick4[size_t(i)]) {
-      ++i;
-      ++cnt;
-    }
-    d.count = cnt;
-    general.push_back(d);
+    for (int f = 0; f < 6; ++f) d.side[f] = brick_side<Brick8>(m, i, f, is_block8);
+    bricks.push_back(d);
   }
-  const int nv = ph.model == 3 ? kNv<3> : kNv<1>;  // FP32 state words per cell
-  std::vector<BlockDesc> all(bricks);
-  all.insert(all.end(), bricks4.begin(), bricks4.end());
-  all.insert(all.end(), general.begin(), general.end());
   cudaError_t e;
-  if ((e = allow_smem_model(ph.model, ph.ischeme == 2)) != cudaSuccess) {
-    snprintf(why, whylen, "shared-memory opt-in of the mixed kernels: %s", cudaGetErrorString(e));
+  if ((e = allow_smem_brick(ph.ischeme == 2, ph.ns == 1)) != cudaSuccess) {
+    snprintf(why, whylen, "shared-memory opt-in of the brick kernel: %s", cudaGetErrorString(e));
     return FVGPU_ERR_CUDA;
   }
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = alloc_slot(r, kBufTables, sizeof(GeoTables))) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufTables], &gt, sizeof gt, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufBlocks, sizeof(BlockDesc) * (all.size() + 1))) != cudaSuccess ||
-      (e = cudaMemcpy(r.buf[kBufBlocks], all.data(), sizeof(BlockDesc) * all.size(), cudaMemcpyHostToDevice)) !=
+      (e = alloc_slot(r, kBufBlocks, sizeof(BlockDesc) * bricks.size())) != cudaSuccess ||
+      (e = cudaMemcpy(r.buf[kBufBlocks], bricks.data(), sizeof(BlockDesc) * bricks.size(), cudaMemcpyHostToDevice)) !=
           cudaSuccess ||
       (e = alloc_slot(r, kBufD1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNf, sizeof(float) * nv * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * nv * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX1, sizeof(float) * nv * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX2, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufSG, ph.ns == 1 ? sizeof(float) * 9 * n : 16)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
@@ -2114,39 +1664,23 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   r.n = n;
   r.model = ph.model;
   r.nbricks = int64_t(bricks.size());
-  r.nbricks4 = int64_t(bricks4.size());
-  r.ngeneral = int64_t(general.size());
-  const int kinds = (r.nbricks > 0) + (r.nbricks4 > 0) + (r.ngeneral > 0);
-  if (kinds > 1 && !r.side[0]) {
-    for (int k = 0; k < 2; ++k)
-      if (cudaStreamCreateWithFlags(&r.side[k], cudaStreamNonBlocking) != cudaSuccess ||
-          cudaEventCreateWithFlags(&r.join_ev[k], cudaEventDisableTiming) != cudaSuccess) {
-        snprintf(why, whylen, "stream / event creation failed");
-        return FVGPU_ERR_CUDA;
-      }
-    if (cudaEventCreateWithFlags(&r.fork_ev, cudaEventDisableTiming) != cudaSuccess) {
-      snprintf(why, whylen, "stream / event creation failed");
-      return FVGPU_ERR_CUDA;
-    }
-  }
+  r.nbricks4 = 0;
+  r.ngeneral = 0;
   r.ready = true;
   return FVGPU_OK;
 }
 
 void release_mixed(MixedResources &r) {
+  if (r.family == 1) {
+    amr::release_mixed(r);
+    r.family = 0;
+    return;
+  }
   for (int i = 0; i < 11; ++i) {
     if (r.buf[i]) cudaFree(r.buf[i]);
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
   }
-  for (int k = 0; k < 2; ++k) {
-    if (r.side[k]) cudaStreamDestroy(r.side[k]);
-    if (r.join_ev[k]) cudaEventDestroy(r.join_ev[k]);
-    r.side[k] = nullptr;
-    r.join_ev[k] = nullptr;
-  }
-  if (r.fork_ev) cudaEventDestroy(r.fork_ev);
-  r.fork_ev = nullptr;
   r.ready = false;
   r.snf_valid = false;
   r.nbricks = r.nbricks4 = r.ngeneral = 0;
@@ -2154,6 +1688,8 @@ void release_mixed(MixedResources &r) {
 
 double *mixed_alt_state(MixedResources &r) { return static_cast<double *>(r.buf[kBufAlt]); }
 
+// both families keep the second FP64 state in kBufAlt and the FP32 copies in
+// kBufSNf / kBufSNfAlt
 void mixed_swap_state(MixedResources &r, void *&state) {
   void *t = state;
   state = r.buf[kBufAlt];
@@ -2164,12 +1700,9 @@ void mixed_swap_state(MixedResources &r, void *&state) {
 }
 
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
+  if (r.family == 1) return amr::mixed_refresh_f32(r, S, neq, marks, st);
   marks.mark(FVGPU_KIND_MIXED_AUX);
-  float *Sf = static_cast<float *>(r.buf[kBufSNf]);
-  if (r.model == 3)
-    k_state_to_f32<3><<<1024, 256, 0, st>>>(S, Sf, r.n, neq);
-  else
-    k_state_to_f32<1><<<1024, 256, 0, st>>>(S, Sf, r.n, neq);
+  k_state_to_f32<1><<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), r.n, neq);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;
@@ -2177,85 +1710,56 @@ cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, Launc
 
 cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const double *S, double *lambda,
                                      LaunchMarks &marks, cudaStream_t st) {
+  if (r.family == 1) return amr::mixed_refresh_f32_lambda(r, ph, S, lambda, marks, st);
   marks.mark(FVGPU_KIND_MIXED_AUX);
   const unsigned blocks = unsigned(std::min<int64_t>((r.n + kBlock - 1) / kBlock, 152 * 8));
   const MixedConst mc = make_const(ph);
-  const int32_t *geom = static_cast<const int32_t *>(r.buf[kBufGeom]);
-  const GeoTables *geo = static_cast<const GeoTables *>(r.buf[kBufTables]);
-  float *Sf = static_cast<float *>(r.buf[kBufSNf]);
-  if (ph.model == 1)
-    k_state_to_f32_lambda<1><<<blocks, kBlock, 0, st>>>(mc, geom, geo, S, Sf, int(r.n), lambda);
-  else
-    k_state_to_f32_lambda<3><<<blocks, kBlock, 0, st>>>(mc, geom, geo, S, Sf, int(r.n), lambda);
+  k_state_to_f32_lambda<1><<<blocks, kBlock, 0, st>>>(mc, static_cast<const int32_t *>(r.buf[kBufGeom]),
+                                                      static_cast<const GeoTables *>(r.buf[kBufTables]), S,
+                                                      static_cast<float *>(r.buf[kBufSNf]), int(r.n), lambda);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;
 }
 
-// the kernel instance of the configuration (EOS model, reconstruction order)
-template <int MODEL, bool MUSCL, class S>
-void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
-  constexpr size_t smem = S::template smem_bytes<kNv<MODEL>>();
-  if (mc.ns == 1) {
-    if constexpr (MODEL == 1) k_mixed_brick<MODEL, MUSCL, true, S><<<grid, S::N, smem, st>>>(mc, a);
-  } else {
-    k_mixed_brick<MODEL, MUSCL, false, S><<<grid, S::N, smem, st>>>(mc, a);
-  }
-}
-
-enum BlockKind { kKindGeneral = 0, kKindBrick8 = 1, kKindBrick4 = 2 };
+namespace {
 
 // Dynamic shared memory above the 48 KiB default needs a per-kernel opt-in
-// (cudaFuncAttributeMaxDynamicSharedMemorySize); set it for every stage
-// kernel of the model before any launch or stream capture.
+// (cudaFuncAttributeMaxDynamicSharedMemorySize); it is set before any launch
+// or stream capture.
 template <class K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(reinterpret_cast<const void *>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
                               int(bytes));
 }
-template <int MODEL, bool MUSCL>
-cudaError_t allow_smem_instance() {
-  cudaError_t e = allow_smem(k_mixed_general<MODEL, MUSCL>, general_smem_bytes<MODEL>());
-  if (e == cudaSuccess)
-    e = allow_smem(k_mixed_brick<MODEL, MUSCL, false, Brick8>, Brick8::template smem_bytes<kNv<MODEL>>());
-  if (e == cudaSuccess)
-    e = allow_smem(k_mixed_brick<MODEL, MUSCL, false, Brick4>, Brick4::template smem_bytes<kNv<MODEL>>());
-  if constexpr (MODEL == 1) {
-    if (e == cudaSuccess)
-      e = allow_smem(k_mixed_brick<MODEL, MUSCL, true, Brick8>, Brick8::template smem_bytes<kNv<MODEL>>());
-    if (e == cudaSuccess)
-      e = allow_smem(k_mixed_brick<MODEL, MUSCL, true, Brick4>, Brick4::template smem_bytes<kNv<MODEL>>());
-  }
-  return e;
-}
-cudaError_t allow_smem_model(int model, bool muscl) {
-  if (model == 1) return muscl ? allow_smem_instance<1, true>() : allow_smem_instance<1, false>();
-  return muscl ? allow_smem_instance<3, true>() : allow_smem_instance<3, false>();
+template <bool MUSCL>
+cudaError_t allow_smem_muscl(bool ns) {
+  constexpr size_t bytes = Brick8::template smem_bytes<kNeqMax>();
+  return ns ? allow_smem(k_mixed_brick<1, MUSCL, true, Brick8>, bytes)
+            : allow_smem(k_mixed_brick<1, MUSCL, false, Brick8>, bytes);
 }
 
-template <int MODEL, bool MUSCL>
-void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
-  if (kind == kKindBrick8)
-    launch_brick<MODEL, MUSCL, Brick8>(grid, mc, a, st);
-  else if (kind == kKindBrick4)
-    launch_brick<MODEL, MUSCL, Brick4>(grid, mc, a, st);
+template <bool MUSCL>
+void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
+  constexpr size_t smem = Brick8::template smem_bytes<kNeqMax>();
+  if (mc.ns == 1)
+    k_mixed_brick<1, MUSCL, true, Brick8><<<grid, Brick8::N, smem, st>>>(mc, a);
   else
-    k_mixed_general<MODEL, MUSCL><<<grid, kBlock, general_smem_bytes<MODEL>(), st>>>(mc, a);
+    k_mixed_brick<1, MUSCL, false, Brick8><<<grid, Brick8::N, smem, st>>>(mc, a);
 }
 
-void launch_kernel(const Phys &ph, int kind, unsigned grid, const MixedConst &mc, const StageArgs &a,
-                   cudaStream_t st) {
-  const bool muscl = ph.ischeme == 2;
-  if (ph.model == 1)
-    muscl ? launch_instance<1, true>(kind, grid, mc, a, st) : launch_instance<1, false>(kind, grid, mc, a, st);
-  else
-    muscl ? launch_instance<3, true>(kind, grid, mc, a, st) : launch_instance<3, false>(kind, grid, mc, a, st);
+}  // namespace
+
+cudaError_t allow_smem_brick(bool muscl, bool ns) {
+  return muscl ? allow_smem_muscl<true>(ns) : allow_smem_muscl<false>(ns);
 }
 
 // One RK step from FP64 state `in` (and its FP32 copy) to `out`.
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,
                                unsigned long long *err, LaunchMarks &marks, cudaStream_t st) {
+  if (r.family == 1)
+    return amr::enqueue_step_mixed(r, ph, m, scheme, cfl_mode, in, out, dt, lambda, cfl, err, marks, st);
   static const int kStages[4][3] = {{0, 0, 0}, {1, 0, 0}, {1, 4, 0}, {1, 2, 3}};
   const int nst = scheme == 1 ? 1 : (scheme == 2 ? 2 : 3);
   if (cfl_mode) {
@@ -2265,9 +1769,9 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
   float *D[2] = {static_cast<float *>(r.buf[kBufD1]), static_cast<float *>(r.buf[kBufD2])};
   float *X[2] = {static_cast<float *>(r.buf[kBufX1]), static_cast<float *>(r.buf[kBufX2])};
   const MixedConst mc = make_const(ph);
-  const BlockDesc *blocks = static_cast<const BlockDesc *>(r.buf[kBufBlocks]);
   for (int k = 0; k < nst; ++k) {
     StageArgs a = stage_args(r, m);
+    a.blocks = static_cast<const BlockDesc *>(r.buf[kBufBlocks]);
     a.SNf = static_cast<const float *>(r.buf[kBufSNf]);
     a.Sin = k == 0 ? a.SNf : X[(k - 1) & 1];
     a.Din = k == 0 ? nullptr : D[(k - 1) & 1];
@@ -2284,45 +1788,18 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.err = err;
     if (ph.ns == 1) {
       marks.mark(FVGPU_KIND_MIXED_AUX);
-      const unsigned gg = unsigned((m.n + kBlock - 1) / kBlock);
-      if (ph.model == 1)
-        k_mixed_grad<1><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
-      else
-        k_mixed_grad<3><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
-      cudaError_t e = cudaGetLastError();
+      k_mixed_grad<1><<<unsigned((m.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(mc, a,
+                                                                               static_cast<float *>(r.buf[kBufSG]));
+      const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
-    // the three kinds of block write disjoint cells: with more than one
-    // present, 4x4x4 bricks and general blocks run on the side streams,
-    // concurrently with the 8x8x4 bricks on the caller's stream
-    const int64_t count[3] = {r.nbricks, r.nbricks4, r.ngeneral};
-    const int64_t offset[3] = {0, r.nbricks, r.nbricks + r.nbricks4};
-    const int kind_of[3] = {kKindBrick8, kKindBrick4, kKindGeneral};
-    const bool fork = ((count[0] > 0) + (count[1] > 0) + (count[2] > 0)) > 1 && r.side[0];
     marks.mark(FVGPU_KIND_MIXED_STAGE);
-    if (fork) {
-      // only side streams that get work join (a captured stream must rejoin)
-      cudaError_t e = cudaEventRecord(r.fork_ev, st);
-      for (int k = 1; k < 3 && e == cudaSuccess; ++k)
-        if (count[k] > 0) e = cudaStreamWaitEvent(r.side[k - 1], r.fork_ev, 0);
-      if (e != cudaSuccess) return e;
-    }
-    for (int k = 2; k >= 0; --k) {  // side streams first, the caller's stream last
-      if (count[k] == 0) continue;
-      cudaStream_t ks = (fork && k > 0) ? r.side[k - 1] : st;
-      a.blocks = blocks + offset[k];
-      launch_kernel(ph, kind_of[k], unsigned(count[k]), mc, a, ks);
-      cudaError_t e = cudaGetLastError();
-      if (e == cudaSuccess && ks != st) e = cudaEventRecord(r.join_ev[k - 1], ks);
-      if (e != cudaSuccess) return e;
-    }
-    if (fork) {
-      for (int k = 1; k < 3; ++k) {
-        if (count[k] == 0) continue;
-        const cudaError_t e = cudaStreamWaitEvent(st, r.join_ev[k - 1], 0);
-        if (e != cudaSuccess) return e;
-      }
-    }
+    if (ph.ischeme == 2)
+      launch_brick<true>(unsigned(r.nbricks), mc, a, st);
+    else
+      launch_brick<false>(unsigned(r.nbricks), mc, a, st);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }

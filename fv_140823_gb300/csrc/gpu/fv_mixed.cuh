@@ -30,6 +30,10 @@ struct MixedResources {
   cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr};
   bool ready = false;
   bool snf_valid = false;  // FP32 copy of the current state is up to date
+  // kernel family of the prepared mesh: 0 the slope-sharing brick kernel
+  // (fv_mixed.cu; meshes of model 1 that are 8x8x4 bricks throughout), 1 the
+  // table-driven family (fv_mixed_amr.cu; every other mesh)
+  int family = 0;
 };
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen);
@@ -47,6 +51,18 @@ cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, Launc
 // (which the caller zeroes)
 cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const double *S, double *lambda,
                                      LaunchMarks &marks, cudaStream_t st);
+namespace amr {
+// The table-driven kernel family (fv_mixed_amr.cu): the same entry points.
+int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen);
+void release_mixed(MixedResources &r);
+cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st);
+cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const double *S, double *lambda,
+                                     LaunchMarks &marks, cudaStream_t st);
+cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
+                               const double *in, double *out, double *dt, double *lambda, const double *cfl,
+                               unsigned long long *err, LaunchMarks &marks, cudaStream_t st);
+}  // namespace amr
+
 // One RK step from FP64 state `in` to `out` (distinct buffers).
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,

@@ -197,10 +197,20 @@ def _mixed_state(case, flags, nsteps, dt):
         return s.state()
 
 
+def bricks_throughout(t) -> bool:
+    """A uniform octree of level >= 3 is 8x8x4 bricks throughout: model 1 runs
+    it on the slope-sharing brick kernel, FVGPU_FLAG_NO_BRICKS (and every
+    other mesh) on the table-driven kernel family."""
+    return bool(np.all(t.level == t.level[0])) and int(t.level[0]) >= 3
+
+
 @pytest.mark.parametrize("name", ["periodic", "sod", "bump", "inflow", "bubble", "tgv", "tgv_walls"])
 def test_brick_kernel_bit_identical_to_general_kernel(name):
-    """The brick fast path and the table-driven kernel accumulate every cell's
-    residual from the same canonical face fluxes in the same order."""
+    """Within the table-driven family the 8x8x4 / 4x4x4 brick kernels and the
+    general kernel accumulate every cell's residual from the same canonical
+    face fluxes in the same order: bit-identical.  On meshes of 8x8x4 bricks
+    throughout the default run uses the slope-sharing kernel instead, which
+    agrees with the table-driven family to FP32 rounding (<= 1e-6)."""
     if name == "periodic":
         c = cases.periodic(level=5)
     elif name == "sod":
@@ -229,7 +239,10 @@ def test_brick_kernel_bit_identical_to_general_kernel(name):
     dt = 2e-7 if name == "bubble" else fixed_dt(c)
     a = _mixed_state(c, 0, 4, dt)
     b = _mixed_state(c, abi.FLAG_NO_BRICKS, 4, dt)
-    assert np.array_equal(a.view(np.int64), b.view(np.int64))
+    if bricks_throughout(c.tables) and c.cfg.model == 1:
+        assert np.all(rel_l2(a, b) <= 1e-6), rel_l2(a, b)
+    else:
+        assert np.array_equal(a.view(np.int64), b.view(np.int64))
 
 
 @pytest.mark.parametrize("flags", [0, abi.FLAG_NO_BRICKS])
@@ -263,8 +276,10 @@ def test_mixed_nonfinite_state_reports_and_context_recovers(flags):
 @pytest.mark.parametrize("periodic", [True, False])
 def test_small_meshes_bricks_and_general_agree(level, periodic):
     """Meshes of 8, 64 and 512 cells: no brick, one 4x4x4 brick, two 8x8x4
-    bricks; periodic ones wrap a brick onto itself.  Bricks and the general
-    kernel give the same bits, and both stay within 1e-6 of FP64."""
+    bricks; periodic ones wrap a brick onto itself.  Within one kernel family
+    the bricks and the general kernel give the same bits (the 512-cell mesh
+    runs the slope-sharing kernel by default and agrees with the table-driven
+    family to FP32 rounding), and every run stays within 1e-6 of FP64."""
     from fv_140823_gb300.mesh import uniform_mesh
     m = uniform_mesh(level, periodic=(1, 1, 1)) if periodic else uniform_mesh(level, side_bc=(2,) * 6)
     t = m.flatten()
@@ -276,6 +291,10 @@ def test_small_meshes_bricks_and_general_agree(level, periodic):
     dt = fixed_dt(c)
     a = _mixed_state(c, 0, 3, dt)
     b = _mixed_state(c, abi.FLAG_NO_BRICKS, 3, dt)
-    assert np.array_equal(a.view(np.int64), b.view(np.int64))
-    assert np.all(rel_l2(a, run(c, abi.FP64, 3, dt)) <= 1e-6)
+    if bricks_throughout(t):
+        assert np.all(rel_l2(a, b) <= 1e-6), rel_l2(a, b)
+    else:
+        assert np.array_equal(a.view(np.int64), b.view(np.int64))
+    ref = run(c, abi.FP64, 3, dt)
+    assert np.all(rel_l2(a, ref) <= 1e-6) and np.all(rel_l2(b, ref) <= 1e-6)
 
