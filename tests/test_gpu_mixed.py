@@ -17,6 +17,16 @@ def solver(t, cfg):
     return Solver(t, cfg)
 
 
+def rel_l2_mom(a, b):
+    """Relative L2 error per field with the three momentum components measured
+    against the norm of the whole momentum (a component that is zero in exact
+    arithmetic has only rounding noise and no relative error of its own)."""
+    e = rel_l2(a, b)
+    nm = max(np.linalg.norm(b[1:4]), 1e-300)
+    e[1:4] = [np.linalg.norm(a[v] - b[v]) / nm for v in (1, 2, 3)]
+    return e
+
+
 def rel_l2(a, b):
     return np.array([np.linalg.norm(a[v] - b[v]) / max(np.linalg.norm(b[v]), 1e-300) for v in range(a.shape[0])])
 
@@ -240,7 +250,7 @@ def test_brick_kernel_bit_identical_to_general_kernel(name):
     a = _mixed_state(c, 0, 4, dt)
     b = _mixed_state(c, abi.FLAG_NO_BRICKS, 4, dt)
     if bricks_throughout(c.tables) and c.cfg.model == 1:
-        assert np.all(rel_l2(a, b) <= 1e-6), rel_l2(a, b)
+        assert np.all(rel_l2_mom(a, b) <= 1e-6), rel_l2_mom(a, b)
     else:
         assert np.array_equal(a.view(np.int64), b.view(np.int64))
 
@@ -292,7 +302,7 @@ def test_small_meshes_bricks_and_general_agree(level, periodic):
     a = _mixed_state(c, 0, 3, dt)
     b = _mixed_state(c, abi.FLAG_NO_BRICKS, 3, dt)
     if bricks_throughout(t):
-        assert np.all(rel_l2(a, b) <= 1e-6), rel_l2(a, b)
+        assert np.all(rel_l2_mom(a, b) <= 1e-6), rel_l2_mom(a, b)
     else:
         assert np.array_equal(a.view(np.int64), b.view(np.int64))
     ref = run(c, abi.FP64, 3, dt)
