@@ -423,7 +423,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_of(full, args),
+        "data": "synthetic", "config": config_of(full, args, gpu=False),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
                          "sample": f"every step is one full SSP-RK3 step (CFL dt) of the "
                                    f"{case.tables.ncells}-cell periodic mesh of the same generator"
@@ -435,11 +435,13 @@ def run_reference(args):
     return 0
 
 
-def config_of(case, args):
-    return {"workload": f"periodic ideal gas {2 ** args.level}^3 uniform octree (level {args.level}), "
-                        f"{case.tables.ncells} cells, SSP-RK3, CFL 0.5, MUSCL/minmod + HLLC, seed 1234",
-            "cells": case.tables.ncells, "scheme": "ssprk3", "cfl": 0.5, "parallelism": "replicas",
-            "l2": "flushed before every timed step (256 MiB write on the library stream)"}
+def config_of(case, args, gpu: bool = True):
+    cfg = {"workload": f"periodic ideal gas {2 ** args.level}^3 uniform octree (level {args.level}), "
+                       f"{case.tables.ncells} cells, SSP-RK3, CFL 0.5, MUSCL/minmod + HLLC, seed 1234",
+           "cells": case.tables.ncells, "scheme": "ssprk3", "cfl": 0.5, "parallelism": "replicas"}
+    if gpu:
+        cfg["l2"] = "flushed before every timed step (256 MiB write on the library stream)"
+    return cfg
 
 
 def main():

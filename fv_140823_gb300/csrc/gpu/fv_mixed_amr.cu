@@ -591,7 +591,7 @@ __device__ __forceinline__ void global_state(const MixedConst &mc, const StageAr
 __device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float q[kNeqMax],
                                                float u[3]) {
   if (bc == 1) {
-    const float rinv = fast_rcp(mc.inflow[0]);
+    const float rinv = fast_rcp(state_rho_rt(mc.model, mc.inflow[0]));
     u[0] = mc.inflow[1] * rinv;
     u[1] = mc.inflow[2] * rinv;
     u[2] = mc.inflow[3] * rinv;
@@ -1480,7 +1480,10 @@ MixedConst make_const(const Phys &ph) {
   mc.gpinf = float(ph.gamma * ph.pinf);
   mc.ylo = float(ph.ymin / 1000.0);
   mc.yhi = float(1.0 - ph.ymin / 1000.0);
-  for (int v = 0; v < kNeqMax; ++v) mc.inflow[v] = float(ph.inflow[v]);
+  // the inflow ghost in FP32 state form (model 3 holds rho - kRhoOff; the
+  // library accepts inflow boundaries for model 1 only)
+  for (int v = 0; v < kNeqMax; ++v)
+    mc.inflow[v] = float(ph.model == 3 && v == 0 ? ph.inflow[0] - kRhoOffD : ph.inflow[v]);
   mc.model = ph.model;
   mc.neq = ph.neq;
   mc.ischeme = ph.ischeme;

@@ -25,8 +25,10 @@
 // Host code cannot use the array's name as a device address (it is a host-side
 // stand-in), so the first call on each device looks up the real address with
 // cudaGetSymbolAddress while that device is current, checks the result and
-// caches it.  That first call therefore performs a runtime query: make it
-// before any stream capture on that device.
+// caches it together with the device's current context.  A call that finds a
+// different context (the old one was destroyed, e.g. by cudaDeviceReset, and
+// the array now lives in the new one) looks the address up again.  Those calls
+// therefore perform a runtime query: make them before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -43,7 +45,26 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_partial[kNoallocBlocks * kNoallocMaxVars];
 
 double *g_partial_addr[kMaxDevices] = {nullptr};
+void *g_partial_ctx[kMaxDevices] = {nullptr};  // the context the cached address belongs to
 std::mutex g_setup_mutex;
+
+// The calling thread's current driver context (cuCtxGetCurrent, fetched from
+// the driver through the runtime so the library needs no link to libcuda).
+typedef int (*CtxGetCurrentFn)(void **);
+void *current_context() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  void *ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 // Same partition and reduction order as fvgpu_conservation: cells split into
 // kNoallocBlocks contiguous ranges, fixed in-block tree, fixed final tree.
@@ -88,11 +109,13 @@ int scratch_on_current_device(double **out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return FVGPU_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_partial_addr[dev]) {
+  void *ctx = current_context();
+  if (!g_partial_addr[dev] || ctx == nullptr || ctx != g_partial_ctx[dev]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
     if (e != cudaSuccess || p == nullptr) return FVGPU_ERR_CUDA;
     g_partial_addr[dev] = static_cast<double *>(p);
+    g_partial_ctx[dev] = current_context();  // the runtime made the primary context current if none was
   }
   *out = g_partial_addr[dev];
   return FVGPU_OK;

@@ -85,12 +85,20 @@ static size_t hash_ptr(const void *p) {
   return (size_t)x;
 }
 
+static void *grow(void *p, size_t bytes) {
+  void *q = realloc(p, bytes ? bytes : 16);
+  if (!q) {
+    printf("fvshim: out of host memory\n");
+    exit(0);
+  }
+  return q;
+}
+
 static void map_reset(int64_t n) {
   size_t cap = 16;
   while (cap < (size_t)(2 * n + 1)) cap <<= 1;
   if (cap != G.mapcap) {
-    free(G.map);
-    G.map = malloc(cap * sizeof(slot_t));
+    G.map = grow(G.map, cap * sizeof(slot_t));  /* exits with a message when out of memory */
     G.mapcap = cap;
   }
   for (size_t i = 0; i < cap; ++i) G.map[i].key = NULL;
@@ -114,14 +122,6 @@ static int64_t map_get(const void *key) {
 
 /* ---- flattening ---------------------------------------------------------------- */
 
-static void *grow(void *p, size_t bytes) {
-  void *q = realloc(p, bytes ? bytes : 16);
-  if (!q) {
-    printf("fvshim: out of host memory\n");
-    exit(0);
-  }
-  return q;
-}
 
 /* Builds the tables from run->topo->locl; returns 0 or a message. */
 static const char *flatten(RUN *run) {

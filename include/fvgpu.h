@@ -192,8 +192,10 @@ int fvgpu_conservation(fvgpu_ctx *ctx, double *sums);
  * sums [neq+1] -- and keeps its scratch in a fixed 48 KiB device array of the
  * library (every GPU that loads the library holds it until exit).  Limits:
  * 1 <= neq <= 5, 1 <= ncells < 2^31, else FVGPU_ERR_ARG.  It allocates
- * nothing.  The first call on a device looks up the array's device address
- * (make it before any stream capture on that device).  All calls share the
+ * nothing.  The first call on a device, and the first after that device's
+ * context was destroyed and created again (cudaDeviceReset), looks up the
+ * array's device address: make it before any stream capture on that device.
+ * All calls share the
  * array: calls that overlap on the GPU race, so order them.  Work is queued on
  * `stream` (a cudaStream_t, NULL = default stream); sums are ready when that
  * stream reaches this point. */
@@ -288,9 +290,11 @@ int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const
 int fvgpu_profile_adjoint(fvgpu_ctx *ctx, int reps, double *ms_residual, double *ms_vjp);
 
 /* ---- diagnostics -------------------------------------------------------- */
-/* Measured FP64 arithmetic rate of the device (G operations/s): separate
- * adds and multiplies from registers on every SM, as the FP64 path issues
- * them; the denominator of that path's roofline.  No reference counterpart. */
+/* Measurement utility, not part of the solver path (no reference
+ * counterpart): the FP64 arithmetic rate of the device in G operations/s,
+ * from separate adds and multiplies in registers on every SM, as the FP64
+ * path issues them.  bench.py divides the FP64 residual's counted operations
+ * by it for that kernel's roofline fraction. */
 int fvgpu_measure_fp64(int device, double *gops);
 
 /* Kernel kinds reported by fvgpu_profile_step. */

@@ -25,7 +25,13 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CFLAGS = ["-O2", "-fno-fast-math", "-ffp-contract=off", "-fPIC", "-std=gnu99"]
-DEFAULT_REF_ROOT = "/root/reference"
+
+
+def default_ref_root() -> str:
+    """The reference tree: FV_REFERENCE_ROOT, else a directory named
+    "reference" beside the repository."""
+    return os.environ.get("FV_REFERENCE_ROOT") or os.path.join(os.path.dirname(REPO), "reference")
+
 
 # The reference files on the residual / RK path, plus the allocation helpers
 # the harness calls (leafallocation, memallocation, createutility) and what
@@ -68,7 +74,8 @@ def build_oracle_ad() -> str:
     return out
 
 
-def build_ref(ref_root: str = DEFAULT_REF_ROOT) -> str | None:
+def build_ref(ref_root: str | None = None) -> str | None:
+    ref_root = ref_root or default_ref_root()
     """Compile the reference's hot path + harness into oracle/_ref/libfvref.so.
 
     Returns None when the reference tree is absent (e.g. on a GPU host)."""
@@ -94,7 +101,7 @@ def build_ref(ref_root: str = DEFAULT_REF_ROOT) -> str | None:
 
 def main(argv: list[str] | None = None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default=DEFAULT_REF_ROOT)
+    ap.add_argument("--ref-root", default=None, help="reference tree (default: FV_REFERENCE_ROOT, else ../reference)")
     a = ap.parse_args(argv)
     print(build_oracle())
     print(build_oracle_ad())
