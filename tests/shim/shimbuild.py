@@ -29,7 +29,8 @@ REPLACED = ("RHS", "RHS_nb", "RK", "faceinterp", "gradcalc")
 OUT = os.path.join(HERE, "_build", "libshimtest.so")
 
 
-def build_shim_test(ref_root: str = oracle_build.DEFAULT_REF_ROOT) -> str | None:
+def build_shim_test(ref_root: str | None = None) -> str | None:
+    ref_root = ref_root or oracle_build.default_ref_root()
     if not os.path.isfile(os.path.join(ref_root, "strdata.h")):
         return None
     obj_dir = os.path.join(HERE, "_build", "obj")
