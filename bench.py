@@ -206,9 +206,10 @@ def e2e_pipelined(case, cfg, nctx: int, steps: int, warmup: int, cfl: float, n: 
     return n * steps / wall / 1e6
 
 
-def time_steps(torch, s, stream, flush, steps: int, cfl: float, scheme="ssprk3"):
+def time_steps(torch, s, stream, flush, steps: int, cfl: float, scheme="ssprk3", dt: float = 0.0):
     """Per-step device times (ms), each step bracketed by events on the
-    library's stream, with an L2 flush before each step outside the events."""
+    library's stream, with an L2 flush before each step outside the events
+    (CFL steps, or fixed-dt steps when dt > 0)."""
     times = []
     with torch.cuda.stream(stream):
         for _ in range(steps):
@@ -216,7 +217,7 @@ def time_steps(torch, s, stream, flush, steps: int, cfl: float, scheme="ssprk3")
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            s.step(scheme, cfl=cfl, nsteps=1)
+            s.step(scheme, dt=dt, cfl=0.0 if dt > 0 else cfl, nsteps=1)
             e1.record(stream)
             times.append((e0, e1))
     torch.cuda.synchronize()
@@ -361,12 +362,70 @@ def run_gpu(args):
             ms_res, ms_vjp = s.profile_adjoint(reps=5)
             results[prec]["adjoint"] = {"ms_residual": ms_res, "ms_vjp": ms_vjp, "vjp_over_residual": ms_vjp / ms_res}
         s.close()
+    results["workloads"] = None if args.no_workloads else amr_workloads(args, torch, flush, hbm_peak)
     err = None
     if abi.MIXED in states and abi.FP64 in states:
         a, b = states[abi.MIXED][0], states[abi.FP64][0]
         names = ["rho", "rho_u", "rho_v", "rho_w", "E"]
         err = {names[v]: float(np.linalg.norm(a[v] - b[v]) / np.linalg.norm(b[v])) for v in range(a.shape[0])}
     return results, err, case, ws, rank, dist
+
+
+WORKLOADS = {
+    "C2": ("two-phase bubble (model 3 mixture EOS), 16^3 base + 3 levels by the density criterion, "
+           "MUSCL/minmod + HLLC, SSP-RK3", lambda: __import__("fv_140823_gb300.cases", fromlist=["x"]).bubble(4, 3)),
+    "C5": ("viscous Taylor-Green vortex Re 1600 Mach 0.1, 32^3 base + 2 levels by the vorticity criterion, "
+           "MUSCL/minmod + HLLC + viscous fluxes, SSP-RK3", lambda: __import__("fv_140823_gb300.cases",
+                                                                             fromlist=["x"]).tgv(5, 2)),
+}
+
+
+def amr_workloads(args, torch, flush, hbm_peak):
+    """The AMR workloads (1:4 faces, two-phase mixture, viscous) on the mixed
+    and FP64 paths: graph-launched SSP-RK3 steps at a fixed dt (the FP64 CFL
+    step of the initial state), each bracketed by events on the library
+    stream with an L2 flush before it; relative L2 error of the mixed state
+    against the FP64 state after `err_steps` steps (momentum components
+    against the norm of the whole momentum)."""
+    from fv_140823_gb300 import abi
+    from fv_140823_gb300.abi import SolverConfig
+    from fv_140823_gb300.solver import Solver
+    out = {}
+    for key, (desc, make) in WORKLOADS.items():
+        case = make()
+        n, nhang = case.tables.ncells, case.tables.nhang
+        # compulsory bytes per step: 416 B per cell plus the 1:4 records read per stage
+        alg = algorithmic_bytes_per_cell_step(case.cfg.neq) * n + 3 * 16 * nhang
+        res = {"workload": desc, "cells": n, "hanging_faces": nhang, "algorithmic_bytes_per_step": alg}
+        states = {}
+        with Solver(case.tables, SolverConfig(**{**case.cfg.__dict__, "precision": abi.FP64})) as s:
+            s.set_state(case.U)
+            dt = s.compute_dt(case.cfl)
+        res["dt"] = dt
+        for prec, name, k in ((abi.MIXED, "mixed", args.workload_steps), (abi.FP64, "fp64", args.workload_fp64_steps)):
+            with Solver(case.tables, SolverConfig(**{**case.cfg.__dict__, "precision": prec})) as s:
+                stream = torch.cuda.ExternalStream(s.stream_handle())
+                s.set_state(case.U)
+                s.step("ssprk3", dt=dt, nsteps=args.warmup)
+                s.synchronize()
+                ms = time_steps(torch, s, stream, flush, k, 0.0, dt=dt)
+                tot = float(sum(ms))
+                res[name] = {"value": n * k / (tot * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": tot / k, "steps": k,
+                             "hbm_frac": alg / (tot / k * 1e-3) / 1e9 / hbm_peak}
+                s.set_state(case.U)
+                s.step("ssprk3", dt=dt, nsteps=args.err_steps_amr)
+                states[prec] = s.state()
+        a, b = states[abi.MIXED], states[abi.FP64]
+        names = ["rho", "rho_u", "rho_v", "rho_w", "E" if case.cfg.model == 1 else "rho_Y"]
+        mom = max(float(np.linalg.norm(b[1:4])), 1e-300)
+        err = {}
+        for v in range(a.shape[0]):
+            den = mom if v in (1, 2, 3) else max(float(np.linalg.norm(b[v])), 1e-300)
+            err[names[v]] = float(np.linalg.norm(a[v] - b[v])) / den
+        res["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+        res["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps_amr, "momentum_against": "|rho u| norm", **err}
+        out[key] = res
+    return out
 
 
 def cpu_baseline(case, steps: int = 1):
@@ -458,11 +517,23 @@ def main():
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--err-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true", help="skip the AMR workloads (C2, C5) of the line")
+    ap.add_argument("--workloads-only", action="store_true",
+                    help="print only the AMR workloads' JSON (no 128^3 arms)")
+    ap.add_argument("--workload-steps", type=int, default=30)
+    ap.add_argument("--workload-fp64-steps", type=int, default=5)
+    ap.add_argument("--err-steps-amr", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     from fv_140823_gb300 import abi
+    if args.workloads_only:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+        print(json.dumps(amr_workloads(args, torch, flush, peaks()[0])))
+        return 0
     results, err, case, ws, rank, dist = run_gpu(args)
     if rank == 0:
         head = abi.MIXED if "value" in results.get(abi.MIXED, {}) else abi.FP64
@@ -488,6 +559,8 @@ def main():
             line["adjoint"] = results[abi.FP64]["adjoint"]
         if err is not None:
             line["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps, **err}
+        if results.get("workloads"):
+            line["workloads"] = results["workloads"]
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(case)
         print(json.dumps(line))

@@ -102,7 +102,7 @@ struct MixedConst {
   float ylo, yhi;  // mass-fraction clip (facercnstr.c:43-44)
   float visc;      // dynamic viscosity (flux_viscous.c, turb = 0)
   int ns, eos;     // viscous fluxes on; energy work term on
-  float inflow[kNeqMax];
+  float inflow[7];  // state words of the inflow ghost (model 3: seven)
   int model, neq, ischeme, pad;
 };
 
@@ -146,44 +146,122 @@ __device__ __forceinline__ const float *geo_face(const GeoTables *G, int level, 
 
 struct FS {
   float r, u, v, w, e, p, c, y;
-  float q[kNeqMax];
 };
 
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
 
-// Density in the FP32 state vectors.  Model 3 (liquid-gas mixture) stores
-// rho - kRhoOff, kRhoOff the saturation density of the mixture EOS
-// (barotropic_eos.c:41, as an FP32 value): near the liquid density an FP32
-// ulp of rho itself is 6e-5, which the stiff liquid branch of the EOS turns
-// into ~130 Pa of pressure; the offset value keeps the liquid density to
-// ~1e-8 for the FP64 pressure inversion (the gas density, ~1, then carries
-// the 6e-5, worth ~5 Pa).  Differences between cells, and so the
-// reconstruction, are unchanged; model 1 stores rho.
+// State words.  Model 1 keeps its five conservative variables as FP32
+// words.  Model 3 (liquid-gas mixture) keeps the density and the gas partial
+// density rho Y as pairs of FP32 words, a high word and the rounding
+// remainder (words 0 + 5 and 4 + 6), with the density shifted by kRhoOff, the
+// saturation density of the mixture EOS (barotropic_eos.c:41, as an FP32
+// value).  The pressure inversion is stiff in both partial densities: near
+// the liquid density an FP32 ulp of rho is 6e-5, which the liquid branch
+// (dp/drho = c_liq^2) turns into ~130 Pa, and the gas density (~1) stored as
+// rho - kRhoOff alone would carry the ulp of ~1000, ~5 Pa of gas pressure.
+// With the pairs, model 3's reconstruction of rho and rho Y (differences,
+// limited slopes, face values) runs in FP64 and the FP64 inversion sees the
+// face values to FP64 rounding; the momentum and the flux arithmetic stay
+// FP32.  Stage increments stay five FP32 words.
+template <int MODEL>
+constexpr int kNv = MODEL == 3 ? 7 : 5;
+constexpr int kNvMax = 7;
 constexpr float kRhoOffF = 998.1618f;
 constexpr double kRhoOffD = double(kRhoOffF);
+// the low word of paired variable v (0: the density, 4: rho Y)
+__host__ __device__ constexpr int lo_word(int v) { return v == 0 ? 5 : 6; }
+// the FP64 value of paired word v of a model-3 state (the density without
+// its offset)
+__device__ __forceinline__ double pair_d(const float *q, int v) { return double(q[v]) + double(q[lo_word(v)]); }
+// splits an FP64 value into paired word v
+__device__ __forceinline__ void set_pair(float *q, int v, double x) {
+  const float h = __double2float_rn(x);
+  q[v] = h;
+  q[lo_word(v)] = __double2float_rn(x - double(h));
+}
+// the density as FP64 and as FP32
 template <int MODEL>
-__device__ __forceinline__ float state_rho(float q0) { return MODEL == 3 ? q0 + kRhoOffF : q0; }
+__device__ __forceinline__ double state_rho_d(const float *q) {
+  if constexpr (MODEL == 3) return kRhoOffD + pair_d(q, 0);
+  return double(q[0]);
+}
 template <int MODEL>
-__device__ __forceinline__ double state_rho_d(float q0) { return MODEL == 3 ? double(q0) + kRhoOffD : double(q0); }
-__device__ __forceinline__ float state_rho_rt(int model, float q0) { return model == 3 ? q0 + kRhoOffF : q0; }
-// the FP32 state value of variable v from the FP64 state value
+__device__ __forceinline__ float state_rho(const float *q) {
+  if constexpr (MODEL == 3) return __double2float_rn(state_rho_d<MODEL>(q));
+  return q[0];
+}
+// FP32 state words of an FP64 state (model 3: seven words)
 template <int MODEL>
-__device__ __forceinline__ float to_state_f32(int v, double x) {
-  return __double2float_rn(MODEL == 3 && v == 0 ? x - kRhoOffD : x);
+__device__ __forceinline__ void to_state_words(const double x[kNeqMax], float q[kNvMax]) {
+#pragma unroll
+  for (int v = 0; v < kNeqMax; ++v) q[v] = __double2float_rn(x[v]);
+  if constexpr (MODEL == 3) {
+    set_pair(q, 0, x[0] - kRhoOffD);
+    set_pair(q, 4, x[4]);
+  }
+}
+
+// The two-phase mixture EOS of barotropic_eos.c:32-129 (the larger root of
+// the pressure quadratic, the liquid sound speed with the mixture fallback)
+// on the two partial densities: the reference's products rho Y and
+// rho (1 - Y) are the gas partial density ry and rho - ry, taken as such from
+// the paired state words.  FP64; false when neither branch has a real root.
+__device__ __forceinline__ bool eos_mixture_partial(double r, double ry, double &p_out, double &c_out) {
+  const double R_G = 286.0, T_ref = 293.15, r_sat = 998.1618, p_sat = 2340.0;
+  const double c_liq = 1482.5, c_mixture = 1.0;
+  const double rg = ry * R_G * T_ref, rl = r - ry;
+  double ct = c_liq;
+  double c2 = ct * ct;
+  double b = c2 * r_sat - p_sat - rg - rl * c2;
+  double d = (p_sat - c2 * r_sat) * rg;
+  double disc = b * b - 4.0 * d;
+  if (!(disc >= 0.0)) {
+    ct = c_mixture;
+    c2 = ct * ct;
+    b = c2 * r_sat - p_sat - rg - rl * c2;
+    d = (p_sat - c2 * r_sat) * rg;
+    disc = b * b - 4.0 * d;
+    if (!(disc >= 0.0)) {
+      p_out = __longlong_as_double(0x7ff8000000000000ll);
+      c_out = ct;
+      return false;
+    }
+  }
+  p_out = 0.5 * (sqrt(disc) - b);
+  c_out = ct;
+  return true;
+}
+
+// Model 3: the FP64 density and gas partial density of a face value for the
+// pressure inversion, with the mass fraction clipped as facercnstr.c:43-44
+// (clip) and returned in FP32 for the flux.
+__device__ __forceinline__ bool mixture_face_eos(const MixedConst &mc, const float *q, bool clip, float &r32,
+                                                 float &y32, float &p32, float &c32) {
+  const double r = kRhoOffD + pair_d(q, 0);
+  double ry = pair_d(q, 4);
+  r32 = __double2float_rn(r);
+  y32 = __double2float_rn(ry) * fast_rcp(r32);
+  if (clip && (y32 < mc.ylo || y32 > mc.yhi)) {
+    y32 = y32 < mc.ylo ? mc.ylo : mc.yhi;
+    ry = double(y32) * r;
+  }
+  double p, c;
+  const bool ok = eos_mixture_partial(r, ry, p, c);
+  p32 = float(p);
+  c32 = float(c);
+  return ok;
 }
 
 // FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
 template <int MODEL>
 __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const float *q, bool clip, FS &s) {
-  s.r = state_rho<MODEL>(q[0]);
-  const float rinv = fast_rcp(s.r);
-  s.u = q[1] * rinv;
-  s.v = q[2] * rinv;
-  s.w = q[3] * rinv;
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) s.q[v] = q[v];
   if (MODEL == 1) {
+    s.r = q[0];
+    const float rinv = fast_rcp(s.r);
+    s.u = q[1] * rinv;
+    s.v = q[2] * rinv;
+    s.w = q[3] * rinv;
     s.e = q[4];
     const float ke = fmaf(s.w, s.w, fmaf(s.v, s.v, s.u * s.u));
     const float e_int = fmaf(-0.5f, ke, s.e * rinv);
@@ -192,61 +270,37 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
     s.y = 0.0f;
     return true;
   }
-  // model 3: mass fraction in FP32, pressure inversion in FP64
-  s.y = q[4] * rinv;
-  if (clip) {
-    s.y = s.y < mc.ylo ? mc.ylo : s.y;
-    s.y = s.y > mc.yhi ? mc.yhi : s.y;
-  }
-  double p, c;
-  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
-  s.p = float(p);
-  s.c = float(c);
+  // model 3: pressure inversion in FP64 on the paired words
+  const bool ok = mixture_face_eos(mc, q, clip, s.r, s.y, s.p, s.c);
+  const float rinv = fast_rcp(s.r);
+  s.u = q[1] * rinv;
+  s.v = q[2] * rinv;
+  s.w = q[3] * rinv;
   s.e = 0.0f;
   return ok;
 }
 
-// Boundary ghost (bc.c:19-49) from the own face state.
+// Value across a boundary face (deltavalues.c:9-14; bc.c:19-49): the own
+// state (transmissive), the inflow state, or the own state with the momentum
+// mirrored as such (slip wall: normal component; no-slip wall: all of it),
+// which on the axis-aligned faces is exact, as in the FP64 path.
 template <int MODEL>
-__device__ __forceinline__ void mixed_ghost(const MixedConst &mc, int bc, int f, FS &g) {
+__device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float *own, float *nb) {
+#pragma unroll
+  for (int v = 0; v < kNv<MODEL>; ++v) nb[v] = own[v];
   if (bc == 1) {
-    mixed_face_state<MODEL>(mc, mc.inflow, false, g);
-  } else if (bc == 3 || bc == 4) {
-    // velocity and momentum mirrored as such (the momentum is not rebuilt as
-    // rho * u): exact on the axis-aligned faces, as in the FP64 path
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) nb[v] = mc.inflow[v];
+  } else if (bc == 3) {
     const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
-    if (bc == 3) {
-      const float un = fmaf(g.w, nz, fmaf(g.v, ny, g.u * nx));
-      g.u = fmaf(-2.0f * un, nx, g.u);
-      g.v = fmaf(-2.0f * un, ny, g.v);
-      g.w = fmaf(-2.0f * un, nz, g.w);
-      const float mn = fmaf(g.q[3], nz, fmaf(g.q[2], ny, g.q[1] * nx));
-      g.q[1] = fmaf(-2.0f * mn, nx, g.q[1]);
-      g.q[2] = fmaf(-2.0f * mn, ny, g.q[2]);
-      g.q[3] = fmaf(-2.0f * mn, nz, g.q[3]);
-    } else {
-      g.u = -g.u;
-      g.v = -g.v;
-      g.w = -g.w;
-      g.q[1] = -g.q[1];
-      g.q[2] = -g.q[2];
-      g.q[3] = -g.q[3];
-    }
-  }
-}
-
-// value across a boundary face: the own state, or its ghost (deltavalues.c:9-14)
-template <int MODEL>
-__device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int f, const float own[kNeqMax],
-                                               float nb[kNeqMax]) {
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) nb[v] = own[v];
-  if (bc == 1 || bc == 3 || bc == 4) {
-    FS g;
-    mixed_face_state<MODEL>(mc, own, false, g);
-    mixed_ghost<MODEL>(mc, bc, f, g);
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) nb[v] = g.q[v];
+    const float mn = fmaf(own[3], nz, fmaf(own[2], ny, own[1] * nx));
+    nb[1] = fmaf(-2.0f * mn, nx, own[1]);
+    nb[2] = fmaf(-2.0f * mn, ny, own[2]);
+    nb[3] = fmaf(-2.0f * mn, nz, own[3]);
+  } else if (bc == 4) {
+    nb[1] = -own[1];
+    nb[2] = -own[2];
+    nb[3] = -own[3];
   }
 }
 
@@ -341,15 +395,15 @@ __device__ __forceinline__ void frame_out(int f, float a, float b, float c, floa
 }
 
 template <int MODEL, int F = -1>
-__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float q[kNeqMax], bool clip, LS &s) {
-  s.r = state_rho<MODEL>(q[0]);
-  s.q4 = q[4];
-  frame_in<F>(f, q, s.mn, s.mm, s.ml);
-  const float rinv = fast_rcp(s.r);
-  s.un = s.mn * rinv;
-  s.um = s.mm * rinv;
-  s.ul = s.ml * rinv;
+__device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const float *q, bool clip, LS &s) {
   if (MODEL == 1) {
+    s.r = q[0];
+    s.q4 = q[4];
+    frame_in<F>(f, q, s.mn, s.mm, s.ml);
+    const float rinv = fast_rcp(s.r);
+    s.un = s.mn * rinv;
+    s.um = s.mm * rinv;
+    s.ul = s.ml * rinv;
     s.e = q[4];
     s.y = 0.0f;
     // p = (gamma - 1) (E - rho |u|^2 / 2) - gamma pinf, rho |u|^2 as m . u
@@ -358,16 +412,15 @@ __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const f
     s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
     return true;
   }
+  // model 3: pressure inversion in FP64 on the paired words
+  const bool ok = mixture_face_eos(mc, q, clip, s.r, s.y, s.p, s.c);
+  s.q4 = q[4];
+  frame_in<F>(f, q, s.mn, s.mm, s.ml);
+  const float rinv = fast_rcp(s.r);
+  s.un = s.mn * rinv;
+  s.um = s.mm * rinv;
+  s.ul = s.ml * rinv;
   s.e = 0.0f;
-  s.y = q[4] * rinv;
-  if (clip) {
-    s.y = s.y < mc.ylo ? mc.ylo : s.y;
-    s.y = s.y > mc.yhi ? mc.yhi : s.y;
-  }
-  double p, c;
-  const bool ok = eos_mixture(state_rho_d<MODEL>(q[0]), double(s.y), p, c);
-  s.p = float(p);
-  s.c = float(c);
   return ok;
 }
 
@@ -537,7 +590,7 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
 // CFL radius at the last stage.  Returns the cell's CFL radius (0 otherwise).
 template <int MODEL>
 __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageArgs &a, int c, float dtv,
-                                             const float R[kNeqMax], bool ok, float qn[kNeqMax]) {
+                                             const float R[kNeqMax], bool ok, float qn[kNvMax]) {
   const int n = a.n;
   bool finite = true;
 #pragma unroll
@@ -560,13 +613,15 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     }
   }
   if (a.last) {
+    double snew[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
-      const double snew = __ldg(a.SN + v * n + c) + double(dn[v]);
-      a.SNout[v * n + c] = snew;
-      qn[v] = to_state_f32<MODEL>(v, snew);
-      a.SNfout[v * n + c] = qn[v];
+      snew[v] = __ldg(a.SN + v * n + c) + double(dn[v]);
+      a.SNout[v * n + c] = snew[v];
     }
+    to_state_words<MODEL>(snew, qn);
+#pragma unroll
+    for (int v = 0; v < kNv<MODEL>; ++v) a.SNfout[v * n + c] = qn[v];
     return true;
   }
 #pragma unroll
@@ -574,30 +629,42 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     a.Dout[v * n + c] = dn[v];
     a.Sout[v * n + c] = __ldg(a.SNf + v * n + c) + dn[v];  // the value the next stage would form
   }
+  if constexpr (MODEL == 3) {  // paired words: the next stage's input to FP64 rounding
+#pragma unroll
+    for (int v = 0; v < kNeqMax; v += 4) {
+      float w[kNvMax];
+      w[v] = __ldg(a.SNf + v * n + c);
+      w[lo_word(v)] = __ldg(a.SNf + lo_word(v) * n + c);
+      set_pair(w, v, pair_d(w, v) + double(dn[v]));
+      a.Sout[v * n + c] = w[v];
+      a.Sout[lo_word(v) * n + c] = w[lo_word(v)];
+    }
+  }
   return false;
 }
 
 // stage state of any cell from global memory (SNf + D, written by the
 // previous stage)
-__device__ __forceinline__ void global_state(const MixedConst &mc, const StageArgs &a, int x, float q[kNeqMax]) {
+template <int MODEL>
+__device__ __forceinline__ void global_state(const StageArgs &a, int x, float *q) {
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) q[v] = v < mc.neq ? __ldg(a.Sin + v * a.n + x) : 0.0f;
+  for (int v = 0; v < kNv<MODEL>; ++v) q[v] = __ldg(a.Sin + v * a.n + x);
 }
 
 // ============================ viscous terms =================================
 
 // Cartesian velocity of the ghost across a boundary face f (bc.c:19-49) from
 // the own face values q.
-__device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float q[kNeqMax],
-                                               float u[3]) {
-  if (bc == 1) {
-    const float rinv = fast_rcp(state_rho_rt(mc.model, mc.inflow[0]));
+template <int MODEL>
+__device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int f, const float *q, float u[3]) {
+  if (bc == 1) {  // the inflow state (state form: model 3 holds rho - kRhoOff)
+    const float rinv = fast_rcp(MODEL == 3 ? mc.inflow[0] + kRhoOffF : mc.inflow[0]);
     u[0] = mc.inflow[1] * rinv;
     u[1] = mc.inflow[2] * rinv;
     u[2] = mc.inflow[3] * rinv;
     return;
   }
-  const float rinv = fast_rcp(state_rho_rt(mc.model, q[0]));
+  const float rinv = fast_rcp(state_rho<MODEL>(q));
   u[0] = q[1] * rinv;
   u[1] = q[2] * rinv;
   u[2] = q[3] * rinv;
@@ -617,20 +684,20 @@ __device__ __forceinline__ void ghost_velocity(const MixedConst &mc, int bc, int
 // FV . n of one face (flux_viscous.c:57-232 with turb = 0) from the face
 // values of both sides (bc > 0: a boundary face, the other side is the
 // ghost of lo) and the momentum gradients of both cells, FP32.
-__device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int bc, const float lo[kNeqMax],
-                                               const float hi[kNeqMax], const float gl[9], const float gh[9],
-                                               float FVn[kNeqMax]) {
+template <int MODEL>
+__device__ __forceinline__ void viscous_normal(const MixedConst &mc, int f, int bc, const float *lo, const float *hi,
+                                               const float gl[9], const float gh[9], float FVn[kNeqMax]) {
   float ul[3], uh[3];
   {
-    const float rinv = fast_rcp(state_rho_rt(mc.model, lo[0]));
+    const float rinv = fast_rcp(state_rho<MODEL>(lo));
     ul[0] = lo[1] * rinv;
     ul[1] = lo[2] * rinv;
     ul[2] = lo[3] * rinv;
   }
   if (bc > 0) {
-    ghost_velocity(mc, bc, f, lo, uh);
+    ghost_velocity<MODEL>(mc, bc, f, lo, uh);
   } else {
-    const float rinv = fast_rcp(state_rho_rt(mc.model, hi[0]));
+    const float rinv = fast_rcp(state_rho<MODEL>(hi));
     uh[0] = hi[1] * rinv;
     uh[1] = hi[2] * rinv;
     uh[2] = hi[3] * rinv;
@@ -671,9 +738,8 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
   const int c = blockIdx.x * kBlock + threadIdx.x;
   const int n = a.n;
   if (c >= n) return;
-  float q[kNeqMax];
-#pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) q[v] = __ldg(a.Sin + v * n + c);
+  float q[kNvMax];
+  global_state<MODEL>(a, c, q);
   const int32_t g = __ldg(a.geom + c);
   const int lev = level_of(g);
   const float inv_vol = a.geo->inv_vol[lev];
@@ -699,8 +765,8 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
         m[2] = mc.inflow[3];
       } else {
         float u[3];
-        ghost_velocity(mc, bc, f, q, u);
-        const float rho = state_rho<MODEL>(q[0]);
+        ghost_velocity<MODEL>(mc, bc, f, q, u);
+        const float rho = state_rho<MODEL>(q);
         m[0] = rho * u[0];
         m[1] = rho * u[1];
         m[2] = rho * u[2];
@@ -730,8 +796,39 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
 
 // ============================ general kernel ================================
 
+// Model 3: the FP64 minmod slope of a paired word (reconctruct_V3.c:17-43,
+// as minmod_slope).
+__device__ __forceinline__ double minmod_slope_d(bool active, double d0, double d1, double inv_p, double inv_m) {
+  const double sp = d0 * inv_p, sm = -d1 * inv_m;
+  const double m = fabs(sm) > fabs(sp) ? sp : sm;
+  return (active && fabs(d0) > 1e-10 && sm * sp > 0.0) ? m : 0.0;
+}
+
+// Model 3: face value of face f of a cell with geometry code gx from its
+// state words and the values across f (nbf) and across the opposite face
+// (nbo): the momentum as recon_face does, the paired words in FP64.
+__device__ __forceinline__ void recon_face_m3(const GeoTables *geo, int32_t gx, int f, const float *qx,
+                                              const float *nbf, const float *nbo, float *out) {
+  const int lev = level_of(gx);
+  const int rf = rel_of(gx, f), ro = rel_of(gx, opp_face(f));
+  const float *gf = geo_face(geo, lev, f, rf);
+  const float dcf = gf[0], inv_p = gf[1];
+  const float inv_m = geo_face(geo, lev, opp_face(f), ro)[1];
+  const bool act = rf != kRelBoundary;
+#pragma unroll
+  for (int v = 1; v < 4; ++v)
+    out[v] = fmaf(dcf, minmod_slope(act, nbf[v] - qx[v], nbo[v] - qx[v], inv_p, inv_m), qx[v]);
+#pragma unroll
+  for (int v = 0; v < kNeqMax; v += 4) {
+    const double q = pair_d(qx, v);
+    const double sl = minmod_slope_d(act, pair_d(nbf, v) - q, pair_d(nbo, v) - q, double(inv_p), double(inv_m));
+    set_pair(out, v, fma(double(dcf), sl, q));
+  }
+}
+
 template <int MODEL>
 struct Block {
+  static constexpr int NV = kNv<MODEL>;
   const StageArgs &a;
   const MixedConst &mc;
   int c0, cnt;
@@ -739,55 +836,71 @@ struct Block {
   __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock])
       : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_) {}
   __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(cnt); }
-  __device__ __forceinline__ void state(int x, float q[kNeqMax]) const {
+  __device__ __forceinline__ void state(int x, float *q) const {
     if (in_block(x)) {
 #pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) q[v] = st[v][x - c0];
+      for (int v = 0; v < NV; ++v) q[v] = st[v][x - c0];
       return;
     }
-    global_state(mc, a, x, q);
+    global_state<MODEL>(a, x, q);
   }
   // value across face f of cell x (deltavalues.c): single neighbour, mean of
-  // the four fine ones, or the boundary ghost
-  __device__ __forceinline__ void across(int x, int f, const float own[kNeqMax], float nb[kNeqMax]) const {
+  // the four fine ones (model 3: the paired words summed in FP64), or the
+  // boundary ghost
+  __device__ __forceinline__ void across(int x, int f, const float *own, float *nb) const {
     const int32_t code = __ldg(a.nbr + f * a.n + x);
     if (code >= 0) {
       state(code, nb);
     } else if (is_hanging(code)) {
       const int32_t *k = a.hang_nbr + 4 * hang_index(code);
       float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      double acc2[2] = {0.0, 0.0};
 #pragma unroll 1
       for (int s = 0; s < 4; ++s) {
-        float q[kNeqMax];
+        float q[kNvMax];
         state(__ldg(k + s), q);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
+        if constexpr (MODEL == 3) {
+          acc2[0] += pair_d(q, 0);
+          acc2[1] += pair_d(q, 4);
+        }
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
+      if constexpr (MODEL == 3) {
+        set_pair(nb, 0, 0.25 * acc2[0]);
+        set_pair(nb, 4, 0.25 * acc2[1]);
+      }
     } else {
       boundary_value<MODEL>(mc, -1 - code, f, own, nb);
     }
   }
   // face value of face f of any cell (used across block edges)
-  __device__ __forceinline__ void recon_any(int x, int f, float out[kNeqMax]) const {
-    float qx[kNeqMax], nbp[kNeqMax], nbm[kNeqMax], d0[kNeqMax], d1[kNeqMax];
+  __device__ __forceinline__ void recon_any(int x, int f, float *out) const {
+    float qx[kNvMax], nbp[kNvMax], nbm[kNvMax];
     state(x, qx);
     across(x, f, qx, nbp);
     across(x, opp_face(f), qx, nbm);
+    if constexpr (MODEL == 3) {
+      recon_face_m3(a.geo, __ldg(a.geom + x), f, qx, nbp, nbm, out);
+    } else {
+      float d0[kNeqMax], d1[kNeqMax];
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      d0[v] = nbp[v] - qx[v];
-      d1[v] = nbm[v] - qx[v];
+      for (int v = 0; v < kNeqMax; ++v) {
+        d0[v] = nbp[v] - qx[v];
+        d1[v] = nbm[v] - qx[v];
+      }
+      recon_face(a.geo, __ldg(a.geom + x), f, qx, d0, d1, out);
     }
-    recon_face(a.geo, __ldg(a.geom + x), f, qx, d0, d1, out);
   }
 };
 
 template <int MODEL, bool MUSCL>
 __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageArgs a) {
-  __shared__ float st[kNeqMax][kBlock];
-  __shared__ float sf[6][kNeqMax][kBlock];
+  constexpr int NV = kNv<MODEL>;
+  __shared__ float st[NV][kBlock];
+  __shared__ float sf[6][NV][kBlock];
   __shared__ float fp[3][kNeqMax][kBlock];
   __shared__ float s_dt;
   const BlockDesc bd = a.blocks[blockIdx.x];
@@ -796,15 +909,14 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
   const int c = c0 + t;
   const int n = a.n;
   const bool active = t < bd.count;
-  constexpr int neq = kNeqMax;  // models 1 and 3: five conservative variables
   constexpr bool muscl = MUSCL;
   Block<MODEL> blk(a, mc, c0, bd.count, st);
 
   // A: own stage state
-  float q[kNeqMax];
+  float q[kNvMax];
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) {
-    q[v] = (active && v < neq) ? __ldg(a.Sin + v * n + c) : 0.0f;
+  for (int v = 0; v < NV; ++v) {
+    q[v] = active ? __ldg(a.Sin + v * n + c) : 0.0f;
     st[v][t] = q[v];
   }
   int32_t nb[6];
@@ -817,7 +929,23 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
 
   // B: own face values
   if (active) {
-    if (muscl) {
+    if (muscl && MODEL == 3) {
+      // one axis at a time: the values across its two faces, both face values
+#pragma unroll 1
+      for (int f = 0; f < 6; ++f) {
+        if (f == 2 || f == 3 || f == 5) continue;  // the lower face of each pair carries the axis
+        const int fo = opp_face(f);
+        float nbf[kNvMax], nbo[kNvMax], o[kNvMax];
+        blk.across(c, f, q, nbf);
+        blk.across(c, fo, q, nbo);
+        recon_face_m3(a.geo, g, f, q, nbf, nbo, o);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sf[f][v][t] = o[v];
+        recon_face_m3(a.geo, g, fo, q, nbo, nbf, o);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sf[fo][v][t] = o[v];
+      }
+    } else if (muscl) {
       float dl[6][kNeqMax];
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
@@ -837,7 +965,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
 #pragma unroll
       for (int f = 0; f < 6; ++f)
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = q[v];
+        for (int v = 0; v < NV; ++v) sf[f][v][t] = q[v];
     }
   }
   __syncthreads();
@@ -872,16 +1000,16 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
       } else {
-        float own[kNeqMax], oth[kNeqMax];
+        float own[kNvMax], oth[kNvMax];
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) {
+        for (int v = 0; v < NV; ++v) {
           own[v] = sf[f][v][t];
           oth[v] = own[v];
         }
         if (!boundary) {
           if (blk.in_block(other)) {
 #pragma unroll
-            for (int v = 0; v < kNeqMax; ++v) oth[v] = sf[fo][v][other - c0];
+            for (int v = 0; v < NV; ++v) oth[v] = sf[fo][v][other - c0];
           } else if (muscl) {
             blk.recon_any(other, fo, oth);
           } else {
@@ -890,9 +1018,9 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
         }
         // canonical orientation: lower side first, frame of the lower cell's + face
         const bool own_low = plus || boundary;
-        float lo[kNeqMax], hi[kNeqMax];
+        float lo[kNvMax], hi[kNvMax];
 #pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) {
+        for (int v = 0; v < NV; ++v) {
           lo[v] = own_low ? own[v] : oth[v];
           hi[v] = own_low ? oth[v] : own[v];
         }
@@ -902,7 +1030,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
           const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
           load_grad9f(a.SG, n, clo, gl);
           load_grad9f(a.SG, n, chi, gh);
-          viscous_normal(mc, own_low ? f : fo, boundary ? -1 - code : 0, lo, hi, gl, gh, FVn);
+          viscous_normal<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, lo, hi, gl, gh, FVn);
 #pragma unroll
           for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
         }
@@ -919,7 +1047,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageAr
 
   float lam = 0.0f;
   if (active) {
-    float qn[kNeqMax];
+    float qn[kNvMax];
     const float dtv = s_dt * a.geo->inv_vol[level_of(g)];
     if (stage_update<MODEL>(mc, a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
   }
@@ -1321,7 +1449,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     float gl[9], gh[9], FVn[kNeqMax];
     load_grad9f(a.SG, n, clo, gl);
     load_grad9f(a.SG, n, chi, gh);
-    viscous_normal(mc, f, bc, lo, hi, gl, gh, FVn);
+    viscous_normal<MODEL>(mc, f, bc, lo, hi, gl, gh, FVn);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
   };
@@ -1436,18 +1564,30 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   add_face(3, sx_m, false);
   add_face(0, sy_m, false);
   add_face(4, sz_m, false);
-  float qn[kNeqMax], lam = 0.0f;
+  float qn[kNvMax], lam = 0.0f;
   if (stage_update<MODEL>(mc, a, c, s_dtv, R, ok, qn) && a.lambda)
     lam = brick_lambda<MODEL>(mc, qn, be, s_geo, s_inv2vol);
   if (a.last && a.lambda) block_max_lambda_f<NB>(lam, a.lambda);
 }
 
-// FP32 copy of an FP64 state (after an upload or an FP64-path step).
-// The first n values (the density) are shifted by off (model 3: kRhoOffD).
-__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count, int64_t n,
-                               double off) {
+// FP32 copy of an FP64 state (after an upload or an FP64-path step), model
+// 1: the count = neq * n values word for word.
+__global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__ Sf, int64_t count) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-    Sf[i] = __double2float_rn(i < n ? S[i] - off : S[i]);
+    Sf[i] = __double2float_rn(S[i]);
+}
+
+// The same for model 3, one cell per thread: seven state words per cell.
+__global__ void k_state_to_f32_m3(const double *__restrict__ S, float *__restrict__ Sf, int64_t n) {
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
+    double x[kNeqMax];
+    float q[kNvMax];
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) x[v] = S[v * n + c];
+    to_state_words<3>(x, q);
+#pragma unroll
+    for (int v = 0; v < kNv<3>; ++v) Sf[v * n + c] = q[v];
+  }
 }
 
 // The same with the CFL spectral radius of the copied state (the mixed
@@ -1458,13 +1598,13 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
                                                                 float *__restrict__ Sf, int n, double *lambda) {
   float lam = 0.0f;
   for (int c = blockIdx.x * kBlock + threadIdx.x; c < n; c += gridDim.x * kBlock) {
-    float q[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    double x[kNeqMax];
+    float q[kNvMax];
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) {
-      if (v >= mc.neq) break;
-      q[v] = to_state_f32<MODEL>(v, S[int64_t(v) * n + c]);
-      Sf[int64_t(v) * n + c] = q[v];
-    }
+    for (int v = 0; v < kNeqMax; ++v) x[v] = S[int64_t(v) * n + c];
+    to_state_words<MODEL>(x, q);
+#pragma unroll
+    for (int v = 0; v < kNv<MODEL>; ++v) Sf[int64_t(v) * n + c] = q[v];
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
   block_max_lambda_f(lam, lambda);
@@ -1480,10 +1620,17 @@ MixedConst make_const(const Phys &ph) {
   mc.gpinf = float(ph.gamma * ph.pinf);
   mc.ylo = float(ph.ymin / 1000.0);
   mc.yhi = float(1.0 - ph.ymin / 1000.0);
-  // the inflow ghost in FP32 state form (model 3 holds rho - kRhoOff; the
-  // library accepts inflow boundaries for model 1 only)
-  for (int v = 0; v < kNeqMax; ++v)
-    mc.inflow[v] = float(ph.model == 3 && v == 0 ? ph.inflow[0] - kRhoOffD : ph.inflow[v]);
+  // the inflow ghost in FP32 state form (model 3: the paired words of
+  // rho - kRhoOff and rho Y; the library accepts inflow boundaries for model
+  // 1 only)
+  for (int v = 0; v < kNeqMax; ++v) mc.inflow[v] = float(ph.inflow[v]);
+  if (ph.model == 3) {
+    for (int v = 0; v < kNeqMax; v += 4) {
+      const double x = v == 0 ? ph.inflow[0] - kRhoOffD : ph.inflow[4];
+      mc.inflow[v] = float(x);
+      mc.inflow[lo_word(v)] = float(x - double(mc.inflow[v]));
+    }
+  }
   mc.model = ph.model;
   mc.neq = ph.neq;
   mc.ischeme = ph.ischeme;
@@ -1723,9 +1870,10 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   // bubble: 30 % fewer general cells, 4 % more general-kernel time).
   std::vector<char> is_block8(size_t(n), 0), is_brick8(size_t(n), 0), in_brick8(size_t(n), 0);
   std::vector<char> is_block4(size_t(n), 0), is_brick4(size_t(n), 0);
-  // bricks for every inviscid run and for viscous runs of model 1 (both
-  // kernels read the cells' gradients straight from the gradient pass)
-  if (!r.force_general && (ph.ns != 1 || ph.model == 1)) {
+  // bricks for model 1, inviscid or viscous (both kernels read the cells'
+  // gradients straight from the gradient pass); model 3 (paired state words,
+  // FP64 reconstruction of the partial densities) runs the general kernel
+  if (!r.force_general && ph.model == 1) {
     find_blocks<Brick8>(m, is_block8);
     for (int64_t i = 0; i < n; ++i)
       if (is_block8[size_t(i)] && brick_sides_resolve<Brick8>(m, i, is_block8)) {
@@ -1776,6 +1924,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   std::vector<BlockDesc> all(bricks);
   all.insert(all.end(), bricks4.begin(), bricks4.end());
   all.insert(all.end(), general.begin(), general.end());
+  const int64_t nv = ph.model == 3 ? kNv<3> : kNv<1>;  // FP32 state words per cell
   cudaError_t e;
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -1787,10 +1936,10 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
       (e = alloc_slot(r, kBufD1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufD2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufAlt, sizeof(double) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNf, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX1, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
-      (e = alloc_slot(r, kBufX2, sizeof(float) * kNeqMax * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNf, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufSNfAlt, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX1, sizeof(float) * nv * n)) != cudaSuccess ||
+      (e = alloc_slot(r, kBufX2, sizeof(float) * nv * n)) != cudaSuccess ||
       (e = alloc_slot(r, kBufSG, ph.ns == 1 ? sizeof(float) * 9 * n : 16)) != cudaSuccess) {
     snprintf(why, whylen, "mixed-path allocation: %s", cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? FVGPU_ERR_NOMEM : FVGPU_ERR_CUDA;
@@ -1838,8 +1987,10 @@ void release_mixed(MixedResources &r) {
 
 cudaError_t mixed_refresh_f32(MixedResources &r, const double *S, int neq, LaunchMarks &marks, cudaStream_t st) {
   marks.mark(FVGPU_KIND_MIXED_AUX);
-  k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n, r.n,
-                                       r.model == 3 ? kRhoOffD : 0.0);
+  if (r.model == 3)
+    k_state_to_f32_m3<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), r.n);
+  else
+    k_state_to_f32<<<1024, 256, 0, st>>>(S, static_cast<float *>(r.buf[kBufSNf]), int64_t(neq) * r.n);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) r.snf_valid = true;
   return e;
@@ -1865,23 +2016,22 @@ cudaError_t mixed_refresh_f32_lambda(MixedResources &r, const Phys &ph, const do
 // the kernel instance of the configuration (EOS model, reconstruction order)
 template <int MODEL, bool MUSCL, class S>
 void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
-  if (mc.ns == 1) {
-    if constexpr (MODEL == 1) k_mixed_brick<MODEL, MUSCL, true, S><<<grid, S::N, 0, st>>>(mc, a);
-  } else {
+  static_assert(MODEL == 1, "bricks serve model 1");
+  if (mc.ns == 1)
+    k_mixed_brick<MODEL, MUSCL, true, S><<<grid, S::N, 0, st>>>(mc, a);
+  else
     k_mixed_brick<MODEL, MUSCL, false, S><<<grid, S::N, 0, st>>>(mc, a);
-  }
 }
 
 enum BlockKind { kKindGeneral = 0, kKindBrick8 = 1, kKindBrick4 = 2 };
 
 template <int MODEL, bool MUSCL>
 void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
-  if (kind == kKindBrick8)
-    launch_brick<MODEL, MUSCL, Brick8>(grid, mc, a, st);
-  else if (kind == kKindBrick4)
-    launch_brick<MODEL, MUSCL, Brick4>(grid, mc, a, st);
-  else
-    k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+  if constexpr (MODEL == 1) {
+    if (kind == kKindBrick8) return launch_brick<MODEL, MUSCL, Brick8>(grid, mc, a, st);
+    if (kind == kKindBrick4) return launch_brick<MODEL, MUSCL, Brick4>(grid, mc, a, st);
+  }
+  k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
 }
 
 void launch_kernel(const Phys &ph, int kind, unsigned grid, const MixedConst &mc, const StageArgs &a,
