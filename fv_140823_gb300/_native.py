@@ -39,6 +39,8 @@ def load_mesh_lib() -> C.CDLL:
         lib.fvmesh_sizes.argtypes = [vp, i64p, i64p]
         lib.fvmesh_leaves.argtypes = [vp, vp, vp]
         lib.fvmesh_refine.argtypes = [vp, vp, C.c_int]
+        lib.fvmesh_adapt.argtypes = [vp, vp, C.c_int, C.c_int]
+        lib.fvmesh_transfer.argtypes = [vp, C.c_int, C.c_int64, vp, vp]
         lib.fvmesh_flatten.argtypes = [vp, vp]
         lib.fvmesh_cell_nodes.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
         lib.fvmesh_domain.argtypes = [vp, vp, vp, vp, vp]

@@ -41,6 +41,7 @@ class Case:
     cfl: float
     nsteps: int
     scheme: str = "ssprk3"
+    mesh: OctreeMesh | None = None  # the host octree the tables were flattened from
 
 
 def conservative_ideal(rho, u, v, w, p, gamma=GAMMA, pinf=0.0):
@@ -134,7 +135,7 @@ def bubble(base_level: int = 4, extra_levels: int = 3, threshold: float = 0.05) 
     h = np.ldexp(1.0, -t.level.astype(np.int64))
     U = _bubble_state(t.centroid, h)
     cfg = SolverConfig(model=3, ischeme=2, ymin=1e-6)
-    return Case("bubble", t, U, cfg, cfl=0.5, nsteps=200)
+    return Case("bubble", t, U, cfg, cfl=0.5, nsteps=200, mesh=m)
 
 
 def bump(base_level: int = 5, extra_levels: int = 2, seed: int = 7, radius: float = 0.2) -> Case:

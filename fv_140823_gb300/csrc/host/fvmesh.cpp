@@ -11,6 +11,7 @@
 #include "fvmesh.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -112,6 +113,12 @@ struct fvmesh {
   int side_bc[6];
   std::vector<Leaf> leaves;
   LeafTable table;
+  // State-transfer plan of the last fvmesh_adapt: per current leaf, the leaf
+  // of the mesh before it that it descends from (>= 0), or -1 - g for the
+  // parent that merge group g (8 former leaves, child order) formed.
+  std::vector<int32_t> src;
+  std::vector<std::array<int32_t, 8>> groups;
+  int64_t n_before = -1;  // leaves before the last fvmesh_adapt (-1: no plan)
 
   double h(int level, int a) const { return std::ldexp(len[a], -level); }
   // Coordinate of grid line I at `level` along axis a.  Because h(level+1) is
@@ -158,15 +165,23 @@ struct fvmesh {
     return true;
   }
 
-  void sort_and_index() {
-    std::vector<std::pair<uint64_t, Leaf>> tmp;
+  // Leaves along the Morton curve; `carry` (one entry per leaf) follows them.
+  void sort_and_index(std::vector<int32_t> *carry = nullptr) {
+    std::vector<std::pair<uint64_t, size_t>> tmp;
     tmp.reserve(leaves.size());
-    for (const Leaf &L : leaves) tmp.emplace_back(morton(L), L);
+    for (size_t n = 0; n < leaves.size(); ++n) tmp.emplace_back(morton(leaves[n]), n);
     std::sort(tmp.begin(), tmp.end(),
-              [](const std::pair<uint64_t, Leaf> &x, const std::pair<uint64_t, Leaf> &y) {
+              [](const std::pair<uint64_t, size_t> &x, const std::pair<uint64_t, size_t> &y) {
                 return x.first < y.first;
               });
-    for (size_t n = 0; n < tmp.size(); ++n) leaves[n] = tmp[n].second;
+    std::vector<Leaf> next(leaves.size());
+    for (size_t n = 0; n < tmp.size(); ++n) next[n] = leaves[tmp[n].second];
+    leaves.swap(next);
+    if (carry) {
+      std::vector<int32_t> c(carry->size());
+      for (size_t n = 0; n < tmp.size(); ++n) c[n] = (*carry)[tmp[n].second];
+      carry->swap(c);
+    }
     table.build(leaves);
   }
 
@@ -196,28 +211,34 @@ struct fvmesh {
     return -1;
   }
 
-  void refine_set(const std::vector<uint8_t> &mark) {
+  // Splits the marked leaves into their 8 children (child ch at offset
+  // bit0 = +x, bit1 = +y, bit2 = +z); children inherit the `carry` entry.
+  void refine_set(const std::vector<uint8_t> &mark, std::vector<int32_t> *carry = nullptr) {
     std::vector<Leaf> next;
-    next.reserve(leaves.size() + 7 * size_t(std::count(mark.begin(), mark.end(), 1)));
+    std::vector<int32_t> cnext;
+    const size_t grow = 7 * size_t(std::count(mark.begin(), mark.end(), 1));
+    next.reserve(leaves.size() + grow);
+    if (carry) cnext.reserve(leaves.size() + grow);
     for (size_t n = 0; n < leaves.size(); ++n) {
       const Leaf &L = leaves[n];
-      if (!mark[n]) {
-        next.push_back(L);
-        continue;
-      }
-      for (int ch = 0; ch < 8; ++ch) {
-        Leaf C;
-        C.level = L.level + 1;
-        for (int a = 0; a < 3; ++a) C.p[a] = 2 * L.p[a] + ((ch >> a) & 1);
+      const int nc = mark[n] ? 8 : 1;
+      for (int ch = 0; ch < nc; ++ch) {
+        Leaf C = L;
+        if (mark[n]) {
+          C.level = L.level + 1;
+          for (int a = 0; a < 3; ++a) C.p[a] = 2 * L.p[a] + ((ch >> a) & 1);
+        }
         next.push_back(C);
+        if (carry) cnext.push_back((*carry)[n]);
       }
     }
     leaves.swap(next);
-    sort_and_index();
+    if (carry) carry->swap(cnext);
+    sort_and_index(carry);
   }
 
   // Refine until every face sees at most one level of difference.
-  int balance() {
+  int balance(std::vector<int32_t> *carry = nullptr) {
     for (int iter = 0; iter < 64; ++iter) {
       std::vector<uint8_t> mark(leaves.size(), 0);
       bool any = false;
@@ -257,9 +278,90 @@ struct fvmesh {
       for (size_t n = 0; n < leaves.size(); ++n)
         if (mark[n] && leaves[n].level >= FVMESH_MAX_LEVEL)
           return fail(FVMESH_ERR_LEVEL, "2:1 balancing needs a level above FVMESH_MAX_LEVEL");
-      refine_set(mark);
+      refine_set(mark, carry);
     }
     return fail(FVMESH_ERR_BALANCE, "2:1 balancing did not converge");
+  }
+
+  // One adaptation pass of meshadaptation.c:23-58 from the target levels
+  // `split` (criterionsplt.c), smoothed as criterionsmth.c does: a leaf
+  // moves at most one level; 8 sibling leaves that all ask for a coarser
+  // level merge into their parent (refineh_1.c:30-62), which keeps the
+  // average of their states (merge.c:93-101); a leaf that asks for a finer
+  // level splits and its children inherit its state (split.c:493); then 2:1
+  // face balance.  Levels stay within [min_level, max_level].  A merge that
+  // would leave the parent next to a face neighbour finer than the children
+  // (now, or after this pass's splits) is skipped, so no merge is undone by
+  // the balancing.
+  int adapt(const int32_t *split, int min_level, int max_level) {
+    const size_t n = leaves.size();
+    std::vector<int8_t> dir(n, 0);  // -1 coarser, +1 finer
+    for (size_t i = 0; i < n; ++i) {
+      const int want = std::min(std::max(int(split[i]), min_level), max_level);
+      dir[i] = want > leaves[i].level ? 1 : (want < leaves[i].level ? -1 : 0);
+    }
+    std::vector<int32_t> group_of(n, -1);
+    groups.clear();
+    for (size_t i = 0; i < n; ++i) {
+      const Leaf &L = leaves[i];
+      if (dir[i] >= 0 || L.level <= min_level || (L.p[0] | L.p[1] | L.p[2]) & 1) continue;
+      std::array<int32_t, 8> kids;
+      bool ok = true;
+      for (int ch = 0; ch < 8 && ok; ++ch) {
+        const int64_t q[3] = {L.p[0] + (ch & 1), L.p[1] + ((ch >> 1) & 1), L.p[2] + ((ch >> 2) & 1)};
+        kids[ch] = find(L.level, q);
+        ok = kids[ch] >= 0 && dir[size_t(kids[ch])] < 0;
+      }
+      if (!ok) continue;
+      // the parent's face neighbours: no leaf finer than the children, none
+      // of the children's level about to split
+      Leaf P;
+      P.level = L.level - 1;
+      for (int a = 0; a < 3; ++a) P.p[a] = L.p[a] / 2;
+      for (int f = 0; f < 6 && ok; ++f) {
+        int64_t w[3], u[3];
+        if (!neighbour_pos(P, f, w, u)) continue;
+        if (cover_level(P.level, w) >= 0) continue;  // a leaf at the parent's level or coarser
+        int64_t q[4][3];
+        near_children(P.level, w, f, q);
+        for (int s = 0; s < 4 && ok; ++s) {
+          const int32_t k = find(L.level, q[s]);
+          ok = k >= 0 && dir[size_t(k)] <= 0;
+        }
+      }
+      if (!ok) continue;
+      for (int ch = 0; ch < 8; ++ch) group_of[size_t(kids[ch])] = int32_t(groups.size());
+      groups.push_back(kids);
+    }
+    std::vector<Leaf> next;
+    std::vector<int32_t> carry;
+    next.reserve(n);
+    carry.reserve(n);
+    std::vector<uint8_t> split_mark;
+    for (size_t i = 0; i < n; ++i) {
+      const Leaf &L = leaves[i];
+      const int32_t g = group_of[i];
+      if (g >= 0) {
+        if (groups[size_t(g)][0] != int32_t(i)) continue;  // the first child stands for the group
+        Leaf P;
+        P.level = L.level - 1;
+        for (int a = 0; a < 3; ++a) P.p[a] = L.p[a] / 2;
+        next.push_back(P);
+        carry.push_back(-1 - g);
+        split_mark.push_back(0);
+        continue;
+      }
+      next.push_back(L);
+      carry.push_back(int32_t(i));
+      split_mark.push_back(dir[i] > 0 && L.level < max_level ? 1 : 0);
+    }
+    leaves.swap(next);
+    table.build(leaves);
+    refine_set(split_mark, &carry);
+    const int rc = balance(&carry);
+    src.swap(carry);
+    n_before = rc == 0 ? int64_t(n) : -1;
+    return rc;
   }
 };
 
@@ -358,6 +460,36 @@ int fvmesh_refine(fvmesh *m, const uint8_t *flags, int max_level) {
     mark[n] = (flags[n] && m->leaves[n].level < max_level) ? 1 : 0;
   m->refine_set(mark);
   return m->balance();
+}
+
+int fvmesh_adapt(fvmesh *m, const int32_t *split, int min_level, int max_level) {
+  if (!m || !split) return fail(FVMESH_ERR_ARG, "null argument");
+  if (min_level < 1 || max_level > FVMESH_MAX_LEVEL || min_level > max_level)
+    return fail(FVMESH_ERR_LEVEL, "need 1 <= min_level <= max_level <= FVMESH_MAX_LEVEL");
+  return m->adapt(split, min_level, max_level);
+}
+
+int fvmesh_transfer(const fvmesh *m, int neq, int64_t n_old, const double *S_old, double *S_new) {
+  if (!m || !S_old || !S_new || neq < 1) return fail(FVMESH_ERR_ARG, "null argument");
+  if (m->n_before < 0 || n_old != m->n_before)
+    return fail(FVMESH_ERR_ARG, "n_old is not the leaf count before the last fvmesh_adapt");
+  const int64_t n = int64_t(m->leaves.size());
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t s = m->src[size_t(i)];
+    for (int v = 0; v < neq; ++v) {
+      const double *col = S_old + int64_t(v) * n_old;
+      double x;
+      if (s >= 0) {
+        x = col[s];
+      } else {
+        // merge.c:93-101: the sum of the kids' states over nsplit, in kid order
+        x = 0.0;
+        for (int ch = 0; ch < 8; ++ch) x += col[m->groups[size_t(-1 - s)][size_t(ch)]] / 8.0;
+      }
+      S_new[int64_t(v) * n + i] = x;
+    }
+  }
+  return 0;
 }
 
 int fvmesh_cell_nodes(const fvmesh *m, int level, int i, int j, int k, double xyz[8][3]) {

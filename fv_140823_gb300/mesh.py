@@ -114,6 +114,24 @@ class OctreeMesh:
             raise ValueError("flags must have one entry per leaf")
         self._check(self._lib.fvmesh_refine(self._h, C.c_void_p(_p(f)), int(max_level)))
 
+    def adapt(self, split, min_level: int, max_level: int) -> None:
+        """One adaptation pass toward the per-leaf target levels `split`
+        (``fvmesh_adapt``: one level per pass, sibling merges, 2:1 balance)."""
+        sp = np.ascontiguousarray(np.asarray(split, dtype=np.int32))
+        if sp.shape != (self.ncells,):
+            raise ValueError("split must have one entry per leaf")
+        self._check(self._lib.fvmesh_adapt(self._h, C.c_void_p(_p(sp)), int(min_level), int(max_level)))
+
+    def transfer(self, S_old: np.ndarray) -> np.ndarray:
+        """State [neq][n_old] on the leaves before the last :meth:`adapt` ->
+        state on the current leaves (children inherit, merged parents average)."""
+        S_old = np.ascontiguousarray(S_old, dtype=np.float64)
+        neq, n_old = S_old.shape
+        S_new = np.empty((neq, self.ncells))
+        self._check(self._lib.fvmesh_transfer(self._h, int(neq), C.c_int64(n_old), C.c_void_p(_p(S_old)),
+                                              C.c_void_p(_p(S_new))))
+        return S_new
+
     def cell_nodes(self, level: int, i: int, j: int, k: int) -> np.ndarray:
         out = np.empty((8, 3), np.float64)
         self._check(self._lib.fvmesh_cell_nodes(self._h, level, i, j, k, C.c_void_p(_p(out))))

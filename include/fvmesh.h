@@ -87,6 +87,21 @@ int fvmesh_leaves(const fvmesh *m, int32_t *level, double *centroid /*[3][n]*/);
  * re-sorted along the Morton curve. */
 int fvmesh_refine(fvmesh *m, const uint8_t *flags, int max_level);
 
+/* One adaptation pass (meshadaptation.c:23-58) from per-leaf target levels
+ * split[ncells] (criterionsplt.c; fvgpu_criterion gives them): each leaf
+ * moves at most one level toward its target, as criterionsmth.c smooths it;
+ * 8 sibling leaves that all ask for a coarser level merge (refineh_1.c:30-62)
+ * unless the parent would sit next to a finer face neighbour; 2:1 face
+ * balance follows.  Levels stay within [min_level, max_level].  Records the
+ * state-transfer plan that fvmesh_transfer applies. */
+int fvmesh_adapt(fvmesh *m, const int32_t *split, int min_level, int max_level);
+
+/* State transfer of the last fvmesh_adapt: S_old [neq][n_old] on the leaves
+ * before it -> S_new [neq][ncells] on the current leaves.  A split leaf's
+ * children take its state (split.c:493); a merged parent takes the sum of its
+ * 8 children's states each divided by 8, in child order (merge.c:93-101). */
+int fvmesh_transfer(const fvmesh *m, int neq, int64_t n_old, const double *S_old, double *S_new);
+
 /* Fill the flattened tables (caller-allocated, sizes from fvmesh_sizes). */
 int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t);
 

@@ -14,9 +14,13 @@ The stored tables are the exact inputs the reference saw, so the fixtures pin
 any implementation that reads them (the oracle on every host, libfvgpu on the
 GPU) without the reference tree.  Needs the reference tree; run from the
 repository root:  python tests/golden/make_golden.py
+(`python tests/golden/make_golden.py fullsize` writes fullsize.json: the
+reference's 100-step Sod run as configured, see fullsize()).
 """
 from __future__ import annotations
 
+import hashlib
+import json
 import os
 import sys
 
@@ -29,7 +33,7 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 from fv_140823_gb300 import cases  # noqa: E402
 from fv_140823_gb300.mesh import refine_by, uniform_mesh  # noqa: E402
-from pyoracle import PhysConfig, RefHarness  # noqa: E402
+from pyoracle import Oracle, PhysConfig, RefHarness  # noqa: E402
 
 
 def _phys(cfg, dt, i_case=0):
@@ -99,5 +103,45 @@ def main():
     _save("inflow_l3", t5, c5, _random_ideal(t5.ncells, rng), 1e-3, "ssprk3", 2, i_case=200)
 
 
+def state_digest(S: np.ndarray) -> str:
+    """SHA-256 of the state's little-endian FP64 bytes, [neq][n] order."""
+    return hashlib.sha256(np.ascontiguousarray(S, dtype="<f8").tobytes()).hexdigest()
+
+
+def fullsize():
+    """The 3-D Sod tube as configured (32^3 leaves, MUSCL/minmod + HLLC,
+    SSP-RK3, 100 steps at CFL 0.5, transmissive sides) run by the reference's
+    own RK / residual code.  The reference has no CFL rule (inputset.c:90
+    reads a fixed dt): each step's dt comes from the oracle's CFL restatement
+    on the reference's own state.  Stored: the SHA-256 of the final state, its
+    per-field sums and the first and last dt (tests/golden/fullsize.json)."""
+    c = cases.sod(level=5)
+    orc = Oracle(c.tables, c.cfg)
+    ref = RefHarness(c.tables, _phys(c.cfg, 1.0))
+    S = c.U
+    dts = []
+    try:
+        for _ in range(100):
+            dt = orc.cfl_dt(S, 0.5)
+            dts.append(dt)
+            ref.set_dt(dt)
+            ref.set_state(S)
+            ref.step("ssprk3", 1)
+            S = ref.state()
+    finally:
+        ref.close()
+    out = {"c1_sod32_ssprk3_cfl05_100": {
+        "workload": "Sod tube, 32^3 uniform leaves, MUSCL/minmod + HLLC, SSP-RK3, CFL 0.5, 100 steps",
+        "ncells": int(c.tables.ncells), "steps": 100, "sha256": state_digest(S),
+        "field_sums": [float(x) for x in S.sum(axis=1)], "dt_first": dts[0], "dt_last": dts[-1]}}
+    path = os.path.join(HERE, "fullsize.json")
+    with open(path, "w") as fh:
+        json.dump(out, fh, indent=1)
+    print(f"fullsize: {os.path.relpath(path, REPO)}")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "fullsize":
+        fullsize()
+    else:
+        main()
