@@ -140,6 +140,7 @@ struct StageArgs {
   double *lambda;           // last stage: CFL radius of the new state
   int irk;
   int last;
+  int ahead;  // the brick this many blocks ahead (one wave of resident blocks) gets its stage input prefetched
   unsigned long long *err;
 };
 
@@ -524,6 +525,9 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
     if (!isfinite(R[v])) finite = false;
   if (!ok) raise_error(a.err, kErrRegion, c);
   if (!finite) raise_error(a.err, kErrNonFinite, c);
+  // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
+  const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
+  const bool first = a.irk == 1;
   float dn[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
@@ -531,12 +535,7 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
     // the stage-input increment, read again here rather than kept in
     // registers through the flux phase
     const float din = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-    switch (a.irk) {
-      case 1: dn[v] = incr; break;
-      case 2: dn[v] = 0.25f * (din + incr); break;
-      case 3: dn[v] = (2.0f / 3.0f) * (din + incr); break;
-      default: dn[v] = 0.5f * (din + incr); break;
-    }
+    dn[v] = first ? incr : w * (din + incr);
   }
   if (a.last) {
     double snew[kNeqMax];
@@ -1092,16 +1091,27 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + int64_t(v) * n + start + 32 * l));
   }
   static_assert(kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes");
+  // the stage input of the brick one wave of resident blocks ahead, on its
+  // way to L2 by the time that block starts
+  if (a.ahead > 0 && int(blockIdx.x) + a.ahead < int(gridDim.x) && t >= NB - NV * kL32) {
+    const int r = t - (NB - NV * kL32), v = r / kL32, l = r % kL32;
+    const int next = __ldg(&a.blocks[blockIdx.x + a.ahead].start);
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Sin + int64_t(v) * n + next + 32 * l));
+  }
+  static_assert(NV * kL32 + kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes do not overlap");
   // 1: the brick's cells and the halo from the six neighbour bricks, copied
   // global -> shared asynchronously (cp.async, no register round trip)
   const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[3 * t]);
+  // lane f < 6 of every warp holds brick side f (read below by shuffle)
+  const int lane_side = __ldg(&bdp->side[(t & 31) < 6 ? (t & 31) : 0]);
   const int ti = int(cw0 & 2047u);
 #pragma unroll
   for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
 #pragma unroll
   for (int h = t; h < kHalo; h += NB) {
     const uint32_t e = __ldg(&g_brick_halo<S>.h[h]);
-    const int base = __ldg(&bdp->side[(e >> 11) & 7u]);
+    static_assert(kHalo % NB == 0, "every lane takes part in the side shuffle");
+    const int base = __shfl_sync(0xffffffffu, lane_side, int((e >> 11) & 7u));
     if (base >= 0) {
       const int hti = int(e & 2047u), x = base + int(e >> 14);
 #pragma unroll
@@ -1492,6 +1502,9 @@ bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
 // otherwise.
 cudaError_t allow_smem_brick(bool muscl, bool ns);  // with the launches below
 
+// resident brick blocks across the GPU (the prefetch distance of the stage input)
+int brick_wave(bool muscl, bool ns);
+
 int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen) {
   r.ready = false;
   r.snf_valid = false;
@@ -1643,6 +1656,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
     snprintf(why, whylen, "shared-memory opt-in of the brick kernel: %s", cudaGetErrorString(e));
     return FVGPU_ERR_CUDA;
   }
+  r.wave = brick_wave(ph.ischeme == 2, ph.ns == 1);
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = alloc_slot(r, kBufTables, sizeof(GeoTables))) != cudaSuccess ||
@@ -1754,6 +1768,19 @@ cudaError_t allow_smem_brick(bool muscl, bool ns) {
   return muscl ? allow_smem_muscl<true>(ns) : allow_smem_muscl<false>(ns);
 }
 
+int brick_wave(bool muscl, bool ns) {
+  constexpr size_t smem = Brick8::template smem_bytes<kNeqMax>();
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  const void *k = muscl ? (ns ? reinterpret_cast<const void *>(k_mixed_brick<1, true, true, Brick8>)
+                              : reinterpret_cast<const void *>(k_mixed_brick<1, true, false, Brick8>))
+                        : (ns ? reinterpret_cast<const void *>(k_mixed_brick<1, false, true, Brick8>)
+                              : reinterpret_cast<const void *>(k_mixed_brick<1, false, false, Brick8>));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Brick8::N, smem) != cudaSuccess) return 0;
+  return sms * per_sm;
+}
+
 // One RK step from FP64 state `in` (and its FP32 copy) to `out`.
 cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView &m, int scheme, bool cfl_mode,
                                const double *in, double *out, double *dt, double *lambda, const double *cfl,
@@ -1784,6 +1811,7 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
     a.dt = dt;
     a.irk = kStages[scheme][k];
     a.last = k == nst - 1;
+    a.ahead = r.wave;
     a.lambda = (a.last && cfl_mode) ? lambda : nullptr;
     a.err = err;
     if (ph.ns == 1) {

@@ -34,6 +34,7 @@ struct MixedResources {
   // (fv_mixed.cu; meshes of model 1 that are 8x8x4 bricks throughout), 1 the
   // table-driven family (fv_mixed_amr.cu; every other mesh)
   int family = 0;
+  int wave = 0;  // resident brick blocks across the GPU (family 0)
 };
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen);
