@@ -523,8 +523,14 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v)
     if (!isfinite(R[v])) finite = false;
-  if (!ok) raise_error(a.err, kErrRegion, c);
-  if (!finite) raise_error(a.err, kErrNonFinite, c);
+  if (!(ok && finite)) raise_error(a.err, ok ? kErrNonFinite : kErrRegion, c);
+  // the stage-input increment, read again here rather than kept in
+  // registers through the flux phase
+  float din[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (a.Din) {
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) din[v] = __ldg(a.Din + v * n + c);
+  }
   // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
   const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
   const bool first = a.irk == 1;
@@ -532,10 +538,7 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     const float incr = dtv * R[v];
-    // the stage-input increment, read again here rather than kept in
-    // registers through the flux phase
-    const float din = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-    dn[v] = first ? incr : w * (din + incr);
+    dn[v] = first ? incr : w * (din[v] + incr);
   }
   if (a.last) {
     double snew[kNeqMax];
@@ -725,6 +728,26 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
 #pragma unroll
   for (int i = 0; i < 9; ++i) SGout[i * n + c] = gr[i];
 }
+
+// Slots of five FP32 words in shared memory: words 0-3 as one float4 and
+// word 4 in a float array beside it, so that a slot moves with two
+// shared-memory instructions.
+struct Slots5 {
+  float4 *p4;
+  float *p1;
+  __device__ __forceinline__ void ld(int i, float q[kNvMax]) const {
+    const float4 u = p4[i];
+    q[0] = u.x;
+    q[1] = u.y;
+    q[2] = u.z;
+    q[3] = u.w;
+    q[4] = p1[i];
+  }
+  __device__ __forceinline__ void st(int i, const float q[kNvMax]) const {
+    p4[i] = make_float4(q[0], q[1], q[2], q[3]);
+    p1[i] = q[4];
+  }
+};
 
 // dynamic shared memory of the kernels (16-byte aligned)
 extern __shared__ __align__(16) float g_mixed_smem[];
@@ -1045,10 +1068,12 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   constexpr int kTile = S::kTile, kFaces = S::kFaces, kHalo = S::kHalo, kHalo1 = S::kHalo1;
   constexpr int kSides = S::kSides, kFvSlots = S::kFvSlots;
   // the tile holds the stage state of the brick and its halo until every
-  // face value is formed, then the face fluxes [5][kFaces]
+  // face value is formed, then the face fluxes (five-word slots)
   float(*tile)[kTile] = reinterpret_cast<float(*)[kTile]>(g_mixed_smem);
-  float(*fvb)[kFvSlots] = reinterpret_cast<float(*)[kFvSlots]>(g_mixed_smem + NV * kTile);  // face values handed on
-  float(*flux)[kFaces] = reinterpret_cast<float(*)[kFaces]>(g_mixed_smem);
+  static_assert(NV == 5 && (NV * kTile) % 4 == 0, "five-word slots, 16-byte aligned");
+  const Slots5 fvb{reinterpret_cast<float4 *>(g_mixed_smem + NV * kTile),
+                   g_mixed_smem + NV * kTile + 4 * kFvSlots};  // face values handed on
+  const Slots5 flux{reinterpret_cast<float4 *>(g_mixed_smem), g_mixed_smem + 4 * kFaces};
   __shared__ float s_geo[6][2][4];  // per face index, relation same / boundary: dcf, 1/dcc, area, k
   __shared__ float s_area[3];       // face area per axis
   __shared__ float s_dtv, s_inv2vol;  // dt / V and 1 / (2 V) of the brick's level
@@ -1180,8 +1205,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
       } else {
         axis_faces<MODEL>(q, nbp, nbm, s_geo[FP][0][3], fpv[AX], fm);
       }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) fvb[v][AX * NB + t] = fm[v];
+      fvb.st(AX * NB + t, fm);
     };
     own_axis(std::integral_constant<int, 0>{});
     own_axis(std::integral_constant<int, 1>{});
@@ -1211,8 +1235,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
           else
             axis_faces<MODEL, 1>(qh, nbp, nbm, k, out, out);
         }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) fvb[v][3 * NB + h] = out[v];
+        fvb.st(3 * NB + h, out);
       }
     }
     __syncthreads();  // the tile is read for the last time above; it now takes the fluxes
@@ -1228,8 +1251,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
       } else {
         float hi[kNvMax];
         const int hs = int((cw2 >> (10 * AX)) & 1023u);
-#pragma unroll
-        for (int v = 0; v < kNvMax; ++v) hi[v] = v < NV ? fvb[v][hs] : 0.0f;
+        fvb.ld(hs, hi);
         int clo = c, chi = c;
         if (NS) {
           const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[slot]);
@@ -1238,8 +1260,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
         }
         ok &= face_flux<MODEL, FP>(mc, a, FP, 0, MUSCL, fpv[AX], hi, clo, chi, Fn);
       }
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) flux[v][slot] = Fn[v];
+      flux.st(slot, Fn);
     };
     own_flux(std::integral_constant<int, 0>{});
     own_flux(std::integral_constant<int, 1>{});
@@ -1251,8 +1272,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
       const int fm = minus_face(ax);
       float Fn[kNeqMax], lo[kNvMax], hi[kNvMax];
       const int los = int(e & 1023u), his = int((e >> 10) & 1023u);
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) hi[v] = v < NV ? fvb[v][his] : 0.0f;
+      fvb.ld(his, hi);
       if (EDGE && ((bmask >> fm) & 1u)) {
         // the brick cell's own domain-boundary face, own frame, stored as the
         // + face flux of the lower cell that is not there
@@ -1261,8 +1281,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) Fn[v] = -Fn[v];
       } else {
-#pragma unroll
-        for (int v = 0; v < kNvMax; ++v) lo[v] = v < NV ? fvb[v][los] : 0.0f;
+        fvb.ld(los, lo);
         int clo = c, chi = c;
         if (NS) {
           const uint32_t cr = __ldg(&g_brick_task_cells<S>.c[3 * NB + j]);
@@ -1276,8 +1295,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
         else
           ok &= face_flux<MODEL, 5>(mc, a, 5, 0, MUSCL, lo, hi, clo, chi, Fn);
       }
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) flux[v][3 * NB + j] = Fn[v];
+      flux.st(3 * NB + j, Fn);
     }
   };
   if (bmask)
@@ -1293,8 +1311,11 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   for (int ax = 0; ax < 3; ++ax) {
     const int sm = int((cw1 >> (10 * ax)) & 1023u), sp = ax * NB + t;
     const float A = s_area[ax];
+    float fm[kNvMax], fp[kNvMax];
+    flux.ld(sm, fm);
+    flux.ld(sp, fp);
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, flux[v][sm] - flux[v][sp], R[v]);
+    for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, fm[v] - fp[v], R[v]);
   }
   float qn[kNvMax], lam = 0.0f;
   if (stage_update<MODEL>(a, c, s_dtv, R, ok, qn) && a.lambda)
