@@ -965,11 +965,11 @@ int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld) {
   if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
   cudaSetDevice(ctx->cfg.device);
   if (ld == ctx->n)  // dense: one linear copy
-    FV_CUDA(ctx, cudaMemcpyAsync(ctx->S.p, U, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyHostToDevice,
+    FV_CUDA(ctx, cudaMemcpyAsync(ctx->S.p, U, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyDefault,
                                  ctx->stream));
   else
     FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->S.p, sizeof(double) * ctx->n, U, sizeof(double) * ld,
-                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyHostToDevice, ctx->stream));
+                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDefault, ctx->stream));
   ctx->lambda_valid = false;
   ctx->mixed.snf_valid = false;
   return FVGPU_OK;
@@ -981,11 +981,11 @@ int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld) {
   if (!U || ld < ctx->n) return set_err(ctx, FVGPU_ERR_ARG, "bad state pointer or leading dimension");
   cudaSetDevice(ctx->cfg.device);
   if (ld == ctx->n)
-    FV_CUDA(ctx, cudaMemcpyAsync(U, ctx->S.p, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyDeviceToHost,
+    FV_CUDA(ctx, cudaMemcpyAsync(U, ctx->S.p, sizeof(double) * ctx->neq * ctx->n, cudaMemcpyDefault,
                                  ctx->stream));
   else
     FV_CUDA(ctx, cudaMemcpy2DAsync(U, sizeof(double) * ld, ctx->S.p, sizeof(double) * ctx->n,
-                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDeviceToHost, ctx->stream));
+                                   sizeof(double) * ctx->n, ctx->neq, cudaMemcpyDefault, ctx->stream));
   return sync_and_check(ctx);
 }
 
@@ -1010,7 +1010,7 @@ int fvgpu_download(fvgpu_ctx *ctx, int field, double *out) {
       b = &ctx->SG; break;
     default: return set_err(ctx, FVGPU_ERR_ARG, "unknown field %d", field);
   }
-  FV_CUDA(ctx, cudaMemcpyAsync(out, b->p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  FV_CUDA(ctx, cudaMemcpyAsync(out, b->p, bytes, cudaMemcpyDefault, ctx->stream));
   return sync_and_check(ctx);
 }
 
@@ -1399,12 +1399,12 @@ int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld
   rc = ensure_adjoint(ctx);
   if (rc) return rc;
   const size_t row = sizeof(double) * size_t(ctx->n);
-  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjW.p, row, w, sizeof(double) * ld, row, ctx->neq, cudaMemcpyHostToDevice,
+  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjW.p, row, w, sizeof(double) * ld, row, ctx->neq, cudaMemcpyDefault,
                                  ctx->stream));
   rc = enqueue_vjp(ctx, ctx->S.as<double>(), ctx->adjW.as<double>(), ctx->adjG.as<double>());
   if (rc) return rc;
   FV_CUDA(ctx, cudaMemcpy2DAsync(dJdU, sizeof(double) * ld, ctx->adjG.p, row, row, ctx->neq,
-                                 cudaMemcpyDeviceToHost, ctx->stream));
+                                 cudaMemcpyDefault, ctx->stream));
   return sync_and_check(ctx);
 }
 
@@ -1448,13 +1448,13 @@ int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const
   ctx->mixed.snf_valid = false;
   ctx->lambda_valid = false;
   // reverse sweep
-  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjG.p, row, gN, sizeof(double) * ld, row, ctx->neq, cudaMemcpyHostToDevice,
+  FV_CUDA(ctx, cudaMemcpy2DAsync(ctx->adjG.p, row, gN, sizeof(double) * ld, row, ctx->neq, cudaMemcpyDefault,
                                  ctx->stream));
   for (int k = nsteps - 1; k >= 0; --k) {
     rc = enqueue_step_adjoint(ctx, scheme, reinterpret_cast<const double *>(ck + cell * size_t(k)));
     if (rc) return rc;
   }
-  FV_CUDA(ctx, cudaMemcpy2DAsync(g0, sizeof(double) * ld, ctx->adjG.p, row, row, ctx->neq, cudaMemcpyDeviceToHost,
+  FV_CUDA(ctx, cudaMemcpy2DAsync(g0, sizeof(double) * ld, ctx->adjG.p, row, row, ctx->neq, cudaMemcpyDefault,
                                  ctx->stream));
   return sync_and_check(ctx);
 }

@@ -148,10 +148,13 @@ typedef struct fvgpu_leaves {
   int side_bc[6];        /* boundary code per face side (ignored on periodic axes) */
 } fvgpu_leaves;
 int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *leaves);
-/* S <- U (host, [neq][ld]); LEAF.S of every leaf (strdata.h:80). */
+/* S <- U ([neq][ld]); LEAF.S of every leaf (strdata.h:80).  U may be host
+ * or device memory (the copy direction follows from unified addressing); the
+ * copy is queued on the context's stream. */
 int fvgpu_upload_state(fvgpu_ctx *ctx, const double *U, int64_t ld);
 int fvgpu_download_state(fvgpu_ctx *ctx, double *U, int64_t ld);
-/* Copy a device field (FVGPU_FIELD_*) to host memory (densely packed). */
+/* Copy a device field (FVGPU_FIELD_*) to host or device memory (densely
+ * packed). */
 int fvgpu_download(fvgpu_ctx *ctx, int field, double *out);
 
 /* ---- the reference's calls -------------------------------------------- */
@@ -263,8 +266,8 @@ int fvgpu_halo_unpack(fvgpu_ctx *ctx, const double *recv_buf);
  * branch switch they are one-sided. */
 
 /* dJdU = (dR/dU)^T w for the residual R(U) of the current state; w and dJdU
- * host arrays [neq][ld].  The context's SF field then holds the face values
- * of the current state. */
+ * arrays [neq][ld] in host or device memory.  The context's SF field then
+ * holds the face values of the current state. */
 int fvgpu_residual_vjp(fvgpu_ctx *ctx, const double *w, double *dJdU, int64_t ld);
 
 /* The same on device arrays [neq][ncells] the caller owns, queued on the
@@ -278,8 +281,8 @@ int fvgpu_residual_vjp_device(fvgpu_ctx *ctx, const double *w, double *dJdU);
  * demand and kept for reuse), then sweeps back: each step's stage states are
  * recomputed from its checkpoint and the stages are reversed.  On return the
  * current state is S_N, exactly as fvgpu_step(ctx, scheme, dt, 0, nsteps)
- * leaves it, and g0 = (dS_N/dS_0)^T gN.  gN and g0 are host arrays
- * [neq][ld]; they may be the same array. */
+ * leaves it, and g0 = (dS_N/dS_0)^T gN.  gN and g0 are arrays [neq][ld] in
+ * host or device memory; they may be the same array. */
 int fvgpu_adjoint_steps(fvgpu_ctx *ctx, int scheme, double dt, int nsteps, const double *gN, double *g0,
                         int64_t ld);
 

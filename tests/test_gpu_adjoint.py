@@ -346,6 +346,27 @@ def test_autograd_wrappers():
         assert bits_equal(U.grad.numpy(), s.adjoint_steps(Wt.numpy(), dt, "ssprk3", 2))
 
 
+def test_autograd_wrappers_on_cuda_tensors():
+    """CUDA tensors go through the C ABI as device pointers: the same bits as
+    the host path, forward and backward, with the results on the device."""
+    torch = pytest.importorskip("torch")
+    from fv_140823_gb300.autograd import residual, steps
+    t, cfg, z = load_golden("amr_periodic_muscl")
+    U0, dt = z["U"], float(z["dt"])
+    rng = np.random.default_rng(5)
+    W = rng.standard_normal(U0.shape)
+    with solver(t, cfg) as s:
+        for fn in (lambda U: residual(s, U), lambda U: steps(s, U, dt, "ssprk3", 2)):
+            got = []
+            for dev in ("cpu", "cuda"):
+                U = torch.tensor(U0, device=dev, requires_grad=True)
+                out = fn(U)
+                assert out.device.type == dev
+                (out * torch.from_numpy(W).to(dev)).sum().backward()
+                got.append((out.detach().cpu().numpy(), U.grad.cpu().numpy()))
+            assert bits_equal(got[0][0], got[1][0]) and bits_equal(got[0][1], got[1][1])
+
+
 @pytest.mark.parametrize("name", ["bubble_l3"])
 def test_adjoint_rejects_unsupported(name):
     from fv_140823_gb300.solver import FvGpuError
