@@ -366,13 +366,13 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   float S_S = num * fast_rcp(den);
   const bool ok = !isnan(S_S);
   if (bc == 3) S_S = 0.0f;
-  // region selection in the order of hllc_euler.c:18-50
-  const bool r1 = 0.0f <= SL;
-  const bool r2 = !r1 && (SL <= 0.0f) && (0.0f <= S_S);
-  const bool r3 = !r1 && !r2 && (S_S <= 0.0f) && (0.0f <= SR);
-  const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
-  const bool left = r1 || r2;
-  const bool star = r2 || r3;
+  // region selection of hllc_euler.c:18-50 (0 <= SL: left; SL <= 0 <= S*:
+  // left star; S* <= 0 <= SR: right star; SR <= 0: right), reduced to two
+  // predicates; with S* not NaN (NaN wave speeds make S* NaN) exactly one
+  // region holds
+  const bool gl = 0.0f <= SL, gs = 0.0f <= S_S, gr = 0.0f <= SR;
+  const bool left = gl || gs;
+  const bool star = !gl && (gs || gr);
   const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn, Kun = left ? L.un : R.un;
   const float Kp = left ? L.p : R.p, Ke = left ? L.e : R.e, Ky = left ? L.y : R.y;
   const float Krinv = left ? L.rinv : R.rinv, Kmm = left ? L.mm : R.mm, Kml = left ? L.ml : R.ml;
@@ -403,7 +403,7 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   Fn[0] = F0;
   frame_out<F>(f, Fa, Fb, Fc, Fn);
   Fn[4] = F4;
-  return ok && (r1 || r2 || r3 || r4);
+  return ok;
 }
 
 // Canonical flux of a face from the lower / upper face values (bc > 0: a
@@ -426,8 +426,14 @@ __device__ __forceinline__ bool canonical_flux(const MixedConst &mc, int f, int 
 // ============================ reconstruction ================================
 
 // minmod of a and b: the one of smaller magnitude when both have the same
-// sign, else zero -- the median of a, b and 0 (four min/max operations)
-__device__ __forceinline__ float minmod(float a, float b) { return fmaxf(fminf(a, b), fminf(fmaxf(a, b), 0.0f)); }
+// sign, else zero.  min.xorsign.abs gives min(|a|, |b|) with the sign bit
+// set when the signs differ; clamped at zero and given a's sign, that is the
+// median of a, b and 0 up to the sign of a zero result.
+__device__ __forceinline__ float minmod(float a, float b) {
+  float m;
+  asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(m) : "f"(a), "f"(b));
+  return copysignf(fmaxf(m, 0.0f), a);
+}
 
 // Face values of a cell on an axis whose two neighbours have the cell's
 // level: s = minmod(q+ - q, q - q-), face+ = q + k s, face- = q - k s.
@@ -1083,11 +1089,11 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   const int n = a.n;
   const int start = __ldg(&bdp->start), level = __ldg(&bdp->level);
   const int c = start + t;
-  uint32_t bmask = 0;  // sides of the brick on the domain boundary
-#pragma unroll
-  for (int f = 0; f < 6; ++f)
-    if (__ldg(&bdp->side[f]) < 0) bmask |= 1u << f;
-  if (t < 6) s_side[t] = __ldg(&bdp->side[t]);
+  // lane f < 6 of every warp holds brick side f (the halo loop reads it by
+  // shuffle); the sides on the domain boundary as a bit mask
+  const int lane_side = __ldg(&bdp->side[(t & 31) < 6 ? (t & 31) : 0]);
+  const uint32_t bmask = __ballot_sync(0xffffffffu, (t & 31) < 6 && lane_side < 0);
+  if (t < 6) s_side[t] = lane_side;
   if (t < 12) {
     const int f = t >> 1, r = t & 1;
     const float *gf = geo_face(a.geo, level, f, r ? kRelBoundary : kRelSame);
@@ -1127,8 +1133,6 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   // 1: the brick's cells and the halo from the six neighbour bricks, copied
   // global -> shared asynchronously (cp.async, no register round trip)
   const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[3 * t]);
-  // lane f < 6 of every warp holds brick side f (read below by shuffle)
-  const int lane_side = __ldg(&bdp->side[(t & 31) < 6 ? (t & 31) : 0]);
   const int ti = int(cw0 & 2047u);
 #pragma unroll
   for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
