@@ -144,6 +144,15 @@ struct StageArgs {
   unsigned long long *err;
 };
 
+// FP32 state arrays of this family (SNf, stage inputs, stage increments) are
+// brick-major: the 8x8x4 brick of cells [256 b, 256 b + 256) keeps its five
+// words per cell as five runs of 256 floats, word v of cell c at
+// fidx(c) + 256 v.  A brick's stage data is then one contiguous 5 KiB run,
+// and every access to a cell's words uses one base index with constant
+// offsets.  (The FP64 state stays [neq][n], the layout of the C ABI.)
+constexpr int kBrickCells = 256;
+__host__ __device__ __forceinline__ int fidx(int c) { return c + 4 * (c & ~(kBrickCells - 1)); }
+
 __device__ __forceinline__ int level_of(int32_t g) { return g & 31; }
 __device__ __forceinline__ int rel_of(int32_t g, int f) { return (g >> (5 + 2 * f)) & 3; }
 __device__ __forceinline__ const float *geo_face(const GeoTables *G, int level, int f, int rel) {
@@ -532,10 +541,11 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
   if (!(ok && finite)) raise_error(a.err, ok ? kErrNonFinite : kErrRegion, c);
   // the stage-input increment, read again here rather than kept in
   // registers through the flux phase
+  const int fc = fidx(c);
   float din[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   if (a.Din) {
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) din[v] = __ldg(a.Din + v * n + c);
+    for (int v = 0; v < kNeqMax; ++v) din[v] = __ldg(a.Din + fc + kBrickCells * v);
   }
   // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
   const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
@@ -555,15 +565,15 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
     }
     to_state_f32<MODEL>(snew, qn);
 #pragma unroll
-    for (int v = 0; v < kNv<MODEL>; ++v) a.SNfout[v * n + c] = qn[v];
+    for (int v = 0; v < kNv<MODEL>; ++v) a.SNfout[fc + kBrickCells * v] = qn[v];
     return true;
   }
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
-    a.Dout[v * n + c] = dn[v];
-    const float sn = __ldg(a.SNf + v * n + c);
+    a.Dout[fc + kBrickCells * v] = dn[v];
+    const float sn = __ldg(a.SNf + fc + kBrickCells * v);
     const float x = sn + dn[v];  // the value the next stage would form
-    a.Sout[v * n + c] = x;
+    a.Sout[fc + kBrickCells * v] = x;
   }
   return false;
 }
@@ -573,7 +583,7 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
 template <int MODEL>
 __device__ __forceinline__ void global_state(const StageArgs &a, int x, float q[kNvMax]) {
 #pragma unroll
-  for (int v = 0; v < kNvMax; ++v) q[v] = v < kNv<MODEL> ? __ldg(a.Sin + v * a.n + x) : 0.0f;
+  for (int v = 0; v < kNvMax; ++v) q[v] = v < kNv<MODEL> ? __ldg(a.Sin + fidx(x) + kBrickCells * v) : 0.0f;
 }
 
 // ============================ viscous terms =================================
@@ -723,11 +733,13 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
       const float A = a.geo->sub_area[lev * 6 + f];
       for (int s = 0; s < 4; ++s) {
         const int ks = __ldg(k + s);
-        const float m[3] = {__ldg(a.Sin + 1 * n + ks), __ldg(a.Sin + 2 * n + ks), __ldg(a.Sin + 3 * n + ks)};
+        const float *p = a.Sin + fidx(ks);
+        const float m[3] = {__ldg(p + kBrickCells), __ldg(p + 2 * kBrickCells), __ldg(p + 3 * kBrickCells)};
         add(m, A);
       }
     } else {
-      const float m[3] = {__ldg(a.Sin + 1 * n + code), __ldg(a.Sin + 2 * n + code), __ldg(a.Sin + 3 * n + code)};
+      const float *p = a.Sin + fidx(code);
+      const float m[3] = {__ldg(p + kBrickCells), __ldg(p + 2 * kBrickCells), __ldg(p + 3 * kBrickCells)};
       add(m, geo_face(a.geo, lev, f, rel_of(g, f))[2]);
     }
   }
@@ -1115,11 +1127,11 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   }
   if (a.Din && t >= kNeqMax * kL64 && t < kNeqMax * (kL64 + kL32)) {  // the stage-input increment
     const int r = t - kNeqMax * kL64, v = r / kL32, l = r % kL32;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + int64_t(v) * n + start + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + fidx(start) + kBrickCells * v + 32 * l));
   }
   if (a.Din && !a.last && t >= kNeqMax * (kL64 + kL32) && t < kNeqMax * (kL64 + 2 * kL32)) {  // FP32 SN
     const int r = t - kNeqMax * (kL64 + kL32), v = r / kL32, l = r % kL32;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + int64_t(v) * n + start + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + fidx(start) + kBrickCells * v + 32 * l));
   }
   static_assert(kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes");
   // the stage input of the brick one wave of resident blocks ahead, on its
@@ -1127,7 +1139,7 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   if (a.ahead > 0 && int(blockIdx.x) + a.ahead < int(gridDim.x) && t >= NB - NV * kL32) {
     const int r = t - (NB - NV * kL32), v = r / kL32, l = r % kL32;
     const int next = __ldg(&a.blocks[blockIdx.x + a.ahead].start);
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Sin + int64_t(v) * n + next + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Sin + fidx(next) + kBrickCells * v + 32 * l));
   }
   static_assert(NV * kL32 + kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes do not overlap");
   // 1: the brick's cells and the halo from the six neighbour bricks, copied
@@ -1135,16 +1147,17 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[3 * t]);
   const int ti = int(cw0 & 2047u);
 #pragma unroll
-  for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + v * n + c);
+  for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + fidx(c) + kBrickCells * v);
 #pragma unroll
   for (int h = t; h < kHalo; h += NB) {
     const uint32_t e = __ldg(&g_brick_halo<S>.h[h]);
     static_assert(kHalo % NB == 0, "every lane takes part in the side shuffle");
+    static_assert(S::N == kBrickCells, "brick-major FP32 arrays hold 256-cell bricks");
     const int base = __shfl_sync(0xffffffffu, lane_side, int((e >> 11) & 7u));
     if (base >= 0) {
       const int hti = int(e & 2047u), x = base + int(e >> 14);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) cp_async4(&tile[v][hti], a.Sin + v * n + x);
+      for (int v = 0; v < NV; ++v) cp_async4(&tile[v][hti], a.Sin + fidx(x) + kBrickCells * v);
     }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
@@ -1339,7 +1352,7 @@ __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__
     to_state_f32<MODEL>(x, q);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v)
-      if (v < neq) Sf[v * n + c] = q[v];
+      if (v < neq) Sf[fidx(int(c)) + kBrickCells * v] = q[v];
   }
 }
 
@@ -1358,7 +1371,7 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
     to_state_f32<MODEL>(x, q);
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v)
-      if (v < mc.neq) Sf[int64_t(v) * n + c] = q[v];
+      if (v < mc.neq) Sf[fidx(c) + kBrickCells * v] = q[v];
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
   block_max_lambda_f(lam, lambda);
@@ -1546,6 +1559,11 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   if (ph.model != 1 || r.force_general || !all_cells_in_bricks(m, is_block8)) {
     r.family = 1;
     return amr::mixed_prepare_host(r, ph, m, why, whylen);
+  }
+  if (m->ncells > (int64_t(INT_MAX) - kBrickCells) / 5) {
+    snprintf(why, whylen, "the mixed path indexes its FP32 arrays with 32-bit integers: at most %lld cells",
+             (long long)((int64_t(INT_MAX) - kBrickCells) / 5));
+    return FVGPU_ERR_UNSUPPORTED;
   }
   r.family = 0;
   // fluxes are evaluated in the face frames of the reference's hexahedral
