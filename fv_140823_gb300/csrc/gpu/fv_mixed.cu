@@ -145,13 +145,29 @@ struct StageArgs {
 };
 
 // FP32 state arrays of this family (SNf, stage inputs, stage increments) are
-// brick-major: the 8x8x4 brick of cells [256 b, 256 b + 256) keeps its five
-// words per cell as five runs of 256 floats, word v of cell c at
-// fidx(c) + 256 v.  A brick's stage data is then one contiguous 5 KiB run,
-// and every access to a cell's words uses one base index with constant
-// offsets.  (The FP64 state stays [neq][n], the layout of the C ABI.)
+// brick-major and cell-major within a brick: the 8x8x4 brick of cells
+// [256 b, 256 b + 256) keeps one 5 KiB run, words 0-3 of its cells as 256
+// float4 (word 0 of cell c at f4idx(c)), then word 4 of its cells (at
+// f1idx(c)).  A cell's five words move with one 16-byte and one 4-byte
+// access; a brick's stage data is one contiguous run.  (The FP64 state stays
+// [neq][n], the layout of the C ABI.)
 constexpr int kBrickCells = 256;
-__host__ __device__ __forceinline__ int fidx(int c) { return c + 4 * (c & ~(kBrickCells - 1)); }
+__host__ __device__ __forceinline__ int f4idx(int c) { return 4 * c + (c & ~(kBrickCells - 1)); }
+__host__ __device__ __forceinline__ int f1idx(int c) { return c + 4 * (c & ~(kBrickCells - 1)) + 4 * kBrickCells; }
+// the first float of the run of the brick that starts at cell b
+__host__ __device__ __forceinline__ int brick_run(int b) { return 5 * b; }
+__device__ __forceinline__ void ld5g(const float *p, int c, float q[5]) {
+  const float4 u = __ldg(reinterpret_cast<const float4 *>(p + f4idx(c)));
+  q[0] = u.x;
+  q[1] = u.y;
+  q[2] = u.z;
+  q[3] = u.w;
+  q[4] = __ldg(p + f1idx(c));
+}
+__device__ __forceinline__ void st5g(float *p, int c, const float q[5]) {
+  *reinterpret_cast<float4 *>(p + f4idx(c)) = make_float4(q[0], q[1], q[2], q[3]);
+  p[f1idx(c)] = q[4];
+}
 
 __device__ __forceinline__ int level_of(int32_t g) { return g & 31; }
 __device__ __forceinline__ int rel_of(int32_t g, int f) { return (g >> (5 + 2 * f)) & 3; }
@@ -541,12 +557,8 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
   if (!(ok && finite)) raise_error(a.err, ok ? kErrNonFinite : kErrRegion, c);
   // the stage-input increment, read again here rather than kept in
   // registers through the flux phase
-  const int fc = fidx(c);
   float din[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  if (a.Din) {
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) din[v] = __ldg(a.Din + fc + kBrickCells * v);
-  }
+  if (a.Din) ld5g(a.Din, c, din);
   // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
   const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
   const bool first = a.irk == 1;
@@ -564,16 +576,16 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
       a.SNout[v * n + c] = snew[v];
     }
     to_state_f32<MODEL>(snew, qn);
-#pragma unroll
-    for (int v = 0; v < kNv<MODEL>; ++v) a.SNfout[fc + kBrickCells * v] = qn[v];
+    st5g(a.SNfout, c, qn);
     return true;
   }
+  {
+    float sn[kNvMax], x[kNvMax];
+    ld5g(a.SNf, c, sn);
 #pragma unroll
-  for (int v = 0; v < kNeqMax; ++v) {
-    a.Dout[fc + kBrickCells * v] = dn[v];
-    const float sn = __ldg(a.SNf + fc + kBrickCells * v);
-    const float x = sn + dn[v];  // the value the next stage would form
-    a.Sout[fc + kBrickCells * v] = x;
+    for (int v = 0; v < kNeqMax; ++v) x[v] = sn[v] + dn[v];  // the value the next stage would form
+    st5g(a.Dout, c, dn);
+    st5g(a.Sout, c, x);
   }
   return false;
 }
@@ -582,8 +594,7 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
 // previous stage)
 template <int MODEL>
 __device__ __forceinline__ void global_state(const StageArgs &a, int x, float q[kNvMax]) {
-#pragma unroll
-  for (int v = 0; v < kNvMax; ++v) q[v] = v < kNv<MODEL> ? __ldg(a.Sin + fidx(x) + kBrickCells * v) : 0.0f;
+  ld5g(a.Sin, x, q);
 }
 
 // ============================ viscous terms =================================
@@ -733,13 +744,13 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
       const float A = a.geo->sub_area[lev * 6 + f];
       for (int s = 0; s < 4; ++s) {
         const int ks = __ldg(k + s);
-        const float *p = a.Sin + fidx(ks);
-        const float m[3] = {__ldg(p + kBrickCells), __ldg(p + 2 * kBrickCells), __ldg(p + 3 * kBrickCells)};
+        const float4 u = __ldg(reinterpret_cast<const float4 *>(a.Sin + f4idx(ks)));
+        const float m[3] = {u.y, u.z, u.w};
         add(m, A);
       }
     } else {
-      const float *p = a.Sin + fidx(code);
-      const float m[3] = {__ldg(p + kBrickCells), __ldg(p + 2 * kBrickCells), __ldg(p + 3 * kBrickCells)};
+      const float4 u = __ldg(reinterpret_cast<const float4 *>(a.Sin + f4idx(code)));
+      const float m[3] = {u.y, u.z, u.w};
       add(m, geo_face(a.geo, lev, f, rel_of(g, f))[2]);
     }
   }
@@ -769,6 +780,12 @@ struct Slots5 {
 
 // dynamic shared memory of the kernels (16-byte aligned)
 extern __shared__ __align__(16) float g_mixed_smem[];
+
+// 16-byte asynchronous global -> shared copy (cp.async.cg: L2 only)
+__device__ __forceinline__ void cp_async16(float4 *dst, const float *src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
 
 // 4-byte asynchronous global -> shared copy (cp.async.ca)
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
@@ -858,7 +875,7 @@ struct BrickShape {
                     N <= 256 && BY % 2 == 0 && kNeqMax * kFaces <= 5 * kTile,
                 "brick table fields");
 };
-using Brick8 = BrickShape<8, 8, 4, 0>;
+using Brick8 = BrickShape<8, 8, 4, 2>;
 
 // lower cell (brick coordinates) and axis of flux slot `slot`
 template <class S>
@@ -948,7 +965,7 @@ constexpr BrickHalo<S> make_brick_halo() {
           }
           const int ti = S::tile_index(hx, hy, hz);
           cell[k] = uint32_t(ti) | (uint32_t(side) << 11) | (uint32_t(morton_local(lx, ly, lz)) << 14);
-          bank_of[k] = ti % 32;
+          bank_of[k] = ti % 8;  // 16-byte slots: eight per 128-byte wavefront
           ++k;
         }
     }
@@ -1087,7 +1104,8 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   constexpr int kSides = S::kSides, kFvSlots = S::kFvSlots;
   // the tile holds the stage state of the brick and its halo until every
   // face value is formed, then the face fluxes (five-word slots)
-  float(*tile)[kTile] = reinterpret_cast<float(*)[kTile]>(g_mixed_smem);
+  static_assert(kTile % 4 == 0, "float4 tile");
+  const Slots5 tile{reinterpret_cast<float4 *>(g_mixed_smem), g_mixed_smem + 4 * kTile};
   static_assert(NV == 5 && (NV * kTile) % 4 == 0, "five-word slots, 16-byte aligned");
   const Slots5 fvb{reinterpret_cast<float4 *>(g_mixed_smem + NV * kTile),
                    g_mixed_smem + NV * kTile + 4 * kFvSlots};  // face values handed on
@@ -1127,11 +1145,11 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   }
   if (a.Din && t >= kNeqMax * kL64 && t < kNeqMax * (kL64 + kL32)) {  // the stage-input increment
     const int r = t - kNeqMax * kL64, v = r / kL32, l = r % kL32;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + fidx(start) + kBrickCells * v + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + brick_run(start) + kBrickCells * v + 32 * l));
   }
   if (a.Din && !a.last && t >= kNeqMax * (kL64 + kL32) && t < kNeqMax * (kL64 + 2 * kL32)) {  // FP32 SN
     const int r = t - kNeqMax * (kL64 + kL32), v = r / kL32, l = r % kL32;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + fidx(start) + kBrickCells * v + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + brick_run(start) + kBrickCells * v + 32 * l));
   }
   static_assert(kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes");
   // the stage input of the brick one wave of resident blocks ahead, on its
@@ -1139,15 +1157,15 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   if (a.ahead > 0 && int(blockIdx.x) + a.ahead < int(gridDim.x) && t >= NB - NV * kL32) {
     const int r = t - (NB - NV * kL32), v = r / kL32, l = r % kL32;
     const int next = __ldg(&a.blocks[blockIdx.x + a.ahead].start);
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Sin + fidx(next) + kBrickCells * v + 32 * l));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Sin + brick_run(next) + kBrickCells * v + 32 * l));
   }
   static_assert(NV * kL32 + kNeqMax * (kL64 + 2 * kL32) <= NB, "prefetch lanes do not overlap");
   // 1: the brick's cells and the halo from the six neighbour bricks, copied
   // global -> shared asynchronously (cp.async, no register round trip)
   const uint32_t cw0 = __ldg(&g_brick_cells<S>.w[3 * t]);
   const int ti = int(cw0 & 2047u);
-#pragma unroll
-  for (int v = 0; v < NV; ++v) cp_async4(&tile[v][ti], a.Sin + fidx(c) + kBrickCells * v);
+  cp_async16(tile.p4 + ti, a.Sin + f4idx(c));
+  cp_async4(tile.p1 + ti, a.Sin + f1idx(c));
 #pragma unroll
   for (int h = t; h < kHalo; h += NB) {
     const uint32_t e = __ldg(&g_brick_halo<S>.h[h]);
@@ -1156,8 +1174,8 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     const int base = __shfl_sync(0xffffffffu, lane_side, int((e >> 11) & 7u));
     if (base >= 0) {
       const int hti = int(e & 2047u), x = base + int(e >> 14);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) cp_async4(&tile[v][hti], a.Sin + fidx(x) + kBrickCells * v);
+      cp_async16(tile.p4 + hti, a.Sin + f4idx(x));
+      cp_async4(tile.p1 + hti, a.Sin + f1idx(x));
     }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
@@ -1175,14 +1193,10 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
       const int sg = ((e >> 13) & 1u) ? st : -st;  // outward step
       const int h1 = int(e & 2047u), own_ti = h1 - sg;
       float own[kNvMax], gv[kNvMax];
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) own[v] = v < NV ? tile[v][own_ti] : 0.0f;
+      tile.ld(own_ti, own);
       boundary_value<MODEL>(mc, -1 - s_side[side], side, own, gv);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        tile[v][h1] = gv[v];
-        tile[v][h1 + sg] = gv[v];
-      }
+      tile.st(h1, gv);
+      tile.st(h1 + sg, gv);
     }
     __syncthreads();  // bmask is uniform across the block
   }
@@ -1199,19 +1213,15 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     // 2: face values.  Own cell: all six (one slope per axis); the + face
     // values stay in registers, the - face values go to the slots.
     float q[kNvMax];
-#pragma unroll
-    for (int v = 0; v < kNvMax; ++v) q[v] = v < NV ? tile[v][ti] : 0.0f;
+    tile.ld(ti, q);
     float fpv[3][kNvMax];
     auto own_axis = [&](auto axc) {
       constexpr int AX = decltype(axc)::value;
       constexpr int FP = plus_face(AX), FM = minus_face(AX);
       constexpr int ST = AX == 0 ? 1 : (AX == 1 ? TX : S::P);
       float nbp[kNvMax], nbm[kNvMax], fm[kNvMax];
-#pragma unroll
-      for (int v = 0; v < kNvMax; ++v) {
-        nbp[v] = v < NV ? tile[v][ti + ST] : 0.0f;
-        nbm[v] = v < NV ? tile[v][ti - ST] : 0.0f;
-      }
+      tile.ld(ti + ST, nbp);
+      tile.ld(ti - ST, nbm);
       if (!MUSCL) {
 #pragma unroll
         for (int v = 0; v < kNvMax; ++v) fpv[AX][v] = fm[v] = q[v];
@@ -1236,12 +1246,9 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
         const bool upper = (e >> 13) & 1u;
         const int st = ax == 0 ? 1 : (ax == 1 ? TX : S::P);
         float qh[kNvMax], nbp[kNvMax], nbm[kNvMax], out[kNvMax];
-#pragma unroll
-        for (int v = 0; v < kNvMax; ++v) {
-          qh[v] = v < NV ? tile[v][hti] : 0.0f;
-          nbp[v] = v < NV ? tile[v][hti + st] : 0.0f;
-          nbm[v] = v < NV ? tile[v][hti - st] : 0.0f;
-        }
+        tile.ld(hti, qh);
+        tile.ld(hti + st, nbp);
+        tile.ld(hti - st, nbm);
         if (!MUSCL) {
 #pragma unroll
           for (int v = 0; v < kNvMax; ++v) out[v] = qh[v];
@@ -1350,9 +1357,7 @@ __global__ void k_state_to_f32(const double *__restrict__ S, float *__restrict__
     for (int v = 0; v < kNeqMax; ++v) x[v] = v < neq ? S[v * n + c] : 0.0;
     float q[kNvMax];
     to_state_f32<MODEL>(x, q);
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v)
-      if (v < neq) Sf[fidx(int(c)) + kBrickCells * v] = q[v];
+    st5g(Sf, int(c), q);
   }
 }
 
@@ -1369,9 +1374,7 @@ __global__ void __launch_bounds__(kBlock) k_state_to_f32_lambda(MixedConst mc, c
     for (int v = 0; v < kNeqMax; ++v) x[v] = v < mc.neq ? S[int64_t(v) * n + c] : 0.0;
     float q[kNvMax];
     to_state_f32<MODEL>(x, q);
-#pragma unroll
-    for (int v = 0; v < kNeqMax; ++v)
-      if (v < mc.neq) Sf[fidx(c) + kBrickCells * v] = q[v];
+    st5g(Sf, c, q);
     lam = fmaxf(lam, cell_lambda_f<MODEL>(mc, geo, __ldg(geom + c), q));
   }
   block_max_lambda_f(lam, lambda);
