@@ -546,9 +546,11 @@ __device__ __forceinline__ float cell_lambda_f(const MixedConst &mc, const GeoTa
 
 // RK stage update of one cell in increment form; FP64 state, FP32 copy and
 // CFL radius at the last stage (qn receives the new FP32 state words).
-template <int MODEL>
+template <int MODEL, int HD = -1, int LS = -1>  // stage has an input increment / is the last (-1: run time)
 __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dtv, const float R[kNeqMax], bool ok,
                                              float qn[kNvMax]) {
+  const bool has_din = HD < 0 ? a.Din != nullptr : HD == 1;
+  const bool last = LS < 0 ? a.last != 0 : LS == 1;
   const int n = a.n;
   bool finite = true;
 #pragma unroll
@@ -558,17 +560,17 @@ __device__ __forceinline__ bool stage_update(const StageArgs &a, int c, float dt
   // the stage-input increment, read again here rather than kept in
   // registers through the flux phase
   float din[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  if (a.Din) ld5g(a.Din, c, din);
+  if (has_din) ld5g(a.Din, c, din);
   // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
   const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
-  const bool first = a.irk == 1;
+  const bool first = HD == 0 ? true : (HD == 1 ? false : a.irk == 1);
   float dn[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     const float incr = dtv * R[v];
     dn[v] = first ? incr : w * (din[v] + incr);
   }
-  if (a.last) {
+  if (last) {
     double snew[kNeqMax];
 #pragma unroll
     for (int v = 0; v < kNeqMax; ++v) {
@@ -1095,9 +1097,14 @@ __device__ __forceinline__ float brick_lambda(const MixedConst &mc, const float 
   return acc * inv2vol;
 }
 
-template <int MODEL, bool MUSCL, bool NS, class S>
+// One instance per stage kind: HD = 1 when the stage has an input increment
+// (every stage but the first), LS = 1 for the last stage of the step (FP64
+// update, FP32 copy, CFL radius); the kind's branches are resolved at
+// compile time.
+template <int MODEL, bool MUSCL, bool NS, class S, int HD, int LS>
 __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     k_mixed_brick(MixedConst mc, StageArgs a) {
+  constexpr bool kHasDin = HD == 1, kLast = LS == 1;
   constexpr int NV = kNv<MODEL>;
   constexpr int TX = S::TX, NB = S::N;
   constexpr int kTile = S::kTile, kFaces = S::kFaces, kHalo = S::kHalo, kHalo1 = S::kHalo1;
@@ -1139,15 +1146,15 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
   // the arrays the update reads at the end, on their way to L2 (128-byte
   // lines: NB / 16 per FP64 variable, NB / 32 per FP32 one)
   constexpr int kL64 = NB / 16, kL32 = NB / 32;
-  if (a.last && t < kNeqMax * kL64) {  // the FP64 step-start state
+  if (kLast && t < kNeqMax * kL64) {  // the FP64 step-start state
     const int v = t / kL64, l = t % kL64;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SN + int64_t(v) * n + start + 16 * l));
   }
-  if (a.Din && t >= kNeqMax * kL64 && t < kNeqMax * (kL64 + kL32)) {  // the stage-input increment
+  if (kHasDin && t >= kNeqMax * kL64 && t < kNeqMax * (kL64 + kL32)) {  // the stage-input increment
     const int r = t - kNeqMax * kL64, v = r / kL32, l = r % kL32;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Din + brick_run(start) + kBrickCells * v + 32 * l));
   }
-  if (a.Din && !a.last && t >= kNeqMax * (kL64 + kL32) && t < kNeqMax * (kL64 + 2 * kL32)) {  // FP32 SN
+  if (kHasDin && !kLast && t >= kNeqMax * (kL64 + kL32) && t < kNeqMax * (kL64 + 2 * kL32)) {  // FP32 SN
     const int r = t - kNeqMax * (kL64 + kL32), v = r / kL32, l = r % kL32;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(a.SNf + brick_run(start) + kBrickCells * v + 32 * l));
   }
@@ -1342,9 +1349,9 @@ __global__ void __launch_bounds__(S::N, NS ? S::kMinBlocksNS : S::kMinBlocks)
     for (int v = 0; v < kNeqMax; ++v) R[v] = fmaf(A, fm[v] - fp[v], R[v]);
   }
   float qn[kNvMax], lam = 0.0f;
-  if (stage_update<MODEL>(a, c, s_dtv, R, ok, qn) && a.lambda)
+  if (stage_update<MODEL, HD, LS>(a, c, s_dtv, R, ok, qn) && a.lambda)
     lam = brick_lambda<MODEL>(mc, qn, be, s_geo, s_inv2vol);
-  if (a.last && a.lambda) block_max_lambda_f<NB>(lam, a.lambda);
+  if (kLast && a.lambda) block_max_lambda_f<NB>(lam, a.lambda);
 }
 
 // FP32 state words of an FP64 state (after an upload or an FP64-path
@@ -1786,32 +1793,42 @@ namespace {
 
 // Dynamic shared memory above the 48 KiB default needs a per-kernel opt-in
 // (cudaFuncAttributeMaxDynamicSharedMemorySize); it is set before any launch
-// or stream capture.
-template <class K>
-cudaError_t allow_smem(K kernel, size_t bytes) {
-  return cudaFuncSetAttribute(reinterpret_cast<const void *>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(bytes));
+// or stream capture (allow_smem_brick).
+
+// the brick kernel of a configuration and stage kind (input increment,
+// last stage)
+template <bool MUSCL, bool NS>
+const void *brick_kernel(bool din, bool last) {
+  return din ? (last ? reinterpret_cast<const void *>(k_mixed_brick<1, MUSCL, NS, Brick8, 1, 1>)
+                     : reinterpret_cast<const void *>(k_mixed_brick<1, MUSCL, NS, Brick8, 1, 0>))
+             : (last ? reinterpret_cast<const void *>(k_mixed_brick<1, MUSCL, NS, Brick8, 0, 1>)
+                     : reinterpret_cast<const void *>(k_mixed_brick<1, MUSCL, NS, Brick8, 0, 0>));
 }
-template <bool MUSCL>
-cudaError_t allow_smem_muscl(bool ns) {
-  constexpr size_t bytes = Brick8::template smem_bytes<kNeqMax>();
-  return ns ? allow_smem(k_mixed_brick<1, MUSCL, true, Brick8>, bytes)
-            : allow_smem(k_mixed_brick<1, MUSCL, false, Brick8>, bytes);
+const void *brick_kernel_rt(bool muscl, bool ns, bool din, bool last) {
+  return muscl ? (ns ? brick_kernel<true, true>(din, last) : brick_kernel<true, false>(din, last))
+               : (ns ? brick_kernel<false, true>(din, last) : brick_kernel<false, false>(din, last));
 }
 
-template <bool MUSCL>
-void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
+cudaError_t launch_brick(bool muscl, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
   constexpr size_t smem = Brick8::template smem_bytes<kNeqMax>();
-  if (mc.ns == 1)
-    k_mixed_brick<1, MUSCL, true, Brick8><<<grid, Brick8::N, smem, st>>>(mc, a);
-  else
-    k_mixed_brick<1, MUSCL, false, Brick8><<<grid, Brick8::N, smem, st>>>(mc, a);
+  const void *k = brick_kernel_rt(muscl, mc.ns == 1, a.Din != nullptr, a.last != 0);
+  MixedConst mc_ = mc;
+  StageArgs a_ = a;
+  void *args[] = {&mc_, &a_};
+  return cudaLaunchKernel(k, dim3(grid), dim3(Brick8::N), args, smem, st);
 }
 
 }  // namespace
 
 cudaError_t allow_smem_brick(bool muscl, bool ns) {
-  return muscl ? allow_smem_muscl<true>(ns) : allow_smem_muscl<false>(ns);
+  constexpr size_t bytes = Brick8::template smem_bytes<kNeqMax>();
+  for (int d = 0; d < 2; ++d)
+    for (int l = 0; l < 2; ++l) {
+      const cudaError_t e = cudaFuncSetAttribute(brick_kernel_rt(muscl, ns, d, l),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+      if (e != cudaSuccess) return e;
+    }
+  return cudaSuccess;
 }
 
 int brick_wave(bool muscl, bool ns) {
@@ -1819,11 +1836,9 @@ int brick_wave(bool muscl, bool ns) {
   int dev = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
-  const void *k = muscl ? (ns ? reinterpret_cast<const void *>(k_mixed_brick<1, true, true, Brick8>)
-                              : reinterpret_cast<const void *>(k_mixed_brick<1, true, false, Brick8>))
-                        : (ns ? reinterpret_cast<const void *>(k_mixed_brick<1, false, true, Brick8>)
-                              : reinterpret_cast<const void *>(k_mixed_brick<1, false, false, Brick8>));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Brick8::N, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brick_kernel_rt(muscl, ns, true, false), Brick8::N,
+                                                    smem) != cudaSuccess)
+    return 0;
   return sms * per_sm;
 }
 
@@ -1868,11 +1883,8 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
       if (e != cudaSuccess) return e;
     }
     marks.mark(FVGPU_KIND_MIXED_STAGE);
-    if (ph.ischeme == 2)
-      launch_brick<true>(unsigned(r.nbricks), mc, a, st);
-    else
-      launch_brick<false>(unsigned(r.nbricks), mc, a, st);
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_brick(ph.ischeme == 2, unsigned(r.nbricks), mc, a, st);
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
