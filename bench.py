@@ -343,6 +343,25 @@ def run_gpu(args):
                               "CUDA events around upload + step + download, one context",
                     "single_context": e2e_value},
         }
+        if prec == abi.MIXED:
+            # FP32 reverse passes of the residual (a mixed context's VJP) on
+            # device arrays, against one mixed stage launch
+            w = torch.ones(case.cfg.neq, n, dtype=torch.float64, device="cuda")
+            o = torch.empty_like(w)
+            torch.cuda.synchronize()
+            s.set_state(case.U)
+            for _ in range(2):
+                s.residual_vjp_device(w.data_ptr(), o.data_ptr())
+            s.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(5):
+                s.residual_vjp_device(w.data_ptr(), o.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            ms_vjp = e0.elapsed_time(e1) / 5
+            results[prec]["adjoint"] = {"ms_vjp_fp32": ms_vjp, "ms_stage": avg_ms, "vjp_over_stage": ms_vjp / avg_ms}
         if prec == abi.FP64:
             # FP64-pipe roofline of the residual kernel: counted FP64 operations
             # per launch over its live launch time, against the measured rate
@@ -556,7 +575,9 @@ def main():
         elif abi.MIXED in results and "unsupported" in results[abi.MIXED]:
             line["mixed"] = results[abi.MIXED]
         if "adjoint" in results.get(abi.FP64, {}):
-            line["adjoint"] = results[abi.FP64]["adjoint"]
+            line["adjoint"] = dict(results[abi.FP64]["adjoint"])
+            if "adjoint" in results.get(abi.MIXED, {}):
+                line["adjoint"]["mixed"] = results[abi.MIXED]["adjoint"]
         if err is not None:
             line["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps, **err}
         if results.get("workloads"):

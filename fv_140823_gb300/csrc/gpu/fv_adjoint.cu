@@ -34,33 +34,38 @@ namespace {
 constexpr int kBlock = 128;
 constexpr int NV = 5;
 
+template <typename T>
 struct St {
-  double r, ux, uy, uz, e, eint, p, c;
+  T r, ux, uy, uz, e, eint, p, c;
 };
 
 // forward face state, model 1 (facevalues.c / facercnstr.c)
-__device__ __forceinline__ void fwd_state(const Phys &ph, const double q[NV], St &s) {
+template <typename T>
+__device__ __forceinline__ void fwd_state(const Phys &ph, const T q[NV], St<T> &s) {
   s.r = q[0];
   s.ux = q[1] / s.r;
   s.uy = q[2] / s.r;
   s.uz = q[3] / s.r;
   s.e = q[4];
-  s.eint = (s.e / s.r) - 0.5 * (s.ux * s.ux + s.uy * s.uy + s.uz * s.uz);
-  s.p = s.r * (ph.gamma - 1.0) * s.eint - ph.gamma * ph.pinf;
-  s.c = sqrt(ph.gamma * (s.p + ph.pinf) / s.r);
+  const T gamma = T(ph.gamma), pinf = T(ph.pinf);
+  s.eint = (s.e / s.r) - T(0.5) * (s.ux * s.ux + s.uy * s.uy + s.uz * s.uz);
+  s.p = s.r * (gamma - T(1.0)) * s.eint - gamma * pinf;
+  s.c = sqrt(gamma * (s.p + pinf) / s.r);
 }
 
 // reverse of fwd_state: (rb, uxb, uyb, uzb, eb, pb, cb) -> qb (accumulated)
-__device__ __forceinline__ void rev_state(const Phys &ph, const double q[NV], const St &s, double rb, double uxb,
-                                          double uyb, double uzb, double eb, double pb, double cb, double qb[NV]) {
+template <typename T>
+__device__ __forceinline__ void rev_state(const Phys &ph, const T q[NV], const St<T> &s, T rb, T uxb,
+                                          T uyb, T uzb, T eb, T pb, T cb, T qb[NV]) {
   // c = sqrt(X), X = gamma (p + pinf) / r
-  const double X = ph.gamma * (s.p + ph.pinf) / s.r;
-  const double Xb = cb / (2.0 * s.c);
-  pb += Xb * ph.gamma / s.r;
+  const T gamma = T(ph.gamma), pinf = T(ph.pinf);
+  const T X = gamma * (s.p + pinf) / s.r;
+  const T Xb = cb / (T(2.0) * s.c);
+  pb += Xb * gamma / s.r;
   rb -= Xb * X / s.r;
   // p = r (gamma - 1) eint - gamma pinf
-  rb += pb * (ph.gamma - 1.0) * s.eint;
-  const double eintb = pb * s.r * (ph.gamma - 1.0);
+  rb += pb * (gamma - T(1.0)) * s.eint;
+  const T eintb = pb * s.r * (gamma - T(1.0));
   // eint = e / r - 0.5 |u|^2
   eb += eintb / s.r;
   rb -= eintb * s.e / (s.r * s.r);
@@ -79,49 +84,50 @@ __device__ __forceinline__ void rev_state(const Phys &ph, const double q[NV], co
 
 // Reverse of the HLLC normal flux Phi = F(U_K).n + S_K (U*_K - U_K) of face
 // frame f: given Phib, accumulate qLb and qRb.
-__device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], const double qR[NV],
-                         const double Phib[NV], const double velLb[3], const double velRb[3], double qLb[NV],
-                         double qRb[NV]) {
+template <typename T>
+__device__ void hllc_vjp(const Phys &ph, int f, int bc, const T qL[NV], const T qR[NV],
+                         const T Phib[NV], const T velLb[3], const T velRb[3], T qLb[NV],
+                         T qRb[NV]) {
   const double *fr = ph.frames + 9 * f;
-  const double nx = fr[0], ny = fr[1], nz = fr[2], mx = fr[3], my = fr[4], mz = fr[5], lx = fr[6], ly = fr[7],
-               lz = fr[8];
-  St L, R;
+  const T nx = T(fr[0]), ny = T(fr[1]), nz = T(fr[2]), mx = T(fr[3]), my = T(fr[4]), mz = T(fr[5]),
+          lx = T(fr[6]), ly = T(fr[7]), lz = T(fr[8]);
+  St<T> L, R;
   fwd_state(ph, qL, L);
   fwd_state(ph, qR, R);
-  const double uL = L.ux * nx + L.uy * ny + L.uz * nz;
-  const double vL = L.ux * mx + L.uy * my + L.uz * mz;
-  const double wL = L.ux * lx + L.uy * ly + L.uz * lz;
-  const double uR = R.ux * nx + R.uy * ny + R.uz * nz;
-  const double vR = R.ux * mx + R.uy * my + R.uz * mz;
-  const double wR = R.ux * lx + R.uy * ly + R.uz * lz;
-  const double ruL = L.r * uL, ruR = R.r * uR;
-  const double a1 = uL + L.c, a2 = uR + R.c, b1 = uL - L.c, b2 = uR - R.c;
+  const T uL = L.ux * nx + L.uy * ny + L.uz * nz;
+  const T vL = L.ux * mx + L.uy * my + L.uz * mz;
+  const T wL = L.ux * lx + L.uy * ly + L.uz * lz;
+  const T uR = R.ux * nx + R.uy * ny + R.uz * nz;
+  const T vR = R.ux * mx + R.uy * my + R.uz * mz;
+  const T wR = R.ux * lx + R.uy * ly + R.uz * lz;
+  const T ruL = L.r * uL, ruR = R.r * uR;
+  const T a1 = uL + L.c, a2 = uR + R.c, b1 = uL - L.c, b2 = uR - R.c;
   const bool sr_left = a1 > a2, sl_left = b1 < b2;  // max / min of compute_wave_speeds.c:53-54
-  const double SR = sr_left ? a1 : a2;
-  const double SL = sl_left ? b1 : b2;
-  const double nn = rotate_s11(nx, ny, nz, 1.0);  // d s11 / d p
-  const double s11L = rotate_s11(nx, ny, nz, L.p), s11R = rotate_s11(nx, ny, nz, R.p);
-  const double num = (L.r * (uL * uL) + s11L) - (R.r * (uR * uR) + s11R) - (SL * ruL) + (SR * ruR);
-  const double den = ruL - ruR - (SL * L.r) + (SR * R.r);
-  double SS = num / den;
+  const T SR = sr_left ? a1 : a2;
+  const T SL = sl_left ? b1 : b2;
+  const T nn = rotate_s11(nx, ny, nz, T(1.0));  // d s11 / d p
+  const T s11L = rotate_s11(nx, ny, nz, L.p), s11R = rotate_s11(nx, ny, nz, R.p);
+  const T num = (L.r * (uL * uL) + s11L) - (R.r * (uR * uR) + s11R) - (SL * ruL) + (SR * ruR);
+  const T den = ruL - ruR - (SL * L.r) + (SR * R.r);
+  T SS = num / den;
   const bool ss_const = bc == 3;
   if (ss_const) SS = 0.0;
   const bool r1 = 0.0 <= SL;
   const bool r2 = !r1 && (SL <= 0.0) && (0.0 <= SS);
   const bool r3 = !r1 && !r2 && (SS <= 0.0) && (0.0 <= SR);
   const bool left = r1 || r2, star = r2 || r3;
-  const St &K = left ? L : R;
-  const double *qK = left ? qL : qR;
-  const double uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
-  const double SK = left ? SL : SR;
+  const St<T> &K = left ? L : R;
+  const T *qK = left ? qL : qR;
+  const T uK = left ? uL : uR, vK = left ? vL : vR, wK = left ? wL : wR;
+  const T SK = left ? SL : SR;
 
   // bars of K-side quantities
-  double rKb = 0, uxKb = 0, uyKb = 0, uzKb = 0, eKb = 0, pKb = 0, uKb = 0, vKb = 0, wKb = 0, SKb = 0, SSb = 0;
-  double qKb[NV] = {0, 0, 0, 0, 0};
+  T rKb = 0, uxKb = 0, uyKb = 0, uzKb = 0, eKb = 0, pKb = 0, uKb = 0, vKb = 0, wKb = 0, SKb = 0, SSb = 0;
+  T qKb[NV] = {0, 0, 0, 0, 0};
   // F(U_K).n: [r uK, r ux uK + p nx, r uy uK + p ny, r uz uK + p nz, uK (e + p)]
   {
-    const double run = K.r * uK;
-    const double runb = Phib[0] + Phib[1] * K.ux + Phib[2] * K.uy + Phib[3] * K.uz;
+    const T run = K.r * uK;
+    const T runb = Phib[0] + Phib[1] * K.ux + Phib[2] * K.uy + Phib[3] * K.uz;
     uxKb += Phib[1] * run;
     uyKb += Phib[2] * run;
     uzKb += Phib[3] * run;
@@ -132,48 +138,48 @@ __device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], con
     uKb += runb * K.r;
   }
   if (star) {
-    const double dK = SK - uK, G = SK - SS;
-    const double Cs = K.r * dK / G;
-    const double T1 = SS * nx + vK * mx + wK * lx, T2 = SS * ny + vK * my + wK * ly,
+    const T dK = SK - uK, G = SK - SS;
+    const T Cs = K.r * dK / G;
+    const T T1 = SS * nx + vK * mx + wK * lx, T2 = SS * ny + vK * my + wK * ly,
                  T3 = SS * nz + vK * mz + wK * lz;
-    const double Z = K.p / (K.r * dK);
-    const double X = SS - uK, Y = SS + Z;
-    const double E = (K.e / K.r) + X * Y;
-    const double Us[NV] = {Cs, Cs * T1, Cs * T2, Cs * T3, Cs * E};
-    double Usb[NV];
+    const T Z = K.p / (K.r * dK);
+    const T X = SS - uK, Y = SS + Z;
+    const T E = (K.e / K.r) + X * Y;
+    const T Us[NV] = {Cs, Cs * T1, Cs * T2, Cs * T3, Cs * E};
+    T Usb[NV];
     for (int i = 0; i < NV; ++i) {  // FH = SK (Us - qK)
       SKb += Phib[i] * (Us[i] - qK[i]);
       Usb[i] = SK * Phib[i];
       qKb[i] -= SK * Phib[i];
     }
-    double Cb = Usb[0] + Usb[1] * T1 + Usb[2] * T2 + Usb[3] * T3 + Usb[4] * E;
-    const double T1b = Cs * Usb[1], T2b = Cs * Usb[2], T3b = Cs * Usb[3];
+    T Cb = Usb[0] + Usb[1] * T1 + Usb[2] * T2 + Usb[3] * T3 + Usb[4] * E;
+    const T T1b = Cs * Usb[1], T2b = Cs * Usb[2], T3b = Cs * Usb[3];
     SSb += T1b * nx + T2b * ny + T3b * nz;
     vKb += T1b * mx + T2b * my + T3b * mz;
     wKb += T1b * lx + T2b * ly + T3b * lz;
-    const double Eb = Cs * Usb[4];
+    const T Eb = Cs * Usb[4];
     eKb += Eb / K.r;
     rKb -= Eb * K.e / (K.r * K.r);
-    const double Xb = Eb * Y, Yb = Eb * X;
+    const T Xb = Eb * Y, Yb = Eb * X;
     SSb += Xb + Yb;
     uKb -= Xb;
-    const double Zb = Yb;
+    const T Zb = Yb;
     pKb += Zb / (K.r * dK);
     rKb -= Zb * Z / K.r;
-    double dKb = -Zb * Z / dK;
+    T dKb = -Zb * Z / dK;
     // Cs = r dK / G
     rKb += Cb * dK / G;
     dKb += Cb * K.r / G;
-    const double Gb = -Cb * Cs / G;
+    const T Gb = -Cb * Cs / G;
     SKb += Gb;
     SSb -= Gb;
     SKb += dKb;
     uKb -= dKb;
   }
   // map the K-side bars to L / R
-  double rLb = 0, uxLb = 0, uyLb = 0, uzLb = 0, eLb = 0, pLb = 0, cLb = 0;
-  double rRb = 0, uxRb = 0, uyRb = 0, uzRb = 0, eRb = 0, pRb = 0, cRb = 0;
-  double uLb = 0, vLb = 0, wLb = 0, uRb = 0, vRb = 0, wRb = 0, SLb = 0, SRb = 0;
+  T rLb = 0, uxLb = 0, uyLb = 0, uzLb = 0, eLb = 0, pLb = 0, cLb = 0;
+  T rRb = 0, uxRb = 0, uyRb = 0, uzRb = 0, eRb = 0, pRb = 0, cRb = 0;
+  T uLb = 0, vLb = 0, wLb = 0, uRb = 0, vRb = 0, wRb = 0, SLb = 0, SRb = 0;
   if (left) {
     rLb += rKb; uxLb += uxKb; uyLb += uyKb; uzLb += uzKb; eLb += eKb; pLb += pKb;
     uLb += uKb; vLb += vKb; wLb += wKb; SLb += SKb;
@@ -185,17 +191,17 @@ __device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], con
   }
   // S* = num / den (a constant on a slip face)
   if (!ss_const) {
-    const double numb = SSb / den, denb = -SSb * num / (den * den);
+    const T numb = SSb / den, denb = -SSb * num / (den * den);
     // num = (rL uL^2 + s11L) - (rR uR^2 + s11R) - SL ruL + SR ruR
     rLb += numb * uL * uL;
-    uLb += numb * 2.0 * L.r * uL;
+    uLb += numb * T(2.0) * L.r * uL;
     pLb += numb * nn;
     rRb -= numb * uR * uR;
-    uRb -= numb * 2.0 * R.r * uR;
+    uRb -= numb * T(2.0) * R.r * uR;
     pRb -= numb * nn;
     SLb -= numb * ruL;
     SRb += numb * ruR;
-    double ruLb = -numb * SL, ruRb = numb * SR;
+    T ruLb = -numb * SL, ruRb = numb * SR;
     // den = ruL - ruR - SL rL + SR rR
     ruLb += denb;
     ruRb -= denb;
@@ -233,26 +239,27 @@ __device__ void hllc_vjp(const Phys &ph, int f, int bc, const double qL[NV], con
 // evaluation, the bars of the face-averaged velocity gradients (gb, order
 // ux uy uz vx vy vz wx wy wz) and of the face-averaged velocity (ufb) when
 // the energy work term is on.  uf and g9 are the forward face averages.
-__device__ __forceinline__ void visc_vjp(const Phys &ph, const double *fr, const double Phib[NV],
-                                         const double uf[3], const double g9[9], double gb[9], double ufb[3]) {
+template <typename T>
+__device__ __forceinline__ void visc_vjp(const Phys &ph, const double *fr, const T Phib[NV],
+                                         const T uf[3], const T g9[9], T gb[9], T ufb[3]) {
   // R_c += A (FV . n): FV bars are -Phib n
-  double FVb[NV][3];
+  T FVb[NV][3];
 #pragma unroll
   for (int v = 0; v < NV; ++v)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) FVb[v][d] = -Phib[v] * fr[d];
-  const double mu = ph.visc + 0.0;
-  const double ux = g9[0], uy = g9[1], uz = g9[2], vx = g9[3], vy = g9[4], vz = g9[5], wx = g9[6], wy = g9[7],
+    for (int d = 0; d < 3; ++d) FVb[v][d] = -Phib[v] * T(fr[d]);
+  const T mu = T(ph.visc) + T(0.0);
+  const T ux = g9[0], uy = g9[1], uz = g9[2], vx = g9[3], vy = g9[4], vz = g9[5], wx = g9[6], wy = g9[7],
                wz = g9[8];
-  double txxb = FVb[1][0], txyb = FVb[1][1] + FVb[2][0], txzb = FVb[1][2] + FVb[3][0];
-  double tyyb = FVb[2][1], tyzb = FVb[2][2] + FVb[3][1], tzzb = FVb[3][2];
+  T txxb = FVb[1][0], txyb = FVb[1][1] + FVb[2][0], txzb = FVb[1][2] + FVb[3][0];
+  T tyyb = FVb[2][1], tyzb = FVb[2][2] + FVb[3][1], tzzb = FVb[3][2];
   ufb[0] = ufb[1] = ufb[2] = 0.0;
   if (ph.eos == 1) {
-    const double D = ux + vy + wz;
-    const double txx = mu * (2.0 * ux - (2.0 / 3.0) * D), tyy = mu * (2.0 * vy - (2.0 / 3.0) * D);
-    const double tzz = mu * (2.0 * wz - (2.0 / 3.0) * D);
-    const double txy = mu * (uy + vx), txz = mu * (uz + wx), tyz = mu * (vz + wy);
-    const double *e = FVb[4];
+    const T D = ux + vy + wz;
+    const T txx = mu * (T(2.0) * ux - T(2.0 / 3.0) * D), tyy = mu * (T(2.0) * vy - T(2.0 / 3.0) * D);
+    const T tzz = mu * (T(2.0) * wz - T(2.0 / 3.0) * D);
+    const T txy = mu * (uy + vx), txz = mu * (uz + wx), tyz = mu * (vz + wy);
+    const T *e = FVb[4];
     ufb[0] = e[0] * txx + e[1] * txy + e[2] * txz;
     ufb[1] = e[0] * txy + e[1] * tyy + e[2] * tyz;
     ufb[2] = e[0] * txz + e[1] * tyz + e[2] * tzz;
@@ -263,30 +270,33 @@ __device__ __forceinline__ void visc_vjp(const Phys &ph, const double *fr, const
     tyzb += uf[2] * e[1] + uf[1] * e[2];
     tzzb += uf[2] * e[2];
   }
-  const double Db = -(2.0 / 3.0) * mu * (txxb + tyyb + tzzb);
-  gb[0] = 2.0 * mu * txxb + Db;
-  gb[4] = 2.0 * mu * tyyb + Db;
-  gb[8] = 2.0 * mu * tzzb + Db;
+  const T Db = -T(2.0 / 3.0) * mu * (txxb + tyyb + tzzb);
+  gb[0] = T(2.0) * mu * txxb + Db;
+  gb[4] = T(2.0) * mu * tyyb + Db;
+  gb[8] = T(2.0) * mu * tzzb + Db;
   gb[1] = gb[3] = mu * txyb;
   gb[2] = gb[6] = mu * txzb;
   gb[5] = gb[7] = mu * tyzb;
 }
 
-__device__ __forceinline__ void load9(const double *__restrict__ SG, int64_t n, int64_t c, double g[9]) {
+template <typename T>
+__device__ __forceinline__ void load9(const double *__restrict__ SG, int64_t n, int64_t c, T g[9]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) g[a * 3 + d] = SG[((1 + a) * 3 + d) * n + c];
+    for (int d = 0; d < 3; ++d) g[a * 3 + d] = T(SG[((1 + a) * 3 + d) * n + c]);
 }
 
-__device__ __forceinline__ void load5(const double *__restrict__ A, int64_t n, int64_t c, double q[NV]) {
+template <typename T, typename A_T>
+__device__ __forceinline__ void load5(const A_T *__restrict__ A, int64_t n, int64_t c, T q[NV]) {
 #pragma unroll
-  for (int v = 0; v < NV; ++v) q[v] = A[v * n + c];
+  for (int v = 0; v < NV; ++v) q[v] = T(A[v * n + c]);
 }
 
 // value across face f of cell x (deltavalues.c), as the forward computes it
+template <typename T>
 __device__ __forceinline__ void across(const Phys &ph, const MeshView &m, const double *__restrict__ U, int64_t x,
-                                       int f, const double own[NV], double nb[NV]) {
+                                       int f, const T own[NV], T nb[NV]) {
   const int64_t n = m.n;
   const int32_t code = m.nbr[f * n + x];
   if (code >= 0) {
@@ -298,11 +308,11 @@ __device__ __forceinline__ void across(const Phys &ph, const MeshView &m, const 
     for (int s = 0; s < 4; ++s) {
       const int64_t ks = k[s];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) nb[v] += U[v * n + ks] / ((double)4);
+      for (int v = 0; v < NV; ++v) nb[v] += T(U[v * n + ks]) / ((T)4);
     }
   } else if (-1 - code == 1) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) nb[v] = ph.inflow[v];
+    for (int v = 0; v < NV; ++v) nb[v] = T(ph.inflow[v]);
   } else {
 #pragma unroll
     for (int v = 0; v < NV; ++v) nb[v] = own[v];
@@ -312,12 +322,13 @@ __device__ __forceinline__ void across(const Phys &ph, const MeshView &m, const 
 // Derivatives of the minmod face value SF = q + dcf grad of face g with
 // respect to q, the value across g (a) and the value across the opposite face
 // (b), per variable (reconctruct_V3.c:17-43).
-__device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g, const double q[NV],
-                                            const double na[NV], const double nb[NV], double dq[NV], double da[NV],
-                                            double db[NV]) {
+template <typename T>
+__device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g, const T q[NV],
+                                            const T na[NV], const T nb[NV], T dq[NV], T da[NV],
+                                            T db[NV]) {
   const int64_t n = m.n;
   const int go = opp_face(g);
-  const double dcf = m.dcf[g * n + x], dcc_p = m.dcc[g * n + x], dcc_m = m.dcc[go * n + x];
+  const T dcf = T(m.dcf[g * n + x]), dcc_p = T(m.dcc[g * n + x]), dcc_m = T(m.dcc[go * n + x]);
   const bool bcf = is_boundary(m.nbr[g * n + x]);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
@@ -325,9 +336,9 @@ __device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g,
     da[v] = 0.0;
     db[v] = 0.0;
     if (bcf) continue;
-    const double d0 = na[v] - q[v], d1 = nb[v] - q[v];
-    if (!(fabs(d0) > 1e-10)) continue;
-    const double product = (-d1 / dcc_m) * (d0 / dcc_p);
+    const T d0 = na[v] - q[v], d1 = nb[v] - q[v];
+    if (!(fabs(d0) > T(1e-10))) continue;
+    const T product = (-d1 / dcc_m) * (d0 / dcc_p);
     if (!(product > 0.0)) continue;
     if (fabs(-d1 / dcc_m) > fabs(d0 / dcc_p)) {  // grad = d0 / dcc_p
       dq[v] -= dcf / dcc_p;
@@ -340,51 +351,52 @@ __device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g,
 }
 
 // 1. reverse of every flux evaluation of cell c
-__global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArgs a) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArgsT<T> a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
   const bool muscl = ph.ischeme == 2;
   const bool ns = ph.ns == 1;
-  double w[NV];
+  T w[NV];
   load5(a.w, n, c, w);
-  double gown[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // bars of this cell's gradients
+  T gown[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // bars of this cell's gradients
   for (int f = 0; f < 6; ++f) {
     const int32_t code = m.nbr[f * n + c];
     const bool boundary = is_boundary(code);
     const int nsub = is_hanging(code) ? 4 : 1;
-    double qL[NV];
+    T qL[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) qL[v] = muscl ? a.SF[(f * NV + v) * n + c] : a.U[v * n + c];
-    double gl[NV] = {0, 0, 0, 0, 0};
+    T gl[NV] = {0, 0, 0, 0, 0};
     const int nf = m.nbr_face[f * n + c];
     for (int s = 0; s < nsub; ++s) {
-      double qR[NV], A;
+      T qR[NV], A;
       int64_t k = -1;
       if (boundary) {
         const int bc = -1 - code;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) qR[v] = bc == 1 ? ph.inflow[v] : qL[v];
-        A = m.area[f * n + c];
+        for (int v = 0; v < NV; ++v) qR[v] = bc == 1 ? T(ph.inflow[v]) : qL[v];
+        A = T(m.area[f * n + c]);
       } else {
         if (code >= 0) {
           k = code;
-          A = m.area[f * n + c];
+          A = T(m.area[f * n + c]);
         } else {
           const int64_t r = hang_index(code);
           k = m.hang_nbr[4 * r + s];
-          A = m.hang_area[4 * r + s];
+          A = T(m.hang_area[4 * r + s]);
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) qR[v] = muscl ? a.SF[(nf * NV + v) * n + k] : a.U[v * n + k];
       }
-      double Phib[NV], gr[NV] = {0, 0, 0, 0, 0};
+      T Phib[NV], gr[NV] = {0, 0, 0, 0, 0};
 #pragma unroll
       for (int v = 0; v < NV; ++v) Phib[v] = -(A)*w[v];
-      double vLb[3] = {0, 0, 0}, vRb[3] = {0, 0, 0}, gnb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      T vLb[3] = {0, 0, 0}, vRb[3] = {0, 0, 0}, gnb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       if (ns) {
         // forward face averages: velocities of both face states, gradients of both cells
-        double gL9[9], gR9[9], g9[9], uf[3];
+        T gL9[9], gR9[9], g9[9], uf[3];
         load9(a.SG, n, c, gL9);
         if (k >= 0)
           load9(a.SG, n, k, gR9);
@@ -392,18 +404,18 @@ __global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArg
 #pragma unroll
           for (int i = 0; i < 9; ++i) gR9[i] = gL9[i];  // a ghost carries the own gradients
 #pragma unroll
-        for (int i = 0; i < 9; ++i) g9[i] = 0.5 * (gL9[i] + gR9[i]);
-        uf[0] = 0.5 * (qL[1] / qL[0] + qR[1] / qR[0]);
-        uf[1] = 0.5 * (qL[2] / qL[0] + qR[2] / qR[0]);
-        uf[2] = 0.5 * (qL[3] / qL[0] + qR[3] / qR[0]);
-        double gb[9], ufb[3];
+        for (int i = 0; i < 9; ++i) g9[i] = T(0.5) * (gL9[i] + gR9[i]);
+        uf[0] = T(0.5) * (qL[1] / qL[0] + qR[1] / qR[0]);
+        uf[1] = T(0.5) * (qL[2] / qL[0] + qR[2] / qR[0]);
+        uf[2] = T(0.5) * (qL[3] / qL[0] + qR[3] / qR[0]);
+        T gb[9], ufb[3];
         visc_vjp(ph, ph.frames + 9 * f, Phib, uf, g9, gb, ufb);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) vLb[d] = vRb[d] = 0.5 * ufb[d];
+        for (int d = 0; d < 3; ++d) vLb[d] = vRb[d] = T(0.5) * ufb[d];
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-          gown[i] += 0.5 * gb[i];
-          gnb[i] = 0.5 * gb[i];
+          gown[i] += T(0.5) * gb[i];
+          gnb[i] = T(0.5) * gb[i];
         }
         if (boundary)
 #pragma unroll
@@ -438,13 +450,14 @@ __global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArg
 }
 
 // 2. adjoint of every face value: own evaluations + neighbour evaluations
-__global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs a) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgsT<T> a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
   for (int f = 0; f < 6; ++f) {
     const int32_t code = m.nbr[f * n + c];
-    double g[NV];
+    T g[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) g[v] = a.gL[(f * NV + v) * n + c];
     if (!is_boundary(code)) {
@@ -475,7 +488,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs
   if (ph.ns != 1) return;
   // adjoint of this cell's gradients: own evaluations + the neighbour
   // evaluations that read them (as s1.g)
-  double gt[9];
+  T gt[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) gt[i] = a.gG[i * n + c];
   for (int f = 0; f < 6; ++f) {
@@ -507,11 +520,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs
 }
 
 // 3. reverse of the reconstruction
-__global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjArgs a) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjArgsT<T> a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
-  double gu[NV] = {0, 0, 0, 0, 0};
+  T gu[NV] = {0, 0, 0, 0, 0};
   if (ph.ischeme != 2) {  // first order: every face value is the cell state
     for (int f = 0; f < 6; ++f)
 #pragma unroll
@@ -520,14 +534,14 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
     for (int v = 0; v < NV; ++v) a.out[v * n + c] = gu[v];
     return;
   }
-  double q[NV];
+  T q[NV];
   load5(a.U, n, c, q);
-  double acr[6][NV];
+  T acr[6][NV];
   for (int f = 0; f < 6; ++f) across(ph, m, a.U, c, f, q, acr[f]);
   // own face values
   for (int g = 0; g < 6; ++g) {
     const int go = opp_face(g);
-    double dq[NV], da[NV], db[NV];
+    T dq[NV], da[NV], db[NV];
     recon_deriv(m, c, g, q, acr[g], acr[go], dq, da, db);
     // across a boundary face whose ghost is the cell's own state (every
     // supported code but inflow) the neighbour value is this cell
@@ -535,7 +549,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
     const bool bnd_b = is_boundary(m.nbr[go * n + c]) && -1 - m.nbr[go * n + c] != 1;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const double gs = a.gSF[(g * NV + v) * n + c];
+      const T gs = a.gSF[(g * NV + v) * n + c];
       gu[v] += gs * dq[v];
       if (bnd_a) gu[v] += gs * da[v];  // transmissive ghost across g is this cell
       if (bnd_b) gu[v] += gs * db[v];
@@ -550,12 +564,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
     for (int s = 0; s < nk; ++s) {
       const int64_t k = is_hanging(code) ? int64_t(m.hang_nbr[4 * hang_index(code) + s]) : int64_t(code);
       // this cell counts 1/4 when the neighbour's face is a 1:4 face
-      const double wgt = is_hanging(m.nbr[gk * n + k]) ? 0.25 : 1.0;
-      double qk[NV], ak[NV], bk[NV];
+      const T wgt = is_hanging(m.nbr[gk * n + k]) ? T(0.25) : T(1.0);
+      T qk[NV], ak[NV], bk[NV];
       load5(a.U, n, k, qk);
       across(ph, m, a.U, k, gk, qk, ak);
       across(ph, m, a.U, k, opp_face(gk), qk, bk);
-      double dq[NV], da[NV], db[NV];
+      T dq[NV], da[NV], db[NV];
       // SF_k[gk]: this cell is across gk (the "a" side)
       recon_deriv(m, k, gk, qk, ak, bk, dq, da, db);
 #pragma unroll
@@ -572,21 +586,22 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
 
 // 4. reverse of gradcalc (gradcalc.c:9-47) for the momentum rows the viscous
 // flux reads: SG_k[1+a][d] = sum over k's faces 0.5 (q_nb + q_k)[1+a] n_d A / V_k
-__global__ void __launch_bounds__(kBlock) k_adj_grad(Phys ph, MeshView m, AdjArgs a) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_adj_grad(Phys ph, MeshView m, AdjArgsT<T> a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
-  const double Vc = m.vol[c];
-  double coef[3] = {0, 0, 0};  // d SG_c[.][d] / d q_c
-  double acc[3] = {0, 0, 0};   // contributions of the neighbours' gradients, per momentum row
+  const T Vc = T(m.vol[c]);
+  T coef[3] = {0, 0, 0};  // d SG_c[.][d] / d q_c
+  T acc[3] = {0, 0, 0};   // contributions of the neighbours' gradients, per momentum row
   for (int f = 0; f < 6; ++f) {
     const int32_t code = m.nbr[f * n + c];
     const double *fr = ph.frames + 9 * f;
     if (is_boundary(code)) {
-      const double own = (-1 - code == 1) ? 0.5 : 1.0;  // ghost = own state except at an inflow
-      const double A = m.area[f * n + c];
+      const T own = (-1 - code == 1) ? T(0.5) : T(1.0);  // ghost = own state except at an inflow
+      const T A = T(m.area[f * n + c]);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) coef[d] += own * fr[d] * A / Vc;
+      for (int d = 0; d < 3; ++d) coef[d] += own * T(fr[d]) * A / Vc;
       continue;
     }
     const int nf = m.nbr_face[f * n + c];
@@ -594,41 +609,72 @@ __global__ void __launch_bounds__(kBlock) k_adj_grad(Phys ph, MeshView m, AdjArg
     const int nsub = is_hanging(code) ? 4 : 1;
     for (int s = 0; s < nsub; ++s) {
       int64_t k;
-      double A;  // this cell's (sub-)face area
+      T A;  // this cell's (sub-)face area
       if (code >= 0) {
         k = code;
-        A = m.area[f * n + c];
+        A = T(m.area[f * n + c]);
       } else {
         const int64_t r = hang_index(code);
         k = m.hang_nbr[4 * r + s];
-        A = m.hang_area[4 * r + s];
+        A = T(m.hang_area[4 * r + s]);
       }
 #pragma unroll
-      for (int d = 0; d < 3; ++d) coef[d] += 0.5 * fr[d] * A / Vc;
+      for (int d = 0; d < 3; ++d) coef[d] += T(0.5) * T(fr[d]) * A / Vc;
       // the area of k's (sub-)face toward this cell
-      double Ak;
+      T Ak;
       const int32_t back = m.nbr[nf * n + k];
       if (back >= 0) {
-        Ak = m.area[nf * n + k];
+        Ak = T(m.area[nf * n + k]);
       } else {
         const int64_t r = hang_index(back);
-        Ak = 0.0;
+        Ak = T(0.0);
         for (int t = 0; t < 4; ++t)
-          if (m.hang_nbr[4 * r + t] == c) Ak = m.hang_area[4 * r + t];
+          if (m.hang_nbr[4 * r + t] == c) Ak = T(m.hang_area[4 * r + t]);
       }
-      const double wk = 0.5 * Ak / m.vol[k];
+      const T wk = T(0.5) * Ak / T(m.vol[k]);
 #pragma unroll
       for (int aa = 0; aa < 3; ++aa)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) acc[aa] += a.gSG[(aa * 3 + d) * n + k] * fk[d] * wk;
+        for (int d = 0; d < 3; ++d) acc[aa] += a.gSG[(aa * 3 + d) * n + k] * T(fk[d]) * wk;
     }
   }
 #pragma unroll
   for (int aa = 0; aa < 3; ++aa) {
-    double g = acc[aa];
+    T g = acc[aa];
 #pragma unroll
     for (int d = 0; d < 3; ++d) g += a.gSG[(aa * 3 + d) * n + c] * coef[d];
     a.out[(1 + aa) * n + c] += g;
+  }
+}
+
+// Face values of faceinterp.c:21-61 / reconctruct_V3.c:3-57 (minmod,
+// iprimtv = 0) in the arithmetic type T, from the FP64 state: the forward
+// states the FP32 reverse passes linearise at.  Boundary values as `across`
+// forms them (the adjoint's boundary codes: inflow and transmissive).
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_adj_faceinterp(Phys ph, MeshView m, const double *__restrict__ U,
+                                                           T *__restrict__ SF) {
+  const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
+  if (c >= m.n) return;
+  const int64_t n = m.n;
+  T q[NV];
+  load5(U, n, c, q);
+  T acr[6][NV];
+  for (int f = 0; f < 6; ++f) across(ph, m, U, c, f, q, acr[f]);
+  for (int f = 0; f < 6; ++f) {
+    const int fo = opp_face(f);
+    const T dcf = T(m.dcf[f * n + c]), dcc_p = T(m.dcc[f * n + c]), dcc_m = T(m.dcc[fo * n + c]);
+    const bool bcf = is_boundary(m.nbr[f * n + c]);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const T d0 = acr[f][v] - q[v], d1 = acr[fo][v] - q[v];
+      T grad = T(0.0);
+      if (!bcf && fabs(d0) > T(1e-10)) {
+        const T sp = d0 / dcc_p, sm = -d1 / dcc_m;
+        if (sm * sp > T(0.0)) grad = fabs(sm) > fabs(sp) ? sp : sm;
+      }
+      SF[(f * NV + v) * n + c] = q[v] + dcf * grad;
+    }
   }
 }
 
@@ -662,10 +708,21 @@ bool adjoint_supported(const Phys &ph, char *why, size_t whylen) {
 }
 
 void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStream_t st) {
-  k_adj_flux<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
-  k_adj_gsf<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
-  k_adj_recon<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
-  if (ph.ns == 1) k_adj_grad<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_flux<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_gsf<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_recon<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  if (ph.ns == 1) k_adj_grad<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+}
+
+void launch_adjoint_f32(const Phys &ph, const MeshView &m, const AdjArgsT<float> &a, cudaStream_t st) {
+  k_adj_flux<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_gsf<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_recon<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  if (ph.ns == 1) k_adj_grad<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+}
+
+void launch_faceinterp_f32(const Phys &ph, const MeshView &m, const double *U, float *SF, cudaStream_t st) {
+  k_adj_faceinterp<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, U, SF);
 }
 
 void launch_adj_scale(const MeshView &m, const double *g, const double *dt, double coef, double *w, cudaStream_t st) {

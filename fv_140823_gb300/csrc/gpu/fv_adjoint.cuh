@@ -28,21 +28,26 @@ namespace fv {
 //   gRg  [6][9][n]        per single-neighbour face: the neighbour's gradient bars
 //   gRgh [nhang][4][9]    per 1:4 sub-face: the fine neighbour's gradient bars
 //   gSG  [9][n]           total gradient bars (may alias gG)
-struct AdjArgs {
+// T is the type of the reverse arithmetic and of the intermediate arrays:
+// double for the FP64 path, float for the FP32-mixed path (state, weights,
+// gradients and the result stay FP64 arrays).
+template <typename T>
+struct AdjArgsT {
   const double *U;
-  const double *SF;
+  const T *SF;
   const double *w;
-  double *gL;
-  double *gR;
-  double *gRh;
-  double *gSF;
+  T *gL;
+  T *gR;
+  T *gRh;
+  T *gSF;
   double *out;
   const double *SG;
-  double *gG;
-  double *gRg;
-  double *gRgh;
-  double *gSG;
+  T *gG;
+  T *gRg;
+  T *gRgh;
+  T *gSG;
 };
+using AdjArgs = AdjArgsT<double>;
 
 // true when the adjoint implements the configuration (model 1);
 // otherwise writes the reason
@@ -51,6 +56,11 @@ bool adjoint_supported(const Phys &ph, char *why, size_t whylen);
 // the gather passes of g = (dR/dU)^T w (faceinterp of U, and gradcalc of U
 // for ns 1, must precede)
 void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStream_t st);
+// the same passes in FP32 (face values from launch_faceinterp_f32, FP64
+// gradcalc for ns 1)
+void launch_adjoint_f32(const Phys &ph, const MeshView &m, const AdjArgsT<float> &a, cudaStream_t st);
+// FP32 face values of the FP64 state U for the FP32 passes
+void launch_faceinterp_f32(const Phys &ph, const MeshView &m, const double *U, float *SF, cudaStream_t st);
 
 // w = coef * dt / vol * g
 void launch_adj_scale(const MeshView &m, const double *g, const double *dt, double coef, double *w,

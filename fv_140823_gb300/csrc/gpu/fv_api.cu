@@ -590,8 +590,46 @@ int ensure_adjoint(fvgpu_ctx *ctx) {
   return FVGPU_OK;
 }
 
-// out = (dR/dU)^T w at U (all device arrays [neq][n]); overwrites SF
+// out = (dR/dU)^T w at U (all device arrays [neq][n]) with the reverse
+// passes in FP32: face values, fluxes, limiter and EOS reversed in FP32, the
+// intermediate arrays FP32 (in the FP64 buffers), FP64 gradients for the
+// viscous flux; overwrites SF
+int enqueue_vjp_f32(fvgpu_ctx *ctx, const double *U, const double *w, double *out) {
+  const fv::MeshView mv = ctx->view();
+  if (ctx->cfg.ischeme == 2) {
+    ctx->marks.mark(FVGPU_KIND_FACEINTERP);
+    fv::launch_faceinterp_f32(ctx->ph, mv, U, ctx->SF.as<float>(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  if (ctx->cfg.ns == 1) {
+    ctx->marks.mark(FVGPU_KIND_GRADCALC);
+    fv::launch_gradcalc_fp64(ctx->ph, mv, U, ctx->SG.as<double>(), ctx->d_err(), ctx->stream);
+    FV_LAUNCHED(ctx);
+  }
+  fv::AdjArgsT<float> a{};
+  a.U = U;
+  a.SF = ctx->SF.as<float>();
+  a.w = w;
+  a.gL = ctx->adjL.as<float>();
+  a.gR = ctx->adjR.as<float>();
+  a.gRh = ctx->adjRh.as<float>();
+  a.gSF = ctx->adjL.as<float>();
+  a.out = out;
+  a.SG = ctx->SG.as<double>();
+  a.gG = ctx->adjGo.as<float>();
+  a.gRg = ctx->adjRg.as<float>();
+  a.gRgh = ctx->adjRgh.as<float>();
+  a.gSG = ctx->adjGo.as<float>();
+  ctx->marks.mark(FVGPU_KIND_ADJOINT);
+  fv::launch_adjoint_f32(ctx->ph, mv, a, ctx->stream);
+  FV_LAUNCHED(ctx);
+  return FVGPU_OK;
+}
+
+// out = (dR/dU)^T w at U (all device arrays [neq][n]); overwrites SF.  A
+// context on the FP32-mixed path runs the FP32 reverse passes.
 int enqueue_vjp(fvgpu_ctx *ctx, const double *U, const double *w, double *out) {
+  if (ctx->cfg.precision == FVGPU_MIXED) return enqueue_vjp_f32(ctx, U, w, out);
   const fv::MeshView mv = ctx->view();
   if (ctx->cfg.ischeme == 2) {
     ctx->marks.mark(FVGPU_KIND_FACEINTERP);

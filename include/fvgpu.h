@@ -263,7 +263,11 @@ int fvgpu_halo_unpack(fvgpu_ctx *ctx, const double *recv_buf);
  * 0), first order or MUSCL, boundary codes other than the walls 3 and 4;
  * other configurations return FVGPU_ERR_UNSUPPORTED.  Derivatives are those of the branch the forward
  * takes at the given state (minmod, wave-speed and HLLC-region choices); at a
- * branch switch they are one-sided. */
+ * branch switch they are one-sided.  In a context on the FP32-mixed path
+ * (FVGPU_MIXED) the reverse passes run in FP32: face values, flux, limiter
+ * and EOS reversed in FP32 with FP32 intermediate sums, linearised at the
+ * FP64 state (the multi-step adjoint recomputes its stage states with FP64
+ * steps); weights, the viscous gradients and the result stay FP64. */
 
 /* dJdU = (dR/dU)^T w for the residual R(U) of the current state; w and dJdU
  * arrays [neq][ld] in host or device memory.  The context's SF field then

@@ -367,6 +367,48 @@ def test_autograd_wrappers_on_cuda_tensors():
             assert bits_equal(got[0][0], got[1][0]) and bits_equal(got[0][1], got[1][1])
 
 
+def _mixed_case(name):
+    """A golden case for the FP32 reverse passes.  The Taylor-Green state is
+    perturbed (relative 1e-3, seeded): on its symmetry planes the HLLC
+    contact speed S* is zero in exact arithmetic, FP32 and FP64 round it to
+    either sign, and the HLLC flux, continuous there, has different
+    derivatives on the two sides."""
+    t, cfg, z = load_golden(name)
+    U = z["U"]
+    if name == "tgv_l3":
+        U = U * (1.0 + 1e-3 * np.random.default_rng(11).standard_normal(U.shape))
+    return t, cfg, U
+
+
+# FP32 reverse passes against FP64: (transposition vs the oracle, VJP, 3 SSP-RK3 steps)
+MIXED_ADJ_TOL = {"amr_periodic_first": (5e-8, 1e-6, 1e-7), "amr_periodic_muscl": (5e-8, 1e-6, 1e-7),
+                 "inflow_l3": (5e-8, 1e-6, 1e-7), "sod_l3": (5e-8, 1e-6, 1e-7), "tgv_l3": (5e-8, 1e-4, 1e-3)}
+
+
+@pytest.mark.parametrize("name", AD_CASES)
+def test_mixed_context_adjoint_in_fp32(name):
+    """A context on the FP32-mixed path reverses the residual in FP32: it
+    still transposes the oracle's exact tangent to FP32 rounding, and its
+    VJP and 3-step adjoint stay close to the FP64 ones."""
+    t, cfg, U = _mixed_case(name)
+    tol_t, tol_v, tol_s = MIXED_ADJ_TOL[name]
+    rng = np.random.default_rng(3)
+    V, W = scaled_random(rng, U), rng.standard_normal(U.shape)
+    _, JV = OracleAD(t, cfg).jvp(U, V)
+    g = {}
+    for prec in (abi.FP64, abi.MIXED):
+        with solver(t, SolverConfig(**{**cfg.__dict__, "precision": prec})) as s:
+            s.set_state(U)
+            g[prec] = s.residual_vjp(W)
+            s.set_state(U)
+            g[("steps", prec)] = s.adjoint_steps(W, 1e-3, "ssprk3", 3)
+    lhs, rhs = float(np.sum(W * JV)), float(np.sum(g[abi.MIXED] * V))
+    assert abs(lhs - rhs) <= tol_t * np.abs(W * JV).sum(), (lhs, rhs)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(g[abi.MIXED], g[abi.FP64]) <= tol_v, rel(g[abi.MIXED], g[abi.FP64])
+    assert rel(g[("steps", abi.MIXED)], g[("steps", abi.FP64)]) <= tol_s
+
+
 @pytest.mark.parametrize("name", ["bubble_l3"])
 def test_adjoint_rejects_unsupported(name):
     from fv_140823_gb300.solver import FvGpuError
