@@ -457,13 +457,13 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   float S_S = __fdividef(num, den);
   const bool ok = !isnan(S_S);
   if (bc == 3) S_S = 0.0f;
-  // region selection in the order of hllc_euler.c:18-50
-  const bool r1 = 0.0f <= SL;
-  const bool r2 = !r1 && (SL <= 0.0f) && (0.0f <= S_S);
-  const bool r3 = !r1 && !r2 && (S_S <= 0.0f) && (0.0f <= SR);
-  const bool r4 = !r1 && !r2 && !r3 && (SR <= 0.0f);
-  const bool left = r1 || r2;
-  const bool star = r2 || r3;
+  // region selection of hllc_euler.c:18-50 (0 <= SL: left; SL <= 0 <= S*:
+  // left star; S* <= 0 <= SR: right star; SR <= 0: right), reduced to two
+  // predicates; with S* not NaN (NaN wave speeds make S* NaN) exactly one
+  // region holds
+  const bool gl = 0.0f <= SL, gs = 0.0f <= S_S, gr = 0.0f <= SR;
+  const bool left = gl || gs;
+  const bool star = !gl && (gs || gr);
   const float Kr = left ? L.r : R.r, Kmn = left ? L.mn : R.mn;
   const float Kun = left ? L.un : R.un, Kum = left ? L.um : R.um, Kul = left ? L.ul : R.ul;
   const float Kp = left ? L.p : R.p, Ke = left ? L.e : R.e, Ky = left ? L.y : R.y;
@@ -494,7 +494,7 @@ __device__ __forceinline__ bool local_hllc(const MixedConst &mc, int f, int bc, 
   Fn[0] = F0;
   frame_out<F>(f, Fa, Fb, Fc, Fn);
   Fn[4] = F4;
-  return ok && (r1 || r2 || r3 || r4);
+  return ok;
 }
 
 // Canonical flux of a face from the lower / upper face values (bc > 0: a
@@ -596,21 +596,22 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v)
     if (!isfinite(R[v])) finite = false;
-  if (!ok) raise_error(a.err, kErrRegion, c);
-  if (!finite) raise_error(a.err, kErrNonFinite, c);
+  if (!(ok && finite)) raise_error(a.err, ok ? kErrNonFinite : kErrRegion, c);
+  // the stage-input increment, read again here rather than kept in
+  // registers through the flux phase
+  float din[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (a.Din) {
+#pragma unroll
+    for (int v = 0; v < kNeqMax; ++v) din[v] = __ldg(a.Din + v * n + c);
+  }
+  // stage weight w: D_k = w (D_in + dt/V R), RK(1) D1 = dt/V R as such
+  const float w = a.irk == 2 ? 0.25f : (a.irk == 3 ? (2.0f / 3.0f) : 0.5f);
+  const bool first = a.irk == 1;
   float dn[kNeqMax];
 #pragma unroll
   for (int v = 0; v < kNeqMax; ++v) {
     const float incr = dtv * R[v];
-    // the stage-input increment, read again here rather than kept in
-    // registers through the flux phase
-    const float din = a.Din ? __ldg(a.Din + v * n + c) : 0.0f;
-    switch (a.irk) {
-      case 1: dn[v] = incr; break;
-      case 2: dn[v] = 0.25f * (din + incr); break;
-      case 3: dn[v] = (2.0f / 3.0f) * (din + incr); break;
-      default: dn[v] = 0.5f * (din + incr); break;
-    }
+    dn[v] = first ? incr : w * (din[v] + incr);
   }
   if (a.last) {
     double snew[kNeqMax];
@@ -896,8 +897,11 @@ struct Block {
   }
 };
 
+// register budgets: model 1 four blocks per SM (64 registers, as shared
+// memory allows), model 3 two (the FP64 reconstruction of the paired words
+// and the pressure inversion fit 96 registers without spilling)
 template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock) k_mixed_general(MixedConst mc, StageArgs a) {
+__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(MixedConst mc, StageArgs a) {
   constexpr int NV = kNv<MODEL>;
   __shared__ float st[NV][kBlock];
   __shared__ float sf[6][NV][kBlock];
