@@ -352,7 +352,7 @@ __device__ __forceinline__ void recon_deriv(const MeshView &m, int64_t x, int g,
 
 // 1. reverse of every flux evaluation of cell c
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArgsT<T> a) {
+__device__ __forceinline__ void adj_flux(const Phys &ph, const MeshView &m, const AdjArgsT<T> &a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsf(Phys ph, MeshView m, AdjArgs
 
 // 3. reverse of the reconstruction
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjArgsT<T> a) {
+__device__ __forceinline__ void adj_recon(const Phys &ph, const MeshView &m, const AdjArgsT<T> &a) {
   const int64_t c = int64_t(blockIdx.x) * kBlock + threadIdx.x;
   if (c >= m.n) return;
   const int64_t n = m.n;
@@ -582,6 +582,20 @@ __global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjAr
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) a.out[v * n + c] = gu[v];
+}
+
+// kernels of passes 1 and 3: the FP64 ones with the whole register file
+// available, the FP32 ones at four (flux) and six (reconstruction) 128-thread
+// blocks per SM, whose register budgets their working sets fit
+__global__ void __launch_bounds__(kBlock) k_adj_flux(Phys ph, MeshView m, AdjArgsT<double> a) { adj_flux(ph, m, a); }
+__global__ void __launch_bounds__(kBlock) k_adj_recon(Phys ph, MeshView m, AdjArgsT<double> a) {
+  adj_recon(ph, m, a);
+}
+__global__ void __launch_bounds__(kBlock, 4) k_adj_flux_f32(Phys ph, MeshView m, AdjArgsT<float> a) {
+  adj_flux(ph, m, a);
+}
+__global__ void __launch_bounds__(kBlock, 6) k_adj_recon_f32(Phys ph, MeshView m, AdjArgsT<float> a) {
+  adj_recon(ph, m, a);
 }
 
 // 4. reverse of gradcalc (gradcalc.c:9-47) for the momentum rows the viscous
@@ -708,16 +722,16 @@ bool adjoint_supported(const Phys &ph, char *why, size_t whylen) {
 }
 
 void launch_adjoint(const Phys &ph, const MeshView &m, const AdjArgs &a, cudaStream_t st) {
-  k_adj_flux<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_flux<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   k_adj_gsf<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
-  k_adj_recon<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_recon<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   if (ph.ns == 1) k_adj_grad<double><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
 }
 
 void launch_adjoint_f32(const Phys &ph, const MeshView &m, const AdjArgsT<float> &a, cudaStream_t st) {
-  k_adj_flux<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_flux_f32<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   k_adj_gsf<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
-  k_adj_recon<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
+  k_adj_recon_f32<<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
   if (ph.ns == 1) k_adj_grad<float><<<grid_of(m.n), kBlock, 0, st>>>(ph, m, a);
 }
 
