@@ -25,6 +25,12 @@ constexpr int kBlock = 256;
 __host__ __device__ constexpr int axis_of(int f) { return (f == 1 || f == 3) ? 0 : ((f == 0 || f == 2) ? 1 : 2); }
 __host__ __device__ constexpr int sign_of(int f) { return (f == 1 || f == 2 || f == 5) ? 1 : -1; }
 __host__ __device__ constexpr int opp_of(int f) { return f ^ (f < 4 ? 2 : 1); }
+// element node of face f at face node s, fcnd2elnd (operatetp.c:113-147, type
+// 0); node n sits at offset (n & 1, n >> 1 & 1, n >> 2 & 1) in (x, y, z)
+__host__ __device__ constexpr int face_node(int f, int s) {
+  return int((f == 0 ? 0x4510u : f == 1 ? 0x1573u : f == 2 ? 0x3762u : f == 3 ? 0x6402u : f == 4 ? 0x0132u : 0x7546u) >>
+             (4 * s)) & 0xf;
+}
 
 __device__ __forceinline__ uint64_t spread3(uint64_t x) {
   x &= 0x1fffff;
@@ -216,15 +222,15 @@ __global__ void k_flatten(View v, const int32_t *offset, DevTables t, unsigned l
           dcf = 0.25 * d;
           dcc = 0.25 * d + 0.5 * d;
         } else {
-          // the 4 children of w on the face toward this cell, sub-face order
-          const int bb = a == 0 ? 1 : 0, cc2 = a == 2 ? 1 : 2;
+          // the 4 children of w on the face toward this cell; child s holds
+          // the corner at this cell's face node s (elconnfin.c:42-45)
           int32_t kids[4];
           bool ok = true;
           for (int s = 0; s < 4; ++s) {
             int64_t q[3];
+            const int node = face_node(f, s);
+            for (int x = 0; x < 3; ++x) q[x] = 2 * w[x] + ((node >> x) & 1);
             q[a] = 2 * w[a] + (sign_of(f) > 0 ? 0 : 1);
-            q[bb] = 2 * w[bb] + (s & 1);
-            q[cc2] = 2 * w[cc2] + (s >> 1);
             const int64_t k = v.find(l + 1, q);
             kids[s] = int32_t(k);
             ok &= k >= 0;

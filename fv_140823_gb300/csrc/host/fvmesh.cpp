@@ -31,6 +31,10 @@ int fail(int code, const char *msg) {
 constexpr int kAxis[6] = {1, 0, 1, 0, 2, 2};
 constexpr int kSign[6] = {-1, +1, +1, -1, -1, +1};
 constexpr int kOpp[6] = {2, 3, 0, 1, 5, 4};
+// Element nodes of face f in face-node order, fcnd2elnd (operatetp.c:113-147,
+// type 0); node n sits at offset (n & 1, n >> 1 & 1, n >> 2 & 1) in (x, y, z).
+constexpr int kFaceNode[6][4] = {{0, 1, 5, 4}, {3, 7, 5, 1}, {2, 6, 7, 3},
+                                 {2, 0, 4, 6}, {2, 3, 1, 0}, {6, 4, 5, 7}};
 
 struct Leaf {
   int32_t level;
@@ -185,17 +189,18 @@ struct fvmesh {
     table.build(leaves);
   }
 
-  // The 4 children of (level, p) that touch face f of a cell on the `side`
-  // opposite to f, in sub-face order: offsets along the two tangential axes
-  // (lower axis first) 00, 10, 01, 11.
+  // The 4 children of (level, p) that touch face f of a cell on the side
+  // opposite to f, in sub-face order: child s holds the corner at node
+  // fcnd2elnd(f, s) of that cell's face.  This is the order the reference's
+  // connectivity gives the fine neighbours of a face (neigtr[f][s], kid
+  // fcrefnd2elnd(ifc2, fcndrot(s, 0)) of the coarse neighbour, elconnfin.c:42-45),
+  // and so the order in which their fluxes are summed.
   void near_children(int level, const int64_t p[3], int f, int64_t q[4][3]) const {
     const int a = kAxis[f];
-    const int b = a == 0 ? 1 : 0;
-    const int c = a == 2 ? 1 : 2;
     for (int s = 0; s < 4; ++s) {
+      const int node = kFaceNode[f][s];
+      for (int x = 0; x < 3; ++x) q[s][x] = 2 * p[x] + ((node >> x) & 1);
       q[s][a] = 2 * p[a] + (kSign[f] > 0 ? 0 : 1);
-      q[s][b] = 2 * p[b] + (s & 1);
-      q[s][c] = 2 * p[c] + (s >> 1);
     }
     (void)level;
   }

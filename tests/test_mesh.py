@@ -41,6 +41,33 @@ def test_links_reciprocal_and_balanced(periodic):
                     assert t.nbr[nf, k] == c
 
 
+# fcnd2elnd (operatetp.c:113-147, type 0): element node of face f at face
+# node s; node n sits at offset (n & 1, n >> 1 & 1, n >> 2 & 1) in (x, y, z).
+FACE_NODES = [[0, 1, 5, 4], [3, 7, 5, 1], [2, 6, 7, 3], [2, 0, 4, 6], [2, 3, 1, 0], [6, 4, 5, 7]]
+
+
+@pytest.mark.parametrize("periodic", [(0, 0, 0), (1, 1, 1)])
+def test_hanging_neighbours_in_face_node_order(periodic):
+    """Fine neighbour s of a 1:4 face holds the coarse face's node s as a corner
+    (the order elconnfin.c:42-45 gives neigtr[f][s], and so the order in which
+    the four sub-face fluxes are summed)."""
+    t = amr(periodic).flatten()
+    nl = {int(l): 1 << int(l) for l in np.unique(t.level)}
+    for r in range(t.nhang):
+        c, f = int(t.hang_cell[r]), int(t.hang_face[r])
+        l = int(t.level[c])
+        for s in range(4):
+            node = FACE_NODES[f][s]
+            corner = [2 * (int(t.ijk[x, c]) + ((node >> x) & 1)) for x in range(3)]  # fine lattice
+            k = int(t.hang_nbr[r, s])
+            lo = [int(t.ijk[x, k]) for x in range(3)]
+            d = [corner[x] - lo[x] for x in range(3)]
+            # the corner lies on the fine cell's closed extent, modulo a periodic wrap
+            d = [d[x] % (2 * nl[l]) if periodic[x] else d[x] for x in range(3)]
+            assert all(v in (0, 1) for v in d), (r, s, c, f, k)
+        assert len(set(int(k) for k in t.hang_nbr[r])) == 4
+
+
 def test_volumes_and_areas():
     m = amr((1, 0, 1))
     t = m.flatten()
