@@ -33,7 +33,8 @@ def build_mesh() -> str:
     os.makedirs(LIB, exist_ok=True)
     out = os.path.join(LIB, "libfvmesh.so")
     _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-          "-Wall", "-I", INCLUDE, os.path.join(CSRC, "host", "fvmesh.cpp"), "-o", out])
+          "-Wall", "-I", INCLUDE, os.path.join(CSRC, "host", "fvmesh.cpp"),
+          os.path.join(CSRC, "host", "fvexport.cpp"), "-o", out])
     return out
 
 

@@ -46,6 +46,11 @@ def load_mesh_lib() -> C.CDLL:
         lib.fvmesh_domain.argtypes = [vp, vp, vp, vp, vp]
         lib.fvmesh_last_error.argtypes = []
         lib.fvmesh_last_error.restype = C.c_char_p
+        lib.fvmesh_export_tecplot.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp,
+                                              C.c_char_p]
+        lib.fvmesh_export_tecplot.restype = C.c_int
+        lib.fvmesh_export_last_error.argtypes = []
+        lib.fvmesh_export_last_error.restype = C.c_char_p
         lib._fv_typed = True
     return lib
 

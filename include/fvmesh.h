@@ -62,7 +62,9 @@ typedef struct fvmesh_tables {
   double  *dcc;        /* [6][ncells] centroid-to-centroid distance, distance.c */
   double  *vol;        /* [ncells] */
   double  *centroid;   /* [3][ncells] */
-  int32_t *hang_nbr;   /* [nhang][4] fine neighbours of a 1:4 face, sub-face order */
+  int32_t *hang_nbr;   /* [nhang][4] fine neighbours of a 1:4 face; neighbour s
+                          holds the face's node s, fcnd2elnd(f, s), as a corner
+                          (the reference's order, elconnfin.c:42-45) */
   double  *hang_area;  /* [nhang][4] sub-face areas */
   int32_t *hang_cell;  /* [nhang] owning (coarse) cell */
   int32_t *hang_face;  /* [nhang] owning face index */
@@ -114,6 +116,32 @@ int fvmesh_cell_nodes(const fvmesh *m, int level, int i, int j, int k, double xy
 int fvmesh_domain(const fvmesh *m, double lo[3], double len[3], int periodic[3], int side_bc[6]);
 
 const char *fvmesh_last_error(void);
+
+/* Tecplot export, exportfield_linked_V3.c:19-572 (called by loop.c:50-55
+ * after gradcalc).  Writes `path` with the reference's bytes: a " VARIABLES"
+ * line, a ZONE line (FEPOINT, BRICK), one point per node link (x y z, iel,
+ * part, then the link means of S[0..neq), P and |grad| of rho, u, v and p),
+ * then 8 one-based link numbers per leaf.  The leaf field comes from the
+ * caller (e.g. downloaded from libfvgpu): S [neq][n] and SG [neq+1][3][n]
+ * (fvgpu_gradcalc's layout; NULL prints zero gradients, as leaves that were
+ * never differentiated hold, leafallocation.c:36-40).  Tables as
+ * fvmesh_flatten fills them; lo/len the box.  Trees of the forest (the "iel"
+ * column) are the cells of level root_level, numbered along the Morton
+ * curve; no leaf may be coarser than root_level. */
+typedef struct fvmesh_tecplot {
+  int model;       /* 1 ideal gas (neq 5), 2 barotropic (neq 4), 3 mixture (neq 5) */
+  int neq;
+  int root_level;
+  int pad;
+  double gamma;    /* matergama[0] */
+  double pinf;     /* materpinf[0] */
+} fvmesh_tecplot;
+
+int fvmesh_export_tecplot(const fvmesh_tecplot *cfg, int64_t ncells, const int32_t *level,
+                          const int32_t *ijk, const int32_t *nbr, const int32_t *hang_nbr,
+                          int64_t nhang, const double lo[3], const double len[3],
+                          const double *S, const double *SG, const char *path);
+const char *fvmesh_export_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -43,6 +43,9 @@ REF_SOURCES = [
     "pvrs_mc", "leafallocation", "memallocation", "createutility", "faceinterp", "distance",
     "deltavalues", "facevalues_MUSCL", "reconctruct_V3", "cons2primtv", "prim2conc",
     "operatetp", "gradcalc", "timecpu", "criterionsplt",
+    # the Tecplot writer (loop.c:55) and what it links: volmvalues, message, getMemory,
+    # tag2adr (communicate1.c)
+    "exportfield_linked_V3", "volmvalues", "message", "getMemory", "communicate1",
 ]
 
 

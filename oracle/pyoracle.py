@@ -87,6 +87,8 @@ class RefHarness:
             L.refh_step.argtypes = [vp, vp, C.c_int]
             L.refh_conservation.argtypes = [vp, vp]
             L.refh_criterion.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+            L.refh_export.argtypes = [vp, C.c_int, C.c_int]
+            L.refh_export.restype = C.c_int
             cls._lib = L
         return cls._lib
 
@@ -176,6 +178,20 @@ class RefHarness:
         out = np.empty(self.neq + 1)
         self.lib().refh_conservation(self._h, _ptr(out))
         return out
+
+    def export(self, root_level: int, tstep: int, directory: str) -> str:
+        """gradcalc + the reference's Tecplot writer (loop.c:50-55) on the
+        current state; returns the path of field_linked<tstep>prt00.dat,
+        written in `directory`."""
+        cwd = os.getcwd()
+        os.chdir(directory)
+        try:
+            rc = self.lib().refh_export(self._h, int(root_level), int(tstep))
+        finally:
+            os.chdir(cwd)
+        if rc != 0:
+            raise ValueError("a leaf is coarser than root_level")
+        return os.path.join(directory, "field_linked%08dprt%02d.dat" % (tstep, 0))
 
     def criterion(self, i_case: int, level: int, geo_adapth: int = 0) -> np.ndarray:
         """criterionsplt.c flags of the leaves (gradients from the last gradcalc)."""

@@ -8,7 +8,8 @@
  * The reference cannot run as shipped (its time-step driver
  * advancetimeexplicit, loop.c:48, is missing, and so are brchconn,
  * cellallocation, bc_reflective and bc_wall).  This harness supplies:
- *   - a serial MPI_Wtime / MPI_Allreduce / MPI_Barrier;
+ *   - a serial MPI_Wtime / MPI_Allreduce / MPI_Barrier, and MPI_Send /
+ *     MPI_Recv that a single process never reaches;
  *   - bc_reflective / bc_wall as no-ops (the reference declares them,
  *     bc.c:38,42, but defines neither);
  *   - the BRANCH / CELL / LEAF objects the residual walks, built directly from
@@ -19,7 +20,8 @@
  *     node coordinates (the reference has no periodic boundary; this mirrors
  *     its proxy "keen" branches, forestconn.c:36-57);
  *   - the stage sequence of the missing driver: RK(0), then per stage
- *     faceinterp (MUSCL) -> gradcalc (viscous) -> RHS -> RK(k).
+ *     faceinterp (MUSCL) -> gradcalc (viscous) -> RHS -> RK(k);
+ *   - the forest the Tecplot writer walks (refh_export).
  * Leaf storage (LEAF.S, SN, RHS, SF, SG) is allocated by the reference's own
  * memallocation.c / leafallocation.c, scratch by createutility.c.
  * Node coordinates use the mesh builder's rule x = lo + I * (len / 2^level).
@@ -45,6 +47,18 @@ int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype dt, MPI_Op op, MPI
 int MPI_Barrier(MPI_Comm c) {
   (void)c;
   return 0;
+}
+/* Point-to-point calls: a single process has no peer.  The writer and the
+ * halo exchange only reach them when run->con->size > 1. */
+int MPI_Send(const void *b, int n, MPI_Datatype dt, int dest, int tag, MPI_Comm c) {
+  (void)b, (void)n, (void)dt, (void)dest, (void)tag, (void)c;
+  fprintf(stderr, "ref_harness: MPI_Send in a serial run\n");
+  return 1;
+}
+int MPI_Recv(void *b, int n, MPI_Datatype dt, int src, int tag, MPI_Comm c, MPI_Status *st) {
+  (void)b, (void)n, (void)dt, (void)src, (void)tag, (void)c, (void)st;
+  fprintf(stderr, "ref_harness: MPI_Recv in a serial run\n");
+  return 1;
 }
 
 /* ---- reference symbols that are declared but never defined -------------- */
@@ -74,6 +88,7 @@ typedef struct refh {
   int64_t nextra, capextra;
   double lo[3], len[3];
   int periodic[3];
+  int32_t *ijk; /* [3][n] leaf positions, for the export's forest */
 } refh;
 
 static const int kAxis[6] = {1, 0, 1, 0, 2, 2};
@@ -150,6 +165,8 @@ refh *refh_create(const refh_config *cfg, int64_t n, const int32_t *level, const
     h->periodic[a] = periodic[a];
   }
   h->n = n;
+  h->ijk = malloc((size_t)(3 * (n > 0 ? n : 1)) * sizeof(int32_t));
+  memcpy(h->ijk, ijk, (size_t)(3 * n) * sizeof(int32_t));
   RUN *run = calloc(1, sizeof(RUN));
   h->run = run;
   run->con = calloc(1, sizeof(CON));
@@ -300,6 +317,7 @@ void refh_destroy(refh *h) {
   for (int64_t e = 0; e < h->nextra; ++e) free(h->extra[e]);
   free(h->extra);
   free(h->cells);
+  free(h->ijk);
   free(h);
 }
 
@@ -382,4 +400,85 @@ void refh_conservation(const refh *h, double *sums) {
     sums[neq] += crnt->cl->Vol;
     crnt = crnt->lnxt;
   }
+}
+
+/* The export of loop.c:50-55 in a serial run: gradcalc, then the reference's
+ * Tecplot writer exportfield_linked_V3 (the halo exchange communicate_S
+ * between them moves nothing on one process).  The writer walks the forest,
+ * so the harness supplies one: the trees are the cells of level root_level in
+ * Morton order (x bit lowest), each tree's leaves the contiguous run of the
+ * leaf list under it, entered through a one-kid stand-in branch when the tree
+ * has more than its root leaf.  The rest of what the writer reads: pleaves,
+ * one partition with no buffer trees, octree splitting (splitmode 8), every
+ * face a 4-node quadrilateral of type 0 and every neighbour angle 0 (all
+ * leaves share one orientation).  The file, field_linked<tstep>prt00.dat, is
+ * written to the working directory.  Returns 0, or -1 when a leaf is coarser
+ * than root_level. */
+static uint64_t spread3_h(uint64_t x) {
+  uint64_t r = 0;
+  for (int b = 0; b < 21; ++b) r |= ((x >> b) & 1ull) << (3 * b);
+  return r;
+}
+
+int refh_export(refh *h, int root_level, int tstep) {
+  RUN *run = h->run;
+  const int64_t n = h->n;
+  for (int64_t c = 0; c < n; ++c)
+    if (h->cells[c]->level < root_level) return -1;
+  const int64_t ntrees = (int64_t)1 << (3 * root_level);
+  TREE **drys = calloc((size_t)ntrees, sizeof(TREE *));
+  BRANCH **stubs = calloc((size_t)ntrees, sizeof(BRANCH *));
+  for (int64_t c = 0; c < n; ++c) {
+    BRANCH *b = h->cells[c];
+    const int sh = b->level - root_level;
+    const uint64_t t = spread3_h((uint64_t)(h->ijk[c] >> sh)) | (spread3_h((uint64_t)(h->ijk[n + c] >> sh)) << 1) |
+                       (spread3_h((uint64_t)(h->ijk[2 * n + c] >> sh)) << 2);
+    b->root = (int)t;
+    if (!drys[t]) {
+      drys[t] = calloc(1, sizeof(TREE));
+      drys[t]->part = 0;
+      drys[t]->brch = b;
+    } else if (!stubs[t]) {
+      BRANCH *first = drys[t]->brch;
+      stubs[t] = calloc(1, sizeof(BRANCH));
+      stubs[t]->nkids = 1;
+      stubs[t]->kids = calloc(1, sizeof(BRANCH *));
+      stubs[t]->kids[0] = first;
+      stubs[t]->root = (int)t;
+      drys[t]->brch = stubs[t];
+    }
+    if (!b->neigag) b->neigag = calloc(6, sizeof(int));
+    for (int f = 0; f < 6; ++f) {
+      b->cl->fc[f].nnds = 4;
+      b->cl->fc[f].type = 0;
+    }
+  }
+  FOREST *topo = run->topo;
+  topo->ntrees = (int)ntrees;
+  topo->drys = drys;
+  topo->pleaves = (int)n;
+  int *nbuff = calloc(1, sizeof(int));
+  topo->nbuff = nbuff;
+  run->con->size = 1;
+  run->con->rank = 0;
+  run->con->splitmode = 8;
+  run->con->tstep = tstep;
+
+  gradcalc(run);
+  exportfield_linked_V3(run);
+
+  for (int64_t t = 0; t < ntrees; ++t) {
+    if (stubs[t]) {
+      free(stubs[t]->kids);
+      free(stubs[t]);
+    }
+    free(drys[t]);
+  }
+  free(stubs);
+  free(drys);
+  free(nbuff);
+  topo->drys = NULL;
+  topo->nbuff = NULL;
+  topo->ntrees = 0;
+  return 0;
 }

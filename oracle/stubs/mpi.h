@@ -1,7 +1,8 @@
 /* Minimal serial stand-in for <mpi.h>, written for the oracle harness.
  * The reference's hot-path sources include <mpi.h> through their common header
- * but only call MPI_Wtime and MPI_Allreduce on that path; the harness runs on a
- * single process, so these declarations are all it needs.  Handle types follow
+ * and call MPI_Wtime, MPI_Allreduce and MPI_Barrier on that path; the Tecplot
+ * writer and the halo code it links with also name MPI_Send / MPI_Recv, which a
+ * single process never reaches.  Handle types follow
  * the integer-handle convention.  Definitions live in oracle/ref_harness.c. */
 #ifndef FVORACLE_STUB_MPI_H
 #define FVORACLE_STUB_MPI_H
@@ -21,4 +22,6 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 double MPI_Wtime(void);
 int MPI_Allreduce(const void *sendbuf, void *recvbuf, int count, MPI_Datatype dt, MPI_Op op, MPI_Comm comm);
 int MPI_Barrier(MPI_Comm comm);
+int MPI_Send(const void *buf, int count, MPI_Datatype dt, int dest, int tag, MPI_Comm comm);
+int MPI_Recv(void *buf, int count, MPI_Datatype dt, int source, int tag, MPI_Comm comm, MPI_Status *status);
 #endif

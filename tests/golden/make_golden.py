@@ -15,7 +15,9 @@ any implementation that reads them (the oracle on every host, libfvgpu on the
 GPU) without the reference tree.  Needs the reference tree; run from the
 repository root:  python tests/golden/make_golden.py
 (`python tests/golden/make_golden.py fullsize` writes fullsize.json: the
-reference's 100-step Sod run as configured, see fullsize()).
+reference's 100-step Sod run as configured, see fullsize();
+`python tests/golden/make_golden.py tecplot` writes tecplot.json: digests of
+the reference's Tecplot files for these cases, see tecplot()).
 """
 from __future__ import annotations
 
@@ -140,8 +142,62 @@ def fullsize():
     print(f"fullsize: {os.path.relpath(path, REPO)}")
 
 
+def tecplot_cases():
+    """(fixture, steps, root_level, i_case) of the Tecplot fixtures: every
+    golden case at its first export (no gradcalc before it), the inviscid
+    ones also after their RK steps, and one case as a single tree."""
+    out = []
+    for path in sorted(os.listdir(HERE)):
+        if not path.endswith(".npz"):
+            continue
+        name = path[:-4]
+        z = np.load(os.path.join(HERE, path))
+        ic = 200 if name.startswith("inflow") else 0
+        rl = int(z["level"].min())
+        out.append((name, 0, rl, ic))
+        if int(z["cfg"][1]) == 0:
+            out.append((name, int(z["nsteps"]), rl, ic))
+    out.append(("sod_l3", 0, 0, 0))
+    return out
+
+
+def tecplot():
+    """The reference's Tecplot writer (exportfield_linked_V3.c, after gradcalc
+    as loop.c:50-55 calls it) on the golden cases: SHA-256 and size of each
+    file, its ZONE line and first point line (tests/golden/tecplot.json)."""
+    import tempfile
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    from fvtest import load_golden  # noqa: E402
+
+    out = {}
+    for name, steps, rl, ic in tecplot_cases():
+        t, cfg, z = load_golden(name)
+        ref = RefHarness(t, _phys(cfg, float(z["dt"]), ic))
+        try:
+            ref.set_state(z["U"])
+            if steps:
+                ref.step(str(z["scheme"]), steps)
+            with tempfile.TemporaryDirectory() as d:
+                with open(ref.export(rl, 12, d), "rb") as fh:
+                    data = fh.read()
+        finally:
+            ref.close()
+        lines = data.split(b"\n")
+        out[f"{name}/steps{steps}/root{rl}"] = {
+            "fixture": name, "steps": steps, "root_level": rl, "tstep": 12, "i_case": ic,
+            "sha256": hashlib.sha256(data).hexdigest(), "bytes": len(data),
+            "zone": lines[1].decode(), "first_point": lines[2].decode()}
+    path = os.path.join(HERE, "tecplot.json")
+    with open(path, "w") as fh:
+        json.dump(out, fh, indent=1)
+    print(f"tecplot: {len(out)} files -> {os.path.relpath(path, REPO)}")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "fullsize":
         fullsize()
+    elif len(sys.argv) > 1 and sys.argv[1] == "tecplot":
+        tecplot()
     else:
         main()
