@@ -57,6 +57,25 @@ struct View {
 
   __device__ double h(int level, int a) const { return ldexp(g.len[a], -level); }
   __device__ double coord(int level, int a, int64_t I) const { return g.lo[a] + double(I) * h(level, a); }
+  // volmproperties (meshproperties.c:66-111), hexahedron: six tetrahedra on
+  // node 0, triple product over 6.0, summed in order (no contraction: this
+  // file builds with -fmad=false)
+  __device__ double volume(int level, const int64_t p[3]) const {
+    const int tet[6][3] = {{1, 3, 5}, {5, 3, 7}, {5, 7, 4}, {3, 2, 7}, {7, 2, 6}, {7, 6, 4}};
+    double o[3];
+    for (int a = 0; a < 3; ++a) o[a] = coord(level, a, p[a]);
+    double vol = 0.0;
+    for (int it = 0; it < 6; ++it) {
+      double d[3][3];
+      for (int in = 0; in < 3; ++in)
+        for (int a = 0; a < 3; ++a) d[in][a] = coord(level, a, p[a] + ((tet[it][in] >> a) & 1)) - o[a];
+      const double c0 = d[0][1] * d[1][2] - d[0][2] * d[1][1];
+      const double c1 = d[0][2] * d[1][0] - d[0][0] * d[1][2];
+      const double c2 = d[0][0] * d[1][1] - d[0][1] * d[1][0];
+      vol += (c0 * d[2][0] + c1 * d[2][1] + c2 * d[2][2]) / 6.0;
+    }
+    return vol;
+  }
   __device__ void centroid(int level, const int64_t p[3], double c[3]) const {
     for (int a = 0; a < 3; ++a) {
       const double lo = coord(level, a, p[a]), hi = coord(level, a, p[a] + 1);
@@ -182,8 +201,7 @@ __global__ void k_flatten(View v, const int32_t *offset, DevTables t, unsigned l
     int64_t pos[3];
     v.pos(c, pos);
     t.level[c] = l;
-    const double hx = v.h(l, 0), hy = v.h(l, 1), hz = v.h(l, 2);
-    t.vol[c] = (hx * hy) * hz;
+    t.vol[c] = v.volume(l, pos);
     double cc[3];
     v.centroid(l, pos, cc);
     int64_t rec = offset[c];

@@ -130,6 +130,27 @@ struct fvmesh {
   // level, so parent and child corners agree bit for bit.
   double coord(int level, int a, int64_t I) const { return lo[a] + double(I) * h(level, a); }
 
+  // Cell volume exactly as volmproperties (meshproperties.c:66-111) forms it
+  // for a hexahedron: six tetrahedra on node 0, each triple product over 6.0,
+  // summed in order.  On a box this can differ from hx*hy*hz in the last bit.
+  double volume(int level, const int64_t p[3]) const {
+    static const int kTet[6][3] = {{1, 3, 5}, {5, 3, 7}, {5, 7, 4}, {3, 2, 7}, {7, 2, 6}, {7, 6, 4}};
+    double nd[8][3];
+    for (int n = 0; n < 8; ++n)
+      for (int a = 0; a < 3; ++a) nd[n][a] = coord(level, a, p[a] + ((n >> a) & 1));
+    double vol = 0.0;
+    for (int it = 0; it < 6; ++it) {
+      double d[3][3];
+      for (int in = 0; in < 3; ++in)
+        for (int a = 0; a < 3; ++a) d[in][a] = nd[kTet[it][in]][a] - nd[0][a];
+      const double c0 = d[0][1] * d[1][2] - d[0][2] * d[1][1];
+      const double c1 = d[0][2] * d[1][0] - d[0][0] * d[1][2];
+      const double c2 = d[0][0] * d[1][1] - d[0][1] * d[1][0];
+      vol += (c0 * d[2][0] + c1 * d[2][1] + c2 * d[2][2]) / 6.0;
+    }
+    return vol;
+  }
+
   // Cell centroid exactly as distance.c:42-56 forms it: the sum over the 8
   // local nodes of (node / 8.0), accumulated in node order.
   void centroid(int level, const int64_t p[3], double c[3]) const {
@@ -532,8 +553,7 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
     if (t->level) t->level[c] = l;
     if (t->ijk)
       for (int a = 0; a < 3; ++a) t->ijk[a * N + c] = L.p[a];
-    const double hx = m->h(l, 0), hy = m->h(l, 1), hz = m->h(l, 2);
-    if (t->vol) t->vol[c] = (hx * hy) * hz;
+    if (t->vol) t->vol[c] = m->volume(l, pos);
     double cc[3];
     m->centroid(l, pos, cc);
     if (t->centroid)

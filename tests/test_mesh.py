@@ -71,9 +71,10 @@ def test_hanging_neighbours_in_face_node_order(periodic):
 def test_volumes_and_areas():
     m = amr((1, 0, 1))
     t = m.flatten()
-    assert t.vol.sum() == pytest.approx(1.0, rel=0, abs=1e-15)
+    assert t.vol.sum() == pytest.approx(1.0, rel=0, abs=1e-14)
     h = np.ldexp(1.0, -t.level.astype(np.int64))
-    assert np.array_equal(t.vol, h * h * h)
+    # six tetrahedra as meshproperties.c:66-111 sums them: within an ulp or two of h^3
+    np.testing.assert_allclose(t.vol, h * h * h, rtol=5e-16, atol=0)
     for r in range(t.nhang):
         c, f = t.hang_cell[r], t.hang_face[r]
         assert t.hang_area[r].sum() == t.area[f, c]
