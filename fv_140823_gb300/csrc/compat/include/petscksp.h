@@ -1,0 +1,2 @@
+/* Resolves to the single PETSc declaration the reference program needs. */
+#include "petsc.h"

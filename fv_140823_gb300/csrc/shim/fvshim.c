@@ -45,9 +45,10 @@ static struct {
   double frames[54];
   int scheme, precision;
   int need_mesh, need_state, has_inner;
+  int has_grad; /* the device holds gradients of the current leaves */
   long uploads, syncs;
   void (*handler)(int, const char *);
-} G = {.scheme = FVGPU_SCHEME_SSPRK3, .precision = FVGPU_FP64, .need_mesh = 1, .need_state = 1};
+} G = {.scheme = 0, .precision = FVGPU_FP64, .need_mesh = 1, .need_state = 1};
 
 /* ---- errors ----------------------------------------------------------------- */
 
@@ -286,6 +287,7 @@ static void ensure(RUN *run) {
     G.need_mesh = 0;
     G.need_state = 1;
     G.has_inner = 0;
+    G.has_grad = 0;
   }
   if (G.need_state) {
     gather_state(run);
@@ -304,6 +306,7 @@ void faceinterp(struct RUN *run) {
 void gradcalc(struct RUN *run) {
   ensure(run);
   CHECK(fvgpu_gradcalc(G.ctx), "gradcalc");
+  G.has_grad = 1;
   /* the host calls gradcalc itself before exporting fields (loop.c:51) */
   fvshim_sync_host(run, FVSHIM_S | FVSHIM_SG);
 }
@@ -337,7 +340,9 @@ void advancetimeexplicit(struct RUN *run) {
   if (con->adapth != 0 && con->adapthstep > 0 && con->istep % con->adapthstep == 0 && G.uploads > 0)
     fvshim_invalidate(run);
   ensure(run);
-  CHECK(fvgpu_step(G.ctx, G.scheme, con->dt, 0.0, 1), "advancetimeexplicit");
+  const int scheme = G.scheme ? G.scheme : (con->method == 1 || con->method == 2 ? con->method : FVGPU_SCHEME_SSPRK3);
+  CHECK(fvgpu_step(G.ctx, scheme, con->dt, 0.0, 1), "advancetimeexplicit");
+  if (con->ns == 1) G.has_grad = 1;
   const int next = con->istep + 1;
   const int restart = con->ststep > 0 && next % con->ststep == 0;
   const int adapt = con->adapth != 0 && con->adapthstep > 0 && next % con->adapthstep == 0;
@@ -359,7 +364,7 @@ void fvshim_sync_host(struct RUN *run, int fields) {
   for (size_t k = 0; k < sizeof kinds / sizeof kinds[0]; ++k) {
     if (!(fields & kinds[k].bit)) continue;
     if (kinds[k].bit == FVSHIM_SF && run->con->ischeme != 2) continue;
-    if (kinds[k].bit == FVSHIM_SG && run->con->ns != 1) continue;
+    if (kinds[k].bit == FVSHIM_SG && !G.has_grad) continue; /* nothing computed them yet */
     const int64_t per = kinds[k].bit == FVSHIM_SF ? 6 * neq : (kinds[k].bit == FVSHIM_SG ? 3 * (neq + 1) : neq);
     G.U = grow(G.U, (size_t)(per * n) * sizeof(double));
     CHECK(fvgpu_download(G.ctx, kinds[k].field, G.U), "fvgpu_download");

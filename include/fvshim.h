@@ -42,15 +42,16 @@ struct RUN;
 #define FVSHIM_SN 2   /* LEAF.SN  */
 #define FVSHIM_RHS 4  /* LEAF.RHS */
 #define FVSHIM_SF 8   /* LEAF.SF (ischeme 2) */
-#define FVSHIM_SG 16  /* LEAF.SG (ns 1) */
+#define FVSHIM_SG 16  /* LEAF.SG (once a gradcalc or a viscous step ran) */
 
 /* Copy device fields into the leaves of run->topo->locl. */
 void fvshim_sync_host(struct RUN *run, int fields);
 /* The mesh or the leaves' S changed on the host (adaptation, restart load,
  * initialisation): flatten and upload again before the next call. */
 void fvshim_invalidate(struct RUN *run);
-/* RK scheme of advancetimeexplicit: FVGPU_SCHEME_EULER / SSPRK2 / SSPRK3
- * (default SSP-RK3). */
+/* RK scheme of advancetimeexplicit: FVGPU_SCHEME_EULER / SSPRK2 / SSPRK3,
+ * or 0 (the default) for the deck's method (CON.method, inputset.c:47):
+ * 1 Euler, 2 SSP-RK2, anything else SSP-RK3. */
 void fvshim_set_scheme(int scheme);
 /* FVGPU_FP64 (default, bit-identical to the reference) or FVGPU_MIXED. */
 void fvshim_set_precision(int precision);
