@@ -161,9 +161,11 @@ __device__ __forceinline__ float fast_sqrt(float x) { return x == 0.0f ? 0.0f : 
 // (dp/drho = c_liq^2) turns into ~130 Pa, and the gas density (~1) stored as
 // rho - kRhoOff alone would carry the ulp of ~1000, ~5 Pa of gas pressure.
 // With the pairs, model 3's reconstruction of rho and rho Y (differences,
-// limited slopes, face values) runs in FP64 and the FP64 inversion sees the
-// face values to FP64 rounding; the momentum and the flux arithmetic stay
-// FP32.  Stage increments stay five FP32 words.
+// limited slopes, face values) and the pressure inversion run in float-float
+// arithmetic (48 bits, below) and see the face values to that rounding; the
+// momentum and the flux arithmetic stay FP32.  Stage increments stay five
+// FP32 words.  FP64 remains where the FP64 state is read or written (the
+// last stage's update, the conversion of an uploaded state).
 template <int MODEL>
 constexpr int kNv = MODEL == 3 ? 7 : 5;
 constexpr int kNvMax = 7;
@@ -171,24 +173,71 @@ constexpr float kRhoOffF = 998.1618f;
 constexpr double kRhoOffD = double(kRhoOffF);
 // the low word of paired variable v (0: the density, 4: rho Y)
 __host__ __device__ constexpr int lo_word(int v) { return v == 0 ? 5 : 6; }
-// the FP64 value of paired word v of a model-3 state (the density without
-// its offset)
-__device__ __forceinline__ double pair_d(const float *q, int v) { return double(q[v]) + double(q[lo_word(v)]); }
+
+// Float-float arithmetic on the FP32 pipe.  A value is the unevaluated sum
+// hi + lo of two floats with |lo| <= ulp(hi) / 2 -- exactly the form of a
+// paired word -- so it carries 48 significant bits.  Error-free steps:
+// Knuth's two-sum, Dekker's fast two-sum (|a| >= |b|), and the exact product
+// a*b - p by one fused multiply-add; sums and products of two pairs are the
+// usual double-single forms (error about 2^-46 of the operands).  GB300's
+// FP64 pipe issues at a small fraction of the FP32 rate, so model 3 keeps its
+// paired words, their reconstruction and the pressure inversion here and
+// uses FP64 only where the FP64 state is read or written.  This file is built
+// with -fmad=false, so no product is fused into a two-sum.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+  const float p = a.hi * b;
+  return ff_fast_two_sum(p, fmaf(a.lo, b, fmaf(a.hi, b, -p)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  return ff_fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p))));
+}
+// square root of a >= 0: the FP32 root and one Newton step on the pair
+__device__ __forceinline__ FF ff_sqrt(FF a) {
+  if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+  const float s = __fsqrt_rn(a.hi);
+  const FF r = ff_sub(a, FF{s * s, fmaf(s, s, -(s * s))});
+  return ff_fast_two_sum(s, __fdiv_rn(r.hi, 2.0f * s));
+}
+__device__ __forceinline__ FF ff_abs(FF a) { return a.hi < 0.0f ? ff_neg(a) : a; }
+// a FP64 constant as a pair (host or device)
+__host__ __device__ constexpr FF ff_const(double x) { return {float(x), float(x - double(float(x)))}; }
+// paired word v as a pair, and a pair stored as paired word v
+__device__ __forceinline__ FF pair_ff(const float *q, int v) { return {q[v], q[lo_word(v)]}; }
+__device__ __forceinline__ void set_pair_ff(float *q, int v, FF x) {
+  q[v] = x.hi;
+  q[lo_word(v)] = x.lo;
+}
+// the density of a model-3 state as a pair (its offset added back)
+__device__ __forceinline__ FF state_rho_ff(const float *q) { return ff_add(FF{kRhoOffF, 0.0f}, pair_ff(q, 0)); }
 // splits an FP64 value into paired word v
 __device__ __forceinline__ void set_pair(float *q, int v, double x) {
   const float h = __double2float_rn(x);
   q[v] = h;
   q[lo_word(v)] = __double2float_rn(x - double(h));
 }
-// the density as FP64 and as FP32
-template <int MODEL>
-__device__ __forceinline__ double state_rho_d(const float *q) {
-  if constexpr (MODEL == 3) return kRhoOffD + pair_d(q, 0);
-  return double(q[0]);
-}
+// the density in FP32
 template <int MODEL>
 __device__ __forceinline__ float state_rho(const float *q) {
-  if constexpr (MODEL == 3) return __double2float_rn(state_rho_d<MODEL>(q));
+  if constexpr (MODEL == 3) return state_rho_ff(q).hi;
   return q[0];
 }
 // FP32 state words of an FP64 state (model 3: seven words)
@@ -206,51 +255,51 @@ __device__ __forceinline__ void to_state_words(const double x[kNeqMax], float q[
 // the pressure quadratic, the liquid sound speed with the mixture fallback)
 // on the two partial densities: the reference's products rho Y and
 // rho (1 - Y) are the gas partial density ry and rho - ry, taken as such from
-// the paired state words.  FP64; false when neither branch has a real root.
-__device__ __forceinline__ bool eos_mixture_partial(double r, double ry, double &p_out, double &c_out) {
-  const double R_G = 286.0, T_ref = 293.15, r_sat = 998.1618, p_sat = 2340.0;
-  const double c_liq = 1482.5, c_mixture = 1.0;
-  const double rg = ry * R_G * T_ref, rl = r - ry;
-  double ct = c_liq;
-  double c2 = ct * ct;
-  double b = c2 * r_sat - p_sat - rg - rl * c2;
-  double d = (p_sat - c2 * r_sat) * rg;
-  double disc = b * b - 4.0 * d;
-  if (!(disc >= 0.0)) {
-    ct = c_mixture;
-    c2 = ct * ct;
-    b = c2 * r_sat - p_sat - rg - rl * c2;
-    d = (p_sat - c2 * r_sat) * rg;
-    disc = b * b - 4.0 * d;
-    if (!(disc >= 0.0)) {
-      p_out = __longlong_as_double(0x7ff8000000000000ll);
-      c_out = ct;
-      return false;
-    }
-  }
-  p_out = 0.5 * (sqrt(disc) - b);
-  c_out = ct;
+// the paired state words.  Float-float: b = c^2 r_sat - p_sat - ry R T -
+// (rho - ry) c^2 cancels to a few parts in 1e4 of its terms in the liquid, and
+// the pairs keep it to ~1e-10 of the pressure.  The larger root is returned
+// rounded to FP32; false when neither branch has a real root.
+// one branch of the inversion: sound speed squared c2 (exact in FP32), k1 =
+// c^2 r_sat - p_sat, k2 = p_sat - c^2 r_sat; false without a real root
+__device__ __forceinline__ bool mixture_root(FF rg, FF rl, FF k1, FF k2, float c2, float &p) {
+  const FF b = ff_sub(ff_sub(k1, rg), ff_mul_f(rl, c2));
+  const FF d = ff_mul(k2, rg);
+  const FF disc = ff_sub(ff_mul(b, b), ff_mul_f(d, 4.0f));
+  if (!(disc.hi >= 0.0f)) return false;
+  p = ff_mul_f(ff_sub(ff_sqrt(disc), b), 0.5f).hi;
   return true;
 }
+__device__ __forceinline__ bool eos_mixture_ff(FF r, FF ry, float &p_out, float &c_out) {
+  constexpr double R_G = 286.0, T_ref = 293.15, r_sat = 998.1618, p_sat = 2340.0;
+  constexpr double c_liq = 1482.5, c_mix = 1.0;
+  constexpr FF kRT = ff_const(R_G * T_ref);
+  const FF rg = ff_mul(ry, kRT), rl = ff_sub(r, ry);
+  c_out = float(c_liq);
+  if (mixture_root(rg, rl, ff_const(c_liq * c_liq * r_sat - p_sat), ff_const(p_sat - c_liq * c_liq * r_sat),
+                   float(c_liq * c_liq), p_out))
+    return true;
+  c_out = float(c_mix);
+  if (mixture_root(rg, rl, ff_const(c_mix * c_mix * r_sat - p_sat), ff_const(p_sat - c_mix * c_mix * r_sat),
+                   float(c_mix * c_mix), p_out))
+    return true;
+  p_out = __int_as_float(0x7fc00000);
+  return false;
+}
 
-// Model 3: the FP64 density and gas partial density of a face value for the
-// pressure inversion, with the mass fraction clipped as facercnstr.c:43-44
-// (clip) and returned in FP32 for the flux.
+// Model 3: the density and gas partial density of a face value as pairs for
+// the pressure inversion, with the mass fraction clipped as
+// facercnstr.c:43-44 (clip), and returned in FP32 for the flux.
 __device__ __forceinline__ bool mixture_face_eos(const MixedConst &mc, const float *q, bool clip, float &r32,
                                                  float &y32, float &p32, float &c32) {
-  const double r = kRhoOffD + pair_d(q, 0);
-  double ry = pair_d(q, 4);
-  r32 = __double2float_rn(r);
-  y32 = __double2float_rn(ry) * fast_rcp(r32);
+  const FF r = state_rho_ff(q);
+  FF ry = pair_ff(q, 4);
+  r32 = r.hi;
+  y32 = ry.hi * fast_rcp(r32);
   if (clip && (y32 < mc.ylo || y32 > mc.yhi)) {
     y32 = y32 < mc.ylo ? mc.ylo : mc.yhi;
-    ry = double(y32) * r;
+    ry = ff_mul_f(r, y32);
   }
-  double p, c;
-  const bool ok = eos_mixture_partial(r, ry, p, c);
-  p32 = float(p);
-  c32 = float(c);
-  return ok;
+  return eos_mixture_ff(r, ry, p32, c32);
 }
 
 // FP32 face state (facercnstr.c:20-59 / facevalues.c:113-142).
@@ -290,7 +339,7 @@ __device__ __forceinline__ void boundary_value(const MixedConst &mc, int bc, int
   for (int v = 0; v < kNv<MODEL>; ++v) nb[v] = own[v];
   if (bc == 1) {
 #pragma unroll
-    for (int v = 0; v < kNeqMax; ++v) nb[v] = mc.inflow[v];
+    for (int v = 0; v < kNv<MODEL>; ++v) nb[v] = mc.inflow[v];
   } else if (bc == 3) {
     const float nx = mc.fr[9 * f], ny = mc.fr[9 * f + 1], nz = mc.fr[9 * f + 2];
     const float mn = fmaf(own[3], nz, fmaf(own[2], ny, own[1] * nx));
@@ -630,13 +679,13 @@ __device__ __forceinline__ bool stage_update(const MixedConst &mc, const StageAr
     a.Dout[v * n + c] = dn[v];
     a.Sout[v * n + c] = __ldg(a.SNf + v * n + c) + dn[v];  // the value the next stage would form
   }
-  if constexpr (MODEL == 3) {  // paired words: the next stage's input to FP64 rounding
+  if constexpr (MODEL == 3) {  // paired words: the next stage's input as a pair
 #pragma unroll
     for (int v = 0; v < kNeqMax; v += 4) {
       float w[kNvMax];
       w[v] = __ldg(a.SNf + v * n + c);
       w[lo_word(v)] = __ldg(a.SNf + lo_word(v) * n + c);
-      set_pair(w, v, pair_d(w, v) + double(dn[v]));
+      set_pair_ff(w, v, ff_add(pair_ff(w, v), FF{dn[v], 0.0f}));
       a.Sout[v * n + c] = w[v];
       a.Sout[lo_word(v) * n + c] = w[lo_word(v)];
     }
@@ -797,17 +846,18 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
 
 // ============================ general kernel ================================
 
-// Model 3: the FP64 minmod slope of a paired word (reconctruct_V3.c:17-43,
+// Model 3: the minmod slope of a paired word as a pair (reconctruct_V3.c:17-43,
 // as minmod_slope).
-__device__ __forceinline__ double minmod_slope_d(bool active, double d0, double d1, double inv_p, double inv_m) {
-  const double sp = d0 * inv_p, sm = -d1 * inv_m;
-  const double m = fabs(sm) > fabs(sp) ? sp : sm;
-  return (active && fabs(d0) > 1e-10 && sm * sp > 0.0) ? m : 0.0;
+__device__ __forceinline__ FF minmod_slope_ff(bool active, FF d0, FF d1, float inv_p, float inv_m) {
+  const FF sp = ff_mul_f(d0, inv_p), sm = ff_mul_f(ff_neg(d1), inv_m);
+  const FF m = ff_sub(ff_abs(sm), ff_abs(sp)).hi > 0.0f ? sp : sm;
+  const bool same_sign = (sm.hi > 0.0f && sp.hi > 0.0f) || (sm.hi < 0.0f && sp.hi < 0.0f);
+  return (active && fabsf(d0.hi) > 1e-10f && same_sign) ? m : FF{0.0f, 0.0f};
 }
 
 // Model 3: face value of face f of a cell with geometry code gx from its
 // state words and the values across f (nbf) and across the opposite face
-// (nbo): the momentum as recon_face does, the paired words in FP64.
+// (nbo): the momentum as recon_face does, the paired words as pairs.
 __device__ __forceinline__ void recon_face_m3(const GeoTables *geo, int32_t gx, int f, const float *qx,
                                               const float *nbf, const float *nbo, float *out) {
   const int lev = level_of(gx);
@@ -821,9 +871,9 @@ __device__ __forceinline__ void recon_face_m3(const GeoTables *geo, int32_t gx, 
     out[v] = fmaf(dcf, minmod_slope(act, nbf[v] - qx[v], nbo[v] - qx[v], inv_p, inv_m), qx[v]);
 #pragma unroll
   for (int v = 0; v < kNeqMax; v += 4) {
-    const double q = pair_d(qx, v);
-    const double sl = minmod_slope_d(act, pair_d(nbf, v) - q, pair_d(nbo, v) - q, double(inv_p), double(inv_m));
-    set_pair(out, v, fma(double(dcf), sl, q));
+    const FF q = pair_ff(qx, v);
+    const FF sl = minmod_slope_ff(act, ff_sub(pair_ff(nbf, v), q), ff_sub(pair_ff(nbo, v), q), inv_p, inv_m);
+    set_pair_ff(out, v, ff_add(q, ff_mul_f(sl, dcf)));
   }
 }
 
@@ -846,7 +896,7 @@ struct Block {
     global_state<MODEL>(a, x, q);
   }
   // value across face f of cell x (deltavalues.c): single neighbour, mean of
-  // the four fine ones (model 3: the paired words summed in FP64), or the
+  // the four fine ones (model 3: the paired words summed as pairs), or the
   // boundary ghost
   __device__ __forceinline__ void across(int x, int f, const float *own, float *nb) const {
     const int32_t code = __ldg(a.nbr + f * a.n + x);
@@ -855,7 +905,7 @@ struct Block {
     } else if (is_hanging(code)) {
       const int32_t *k = a.hang_nbr + 4 * hang_index(code);
       float acc[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      double acc2[2] = {0.0, 0.0};
+      FF acc2[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
 #pragma unroll 1
       for (int s = 0; s < 4; ++s) {
         float q[kNvMax];
@@ -863,15 +913,15 @@ struct Block {
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) acc[v] += q[v];
         if constexpr (MODEL == 3) {
-          acc2[0] += pair_d(q, 0);
-          acc2[1] += pair_d(q, 4);
+          acc2[0] = ff_add(acc2[0], pair_ff(q, 0));
+          acc2[1] = ff_add(acc2[1], pair_ff(q, 4));
         }
       }
 #pragma unroll
       for (int v = 0; v < kNeqMax; ++v) nb[v] = 0.25f * acc[v];
-      if constexpr (MODEL == 3) {
-        set_pair(nb, 0, 0.25 * acc2[0]);
-        set_pair(nb, 4, 0.25 * acc2[1]);
+      if constexpr (MODEL == 3) {  // a quarter of a pair is exact
+        set_pair_ff(nb, 0, FF{0.25f * acc2[0].hi, 0.25f * acc2[0].lo});
+        set_pair_ff(nb, 4, FF{0.25f * acc2[1].hi, 0.25f * acc2[1].lo});
       }
     } else {
       boundary_value<MODEL>(mc, -1 - code, f, own, nb);
@@ -898,8 +948,8 @@ struct Block {
 };
 
 // register budgets: model 1 four blocks per SM (64 registers, as shared
-// memory allows), model 3 two (the FP64 reconstruction of the paired words
-// and the pressure inversion fit 96 registers without spilling)
+// memory allows), model 3 two (the float-float reconstruction of the paired
+// words and the pressure inversion take about 100 registers)
 template <int MODEL, bool MUSCL>
 __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(MixedConst mc, StageArgs a) {
   constexpr int NV = kNv<MODEL>;
