@@ -1,6 +1,8 @@
 // FP32-mixed path interface (fv_mixed.cu).
 #pragma once
 
+#include <vector>
+
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -35,6 +37,9 @@ struct MixedResources {
   // table-driven family (fv_mixed_amr.cu; every other mesh)
   int family = 0;
   int wave = 0;  // resident brick blocks across the GPU (family 0)
+  // host copy of the per-level geometry tables (family 1): the general
+  // kernel takes them by value, so they sit in the constant bank
+  std::vector<unsigned char> geo_host;
 };
 
 bool mixed_supported(const Phys &ph, char *why, size_t whylen);

@@ -784,7 +784,9 @@ __device__ __forceinline__ void load_grad9f(const float *__restrict__ SG, int n,
 // Green-Gauss momentum gradients of the stage-input state (gradcalc.c:9-47,
 // rows of rho u, rho v, rho w), FP32, one cell per thread.
 template <int MODEL>
-__global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs a, float *__restrict__ SGout) {
+__global__ void __launch_bounds__(kBlock)
+    k_mixed_grad(MixedConst mc, StageArgs a, float *__restrict__ SGout, const __grid_constant__ GeoTables geo_tab) {
+  const GeoTables *geo = &geo_tab;
   const int c = blockIdx.x * kBlock + threadIdx.x;
   const int n = a.n;
   if (c >= n) return;
@@ -792,7 +794,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
   global_state<MODEL>(a, c, q);
   const int32_t g = __ldg(a.geom + c);
   const int lev = level_of(g);
-  const float inv_vol = a.geo->inv_vol[lev];
+  const float inv_vol = geo->inv_vol[lev];
   float gr[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int f = 0; f < 6; ++f) {
     const int32_t code = __ldg(a.nbr + f * n + c);
@@ -826,10 +828,10 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
           m[2] = q[3];
         }
       }
-      add(m, geo_face(a.geo, lev, f, kRelBoundary)[2]);
+      add(m, geo_face(geo, lev, f, kRelBoundary)[2]);
     } else if (is_hanging(code)) {
       const int32_t *k = a.hang_nbr + 4 * hang_index(code);
-      const float A = a.geo->sub_area[lev * 6 + f];
+      const float A = geo->sub_area[lev * 6 + f];
       for (int s = 0; s < 4; ++s) {
         const int ks = __ldg(k + s);
         const float m[3] = {__ldg(a.Sin + 1 * n + ks), __ldg(a.Sin + 2 * n + ks), __ldg(a.Sin + 3 * n + ks)};
@@ -837,7 +839,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_grad(MixedConst mc, StageArgs 
       }
     } else {
       const float m[3] = {__ldg(a.Sin + 1 * n + code), __ldg(a.Sin + 2 * n + code), __ldg(a.Sin + 3 * n + code)};
-      add(m, geo_face(a.geo, lev, f, rel_of(g, f))[2]);
+      add(m, geo_face(geo, lev, f, rel_of(g, f))[2]);
     }
   }
 #pragma unroll
@@ -882,10 +884,12 @@ struct Block {
   static constexpr int NV = kNv<MODEL>;
   const StageArgs &a;
   const MixedConst &mc;
+  const GeoTables *geo;  // the kernel's by-value copy (constant bank)
   int c0, cnt;
   const float (*st)[kBlock];
-  __device__ Block(const StageArgs &a_, const MixedConst &mc_, int c0_, int cnt_, const float (*st_)[kBlock])
-      : a(a_), mc(mc_), c0(c0_), cnt(cnt_), st(st_) {}
+  __device__ Block(const StageArgs &a_, const MixedConst &mc_, const GeoTables *geo_, int c0_, int cnt_,
+                   const float (*st_)[kBlock])
+      : a(a_), mc(mc_), geo(geo_), c0(c0_), cnt(cnt_), st(st_) {}
   __device__ __forceinline__ bool in_block(int x) const { return unsigned(x - c0) < unsigned(cnt); }
   __device__ __forceinline__ void state(int x, float *q) const {
     if (in_block(x)) {
@@ -899,7 +903,10 @@ struct Block {
   // the four fine ones (model 3: the paired words summed as pairs), or the
   // boundary ghost
   __device__ __forceinline__ void across(int x, int f, const float *own, float *nb) const {
-    const int32_t code = __ldg(a.nbr + f * a.n + x);
+    across_code(__ldg(a.nbr + f * a.n + x), f, own, nb);
+  }
+  // the same with the neighbour code of face f already at hand
+  __device__ __forceinline__ void across_code(int32_t code, int f, const float *own, float *nb) const {
     if (code >= 0) {
       state(code, nb);
     } else if (is_hanging(code)) {
@@ -934,7 +941,7 @@ struct Block {
     across(x, f, qx, nbp);
     across(x, opp_face(f), qx, nbm);
     if constexpr (MODEL == 3) {
-      recon_face_m3(a.geo, __ldg(a.geom + x), f, qx, nbp, nbm, out);
+      recon_face_m3(geo, __ldg(a.geom + x), f, qx, nbp, nbm, out);
     } else {
       float d0[kNeqMax], d1[kNeqMax];
 #pragma unroll
@@ -942,7 +949,7 @@ struct Block {
         d0[v] = nbp[v] - qx[v];
         d1[v] = nbm[v] - qx[v];
       }
-      recon_face(a.geo, __ldg(a.geom + x), f, qx, d0, d1, out);
+      recon_face(geo, __ldg(a.geom + x), f, qx, d0, d1, out);
     }
   }
 };
@@ -951,7 +958,8 @@ struct Block {
 // memory allows), model 3 two (the float-float reconstruction of the paired
 // words and the pressure inversion take about 100 registers)
 template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(MixedConst mc, StageArgs a) {
+__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4)
+    k_mixed_general(MixedConst mc, StageArgs a, const __grid_constant__ GeoTables geo_tab) {
   constexpr int NV = kNv<MODEL>;
   __shared__ float st[NV][kBlock];
   __shared__ float sf[6][NV][kBlock];
@@ -964,7 +972,8 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(Mi
   const int n = a.n;
   const bool active = t < bd.count;
   constexpr bool muscl = MUSCL;
-  Block<MODEL> blk(a, mc, c0, bd.count, st);
+  const GeoTables *geo = &geo_tab;
+  Block<MODEL> blk(a, mc, geo, c0, bd.count, st);
 
   // A: own stage state
   float q[kNvMax];
@@ -990,12 +999,12 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(Mi
         if (f == 2 || f == 3 || f == 5) continue;  // the lower face of each pair carries the axis
         const int fo = opp_face(f);
         float nbf[kNvMax], nbo[kNvMax], o[kNvMax];
-        blk.across(c, f, q, nbf);
-        blk.across(c, fo, q, nbo);
-        recon_face_m3(a.geo, g, f, q, nbf, nbo, o);
+        blk.across_code(nb[f], f, q, nbf);
+        blk.across_code(nb[fo], fo, q, nbo);
+        recon_face_m3(geo, g, f, q, nbf, nbo, o);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sf[f][v][t] = o[v];
-        recon_face_m3(a.geo, g, fo, q, nbo, nbf, o);
+        recon_face_m3(geo, g, fo, q, nbo, nbf, o);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sf[fo][v][t] = o[v];
       }
@@ -1004,14 +1013,14 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(Mi
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         float nbv[kNeqMax];
-        blk.across(c, f, q, nbv);
+        blk.across_code(nb[f], f, q, nbv);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) dl[f][v] = nbv[v] - q[v];
       }
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         float o[kNeqMax];
-        recon_face(a.geo, g, f, q, dl[f], dl[opp_face(f)], o);
+        recon_face(geo, g, f, q, dl[f], dl[opp_face(f)], o);
 #pragma unroll
         for (int v = 0; v < kNeqMax; ++v) sf[f][v][t] = o[v];
       }
@@ -1041,7 +1050,7 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(Mi
     const int rel = rel_of(g, f);
     const int nsub = hanging ? 4 : 1;
     const int32_t *hk = hanging ? a.hang_nbr + 4 * hang_index(code) : nullptr;
-    const float A = hanging ? a.geo->sub_area[lev * 6 + f] : geo_face(a.geo, lev, f, rel)[2];
+    const float A = hanging ? geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
 #pragma unroll 1
     for (int s = 0; s < nsub; ++s) {
       const int other = boundary ? -1 : (hanging ? __ldg(hk + s) : code);
@@ -1102,8 +1111,8 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4) k_mixed_general(Mi
   float lam = 0.0f;
   if (active) {
     float qn[kNvMax];
-    const float dtv = s_dt * a.geo->inv_vol[level_of(g)];
-    if (stage_update<MODEL>(mc, a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, a.geo, g, qn);
+    const float dtv = s_dt * geo->inv_vol[level_of(g)];
+    if (stage_update<MODEL>(mc, a, c, dtv, R, ok, qn) && a.lambda) lam = cell_lambda_f<MODEL>(mc, geo, g, qn);
   }
   if (a.last && a.lambda) block_max_lambda_f(lam, a.lambda);
 }
@@ -1979,6 +1988,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   all.insert(all.end(), bricks4.begin(), bricks4.end());
   all.insert(all.end(), general.begin(), general.end());
   const int64_t nv = ph.model == 3 ? kNv<3> : kNv<1>;  // FP32 state words per cell
+  r.geo_host.assign(reinterpret_cast<const unsigned char *>(&gt), reinterpret_cast<const unsigned char *>(&gt) + sizeof gt);
   cudaError_t e;
   if ((e = alloc_slot(r, kBufGeom, sizeof(int32_t) * n)) != cudaSuccess ||
       (e = cudaMemcpy(r.buf[kBufGeom], geom.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -2080,21 +2090,22 @@ void launch_brick(unsigned grid, const MixedConst &mc, const StageArgs &a, cudaS
 enum BlockKind { kKindGeneral = 0, kKindBrick8 = 1, kKindBrick4 = 2 };
 
 template <int MODEL, bool MUSCL>
-void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageArgs &a, cudaStream_t st) {
+void launch_instance(int kind, unsigned grid, const MixedConst &mc, const StageArgs &a, const GeoTables &geo,
+                     cudaStream_t st) {
   if constexpr (MODEL == 1) {
     if (kind == kKindBrick8) return launch_brick<MODEL, MUSCL, Brick8>(grid, mc, a, st);
     if (kind == kKindBrick4) return launch_brick<MODEL, MUSCL, Brick4>(grid, mc, a, st);
   }
-  k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a);
+  k_mixed_general<MODEL, MUSCL><<<grid, kBlock, 0, st>>>(mc, a, geo);
 }
 
 void launch_kernel(const Phys &ph, int kind, unsigned grid, const MixedConst &mc, const StageArgs &a,
-                   cudaStream_t st) {
+                   const GeoTables &geo, cudaStream_t st) {
   const bool muscl = ph.ischeme == 2;
   if (ph.model == 1)
-    muscl ? launch_instance<1, true>(kind, grid, mc, a, st) : launch_instance<1, false>(kind, grid, mc, a, st);
+    muscl ? launch_instance<1, true>(kind, grid, mc, a, geo, st) : launch_instance<1, false>(kind, grid, mc, a, geo, st);
   else
-    muscl ? launch_instance<3, true>(kind, grid, mc, a, st) : launch_instance<3, false>(kind, grid, mc, a, st);
+    muscl ? launch_instance<3, true>(kind, grid, mc, a, geo, st) : launch_instance<3, false>(kind, grid, mc, a, geo, st);
 }
 
 // One RK step from FP64 state `in` (and its FP32 copy) to `out`.
@@ -2131,9 +2142,11 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
       marks.mark(FVGPU_KIND_MIXED_AUX);
       const unsigned gg = unsigned((m.n + kBlock - 1) / kBlock);
       if (ph.model == 1)
-        k_mixed_grad<1><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
+        k_mixed_grad<1><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]),
+                                               *reinterpret_cast<const GeoTables *>(r.geo_host.data()));
       else
-        k_mixed_grad<3><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]));
+        k_mixed_grad<3><<<gg, kBlock, 0, st>>>(mc, a, static_cast<float *>(r.buf[kBufSG]),
+                                               *reinterpret_cast<const GeoTables *>(r.geo_host.data()));
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -2156,7 +2169,8 @@ cudaError_t enqueue_step_mixed(MixedResources &r, const Phys &ph, const MeshView
       if (count[k] == 0) continue;
       cudaStream_t ks = (fork && k > 0) ? r.side[k - 1] : st;
       a.blocks = blocks + offset[k];
-      launch_kernel(ph, kind_of[k], unsigned(count[k]), mc, a, ks);
+      launch_kernel(ph, kind_of[k], unsigned(count[k]), mc, a, *reinterpret_cast<const GeoTables *>(r.geo_host.data()),
+                    ks);
       cudaError_t e = cudaGetLastError();
       if (e == cudaSuccess && ks != st) e = cudaEventRecord(r.join_ev[k - 1], ks);
       if (e != cudaSuccess) return e;
