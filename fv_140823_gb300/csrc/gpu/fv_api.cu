@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "../host/fvframes.h"
 #include "fv_adjoint.cuh"
 #include "fv_flatten.cuh"
 #include "fv_kernels.cuh"
@@ -145,11 +146,13 @@ uint64_t fnv1a(uint64_t h, const void *data, size_t bytes) {
 }
 constexpr uint64_t kFnvSeed = 0xcbf29ce484222325ull;
 
-// Face frames of an axis-aligned box (fvmesh_flatten's table: outward normal,
-// t1 along the face's first edge, t2 = n x t1; normalvector.c / tagvector.c)
-const double kBoxFrames[54] = {0, -1, 0, 1, 0, 0, 0, 0, 1,  1, 0, 0, 0, 0, 1, 0, -1, 0,
-                               0, 1, 0, 0, 0, 1, 1, 0, 0,   -1, 0, 0, 0, -1, 0, 0, 0, 1,
-                               0, 0, -1, 1, 0, 0, 0, -1, 0, 0, 0, 1, 0, -1, 0, 1, 0, 0};
+// Face frames of an axis-aligned box, the same as fvmesh_flatten's
+// (normalvector.c / tagvector.c; ../host/fvframes.h)
+struct BoxFrames {
+  double v[54];
+  BoxFrames() { fv_box_frames(v); }
+};
+const BoxFrames kBoxFrames;
 
 int set_err(fvgpu_ctx *ctx, int code, const char *fmt, ...) {
   char buf[512];
@@ -992,7 +995,7 @@ int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *lv) {
   m.vol = h_vol.data();
   m.hang_nbr = h_hnbr.data();
   m.hang_area = h_harea.data();
-  m.frames = kBoxFrames;
+  m.frames = kBoxFrames.v;
   m.level = h_level.data();
   return finish_mesh(ctx, &m);
 }

@@ -57,6 +57,22 @@ struct View {
 
   __device__ double h(int level, int a) const { return ldexp(g.len[a], -level); }
   __device__ double coord(int level, int a, int64_t I) const { return g.lo[a] + double(I) * h(level, a); }
+  // areaproperties (meshproperties.c:29-63): face f's two triangles (face
+  // nodes 0,1,2 and 0,2,3), half the norm of each cross product, summed
+  __device__ double face_area(int level, const int64_t p[3], int f) const {
+    double nd[4][3];
+    for (int s = 0; s < 4; ++s)
+      for (int a = 0; a < 3; ++a) nd[s][a] = coord(level, a, p[a] + ((face_node(f, s) >> a) & 1));
+    double area = 0.0;
+    for (int it = 0; it < 2; ++it) {
+      const double dx1 = nd[1 + it][0] - nd[0][0], dx2 = nd[2 + it][0] - nd[0][0];
+      const double dy1 = nd[1 + it][1] - nd[0][1], dy2 = nd[2 + it][1] - nd[0][1];
+      const double dz1 = nd[1 + it][2] - nd[0][2], dz2 = nd[2 + it][2] - nd[0][2];
+      const double cx = dy1 * dz2 - dz1 * dy2, cy = dz1 * dx2 - dx1 * dz2, cz = dx1 * dy2 - dy1 * dx2;
+      area += fabs(0.5 * sqrt(cx * cx + cy * cy + cz * cz));
+    }
+    return area;
+  }
   // volmproperties (meshproperties.c:66-111), hexahedron: six tetrahedra on
   // node 0, triple product over 6.0, summed in order (no contraction: this
   // file builds with -fmad=false)
@@ -208,11 +224,9 @@ __global__ void k_flatten(View v, const int32_t *offset, DevTables t, unsigned l
     for (int f = 0; f < 6; ++f) {
       const int64_t fc = int64_t(f) * N + c;
       const int a = axis_of(f);
-      const int b = a == 0 ? 1 : 0;
-      const int cax = a == 2 ? 1 : 2;
       int64_t w[3], u[3];
       int32_t code;
-      const double area = v.h(l, b) * v.h(l, cax);
+      const double area = v.face_area(l, pos, f);
       double dcf = 0.0, dcc = 0.0;
       int nface = opp_of(f);
       if (!v.neighbour_pos(l, pos, f, w, u)) {
@@ -255,10 +269,15 @@ __global__ void k_flatten(View v, const int32_t *offset, DevTables t, unsigned l
           }
           if (!ok) atomicCAS(err, 0ull, (3ull << 40) | (unsigned long long)c);
           code = int32_t(-16 - rec);  // FVGPU_HANG0 - record
-          const double sub = v.h(l + 1, b) * v.h(l + 1, cax);
           for (int s = 0; s < 4; ++s) {
+            // the fine neighbour's own face toward this cell, at its
+            // unwrapped position (areaproperties on neigtr[f][s])
+            int64_t qu[3];
+            const int node = face_node(f, s);
+            for (int x = 0; x < 3; ++x) qu[x] = 2 * u[x] + ((node >> x) & 1);
+            qu[a] = 2 * u[a] + (sign_of(f) > 0 ? 0 : 1);
             t.hang_nbr[rec * 4 + s] = kids[s];
-            t.hang_area[rec * 4 + s] = sub;
+            t.hang_area[rec * 4 + s] = v.face_area(l + 1, qu, opp_of(f));
           }
           ++rec;
           v.centroid(l, u, cn);

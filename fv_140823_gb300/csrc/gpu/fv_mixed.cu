@@ -1545,6 +1545,16 @@ bool mixed_supported(const Phys &ph, char *why, size_t whylen) {
   return true;
 }
 
+// Geometry of two faces is the same for the FP32 tables when the FP32 values
+// agree to a few ulps: the FP64 areas and distances follow the reference's
+// node-coordinate arithmetic and vary in the last bits from cell to cell
+// where the box length is not a power of two.
+static bool same_geo(float a, float b) {
+  if (a == b) return true;
+  const float m = fabsf(a) > fabsf(b) ? fabsf(a) : fabsf(b);
+  return fabsf(a - b) <= 4e-7f * m;
+}
+
 // The kernel family of a mesh: the brick kernel of this file for model 1 in
 // 8x8x4 bricks throughout, the table-driven family (fv_mixed_amr.cu)
 // otherwise.
@@ -1617,7 +1627,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         const int64_t h = int64_t(FVGPU_HANG0) - nc;
         const float sa = float(m->hang_area[4 * h]);
         for (int s = 1; s < 4; ++s)
-          if (float(m->hang_area[4 * h + s]) != sa) {
+          if (!same_geo(float(m->hang_area[4 * h + s]), sa)) {
             snprintf(why, whylen, "the mixed path needs equal sub-face areas");
             return FVGPU_ERR_UNSUPPORTED;
           }
@@ -1625,7 +1635,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         if (!seen_sub[k]) {
           seen_sub[k] = 1;
           gt.sub_area[k] = sa;
-        } else if (gt.sub_area[k] != sa) {
+        } else if (!same_geo(gt.sub_area[k], sa)) {
           snprintf(why, whylen, "the mixed path needs one sub-face area per level and face");
           return FVGPU_ERR_UNSUPPORTED;
         }
@@ -1662,7 +1672,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         e[1] = inv_dcc;
         e[2] = area;
         e[3] = kf;
-      } else if (e[0] != dcf || !(e[1] == inv_dcc) || e[2] != area || e[3] != kf) {
+      } else if (!same_geo(e[0], dcf) || !same_geo(e[1], inv_dcc) || !same_geo(e[2], area) || !same_geo(e[3], kf)) {
         snprintf(why, whylen, "the mixed path needs octree-regular geometry (cell %lld face %d)", (long long)c, f);
         return FVGPU_ERR_UNSUPPORTED;
       }
@@ -1673,7 +1683,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         if (!seen_axis[ai]) {
           seen_axis[ai] = 1;
           gt.axis_area[ai] = area;
-        } else if (gt.axis_area[ai] != area) {
+        } else if (!same_geo(gt.axis_area[ai], area)) {
           snprintf(why, whylen, "the mixed path needs equal areas of a cell's single-neighbour faces on an axis "
                                 "(cell %lld face %d)", (long long)c, f);
           return FVGPU_ERR_UNSUPPORTED;

@@ -1820,6 +1820,16 @@ bool brick_sides_resolve(const fvgpu_mesh_soa *m, int64_t i, const std::vector<c
   return true;
 }
 
+// Geometry of two faces is the same for the FP32 tables when the FP32 values
+// agree to a few ulps: the FP64 areas and distances follow the reference's
+// node-coordinate arithmetic and vary in the last bits from cell to cell
+// where the box length is not a power of two.
+static bool same_geo(float a, float b) {
+  if (a == b) return true;
+  const float m = fabsf(a) > fabsf(b) ? fabsf(a) : fabsf(b);
+  return fabsf(a - b) <= 4e-7f * m;
+}
+
 }  // namespace
 
 int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen) {
@@ -1874,7 +1884,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         const int64_t h = int64_t(FVGPU_HANG0) - nc;
         const float sa = float(m->hang_area[4 * h]);
         for (int s = 1; s < 4; ++s)
-          if (float(m->hang_area[4 * h + s]) != sa) {
+          if (!same_geo(float(m->hang_area[4 * h + s]), sa)) {
             snprintf(why, whylen, "the mixed path needs equal sub-face areas");
             return FVGPU_ERR_UNSUPPORTED;
           }
@@ -1882,7 +1892,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         if (!seen_sub[k]) {
           seen_sub[k] = 1;
           gt.sub_area[k] = sa;
-        } else if (gt.sub_area[k] != sa) {
+        } else if (!same_geo(gt.sub_area[k], sa)) {
           snprintf(why, whylen, "the mixed path needs one sub-face area per level and face");
           return FVGPU_ERR_UNSUPPORTED;
         }
@@ -1916,7 +1926,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
         e[0] = dcf;
         e[1] = inv_dcc;
         e[2] = area;
-      } else if (e[0] != dcf || !(e[1] == inv_dcc) || e[2] != area) {
+      } else if (!same_geo(e[0], dcf) || !same_geo(e[1], inv_dcc) || !same_geo(e[2], area)) {
         snprintf(why, whylen, "the mixed path needs octree-regular geometry (cell %lld face %d)", (long long)c, f);
         return FVGPU_ERR_UNSUPPORTED;
       }

@@ -9,6 +9,7 @@
 // Morton curve.  fvmesh_flatten() turns it into the SoA tables the GPU
 // library consumes.
 #include "fvmesh.h"
+#include "fvframes.h"
 
 #include <algorithm>
 #include <array>
@@ -149,6 +150,27 @@ struct fvmesh {
       vol += (c0 * d[2][0] + c1 * d[2][1] + c2 * d[2][2]) / 6.0;
     }
     return vol;
+  }
+
+  // Area of face f of the cell at (level, p) exactly as areaproperties
+  // (meshproperties.c:29-63) forms it from the node coordinates: the face's
+  // triangles (face nodes 0,1,2 and 0,2,3), each half the norm of the cross
+  // product of its edges from face node 0, summed in order.  Where the box
+  // length is not a power of two the node coordinates round, and the area
+  // differs from hx*hy by up to ~1e-13 relative, differently from cell to cell.
+  double face_area(int level, const int64_t p[3], int f) const {
+    double nd[4][3];
+    for (int s = 0; s < 4; ++s)
+      for (int a = 0; a < 3; ++a) nd[s][a] = coord(level, a, p[a] + ((kFaceNode[f][s] >> a) & 1));
+    double area = 0.0;
+    for (int it = 0; it < 2; ++it) {
+      const double dx1 = nd[1 + it][0] - nd[0][0], dx2 = nd[2 + it][0] - nd[0][0];
+      const double dy1 = nd[1 + it][1] - nd[0][1], dy2 = nd[2 + it][1] - nd[0][1];
+      const double dz1 = nd[1 + it][2] - nd[0][2], dz2 = nd[2 + it][2] - nd[0][2];
+      const double cx = dy1 * dz2 - dz1 * dy2, cy = dz1 * dx2 - dx1 * dz2, cz = dx1 * dy2 - dy1 * dx2;
+      area += std::fabs(0.5 * std::sqrt(cx * cx + cy * cy + cz * cz));
+    }
+    return area;
   }
 
   // Cell centroid exactly as distance.c:42-56 forms it: the sum over the 8
@@ -532,19 +554,8 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
   int64_t nh = 0;
 
   // Frames per face index: outward normal, t1 along the face's first edge
-  // (node fcnd2elnd(f,0) -> fcnd2elnd(f,1), operatetp.c:113-147) and
-  // t2 = n x t1, as normalvector.c / tagvector.c form them for a box.
-  static const double kFrames[6][9] = {
-      {0, -1, 0, 1, 0, 0, 0, 0, 1},   // f0 -y
-      {1, 0, 0, 0, 0, 1, 0, -1, 0},   // f1 +x
-      {0, 1, 0, 0, 0, 1, 1, 0, 0},    // f2 +y
-      {-1, 0, 0, 0, -1, 0, 0, 0, 1},  // f3 -x
-      {0, 0, -1, 1, 0, 0, 0, -1, 0},  // f4 -z
-      {0, 0, 1, 0, -1, 0, 1, 0, 0},   // f5 +z
-  };
-  if (t->frames)
-    for (int f = 0; f < 6; ++f)
-      for (int q = 0; q < 9; ++q) t->frames[f * 9 + q] = kFrames[f][q] + 0.0;
+  // and t2, as normalvector.c / tagvector.c form them (signed zeros included)
+  if (t->frames) fv_box_frames(t->frames);
 
   for (int64_t c = 0; c < N; ++c) {
     const Leaf &L = m->leaves[size_t(c)];
@@ -561,12 +572,9 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
 
     for (int f = 0; f < 6; ++f) {
       const int64_t fc = int64_t(f) * N + c;
-      const int a = kAxis[f];
-      const int b = a == 0 ? 1 : 0;
-      const int cax = a == 2 ? 1 : 2;
       int64_t w[3], u[3];
       int32_t code;
-      double area = m->h(l, b) * m->h(l, cax);
+      const double area = m->face_area(l, pos, f);
       double dcf = 0.0, dcc = 0.0;
       int nface = kOpp[f];
       if (!m->neighbour_pos(L, f, w, u)) {
@@ -606,10 +614,13 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
             if (kids[s] < 0) return fail(FVMESH_ERR_BALANCE, "face sees more than one level of refinement");
           }
           code = FVMESH_HANG0 - int32_t(nh);
-          const double sub = m->h(l + 1, b) * m->h(l + 1, cax);
+          // areaproperties: each sub-face area is the fine neighbour's own
+          // face toward this cell, at the neighbour's unwrapped position
+          int64_t qu[4][3];
+          m->near_children(l, u, f, qu);
           for (int s = 0; s < 4; ++s) {
             if (t->hang_nbr) t->hang_nbr[nh * 4 + s] = kids[s];
-            if (t->hang_area) t->hang_area[nh * 4 + s] = sub;
+            if (t->hang_area) t->hang_area[nh * 4 + s] = m->face_area(l + 1, qu[s], kOpp[f]);
           }
           if (t->hang_cell) t->hang_cell[nh] = int32_t(c);
           if (t->hang_face) t->hang_face[nh] = f;

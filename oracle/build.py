@@ -46,6 +46,8 @@ REF_SOURCES = [
     # the Tecplot writer (loop.c:55) and what it links: volmvalues, message, getMemory,
     # tag2adr (communicate1.c)
     "exportfield_linked_V3", "volmvalues", "message", "getMemory", "communicate1",
+    # the geometry routines (refh_geometry): areas, volumes, face frames
+    "meshproperties", "normalvector", "tagvector",
 ]
 
 

@@ -89,6 +89,7 @@ class RefHarness:
             L.refh_criterion.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
             L.refh_export.argtypes = [vp, C.c_int, C.c_int]
             L.refh_export.restype = C.c_int
+            L.refh_geometry.argtypes = [vp, vp, vp, vp]
             cls._lib = L
         return cls._lib
 
@@ -178,6 +179,16 @@ class RefHarness:
         out = np.empty(self.neq + 1)
         self.lib().refh_conservation(self._h, _ptr(out))
         return out
+
+    def geometry(self):
+        """The reference's own volume, face / sub-face areas and face frames of
+        every leaf (meshproperties.c, normalvector.c, tagvector.c): vol [n],
+        area [6][4][n], frames [6][9][n]."""
+        vol = np.empty(self.n)
+        area = np.empty((6, 4, self.n))
+        frames = np.empty((6, 9, self.n))
+        self.lib().refh_geometry(self._h, _ptr(vol), _ptr(area), _ptr(frames))
+        return vol, area, frames
 
     def export(self, root_level: int, tstep: int, directory: str) -> str:
         """gradcalc + the reference's Tecplot writer (loop.c:50-55) on the

@@ -226,6 +226,10 @@ refh *refh_create(const refh_config *cfg, int64_t n, const int32_t *level, const
     cl->xc = centroid[c];
     cl->yc = centroid[n + c];
     cl->zc = centroid[2 * n + c];
+    for (int f = 0; f < 6; ++f) {
+      cl->fc[f].nnds = 4; /* createlfc.c:20-45, hexahedron */
+      cl->fc[f].type = 0;
+    }
     b->neigtr = calloc(6, sizeof(BRANCH **));
     b->lfc_neigs = calloc(6, sizeof(int));
     b->neigfc = calloc(6, sizeof(int));
@@ -481,4 +485,32 @@ int refh_export(refh *h, int root_level, int tstep) {
   topo->nbuff = NULL;
   topo->ntrees = 0;
   return 0;
+}
+
+/* The reference's own geometry of every leaf from the harness's node
+ * coordinates: cell volume (volmproperties), face and sub-face areas
+ * (areaproperties; a 1:4 face's four areas come from the fine neighbours'
+ * faces, in neigtr order) and the per-face frames n, t1, t2
+ * (normalvectorcalc, tagvectorcalc), all from meshproperties.c, normalvector.c
+ * and tagvector.c.  vol [n], area [6][4][n] (zero where a face has fewer
+ * sub-faces), frames [6][9][n].  The leaves' own geometry fields are
+ * overwritten with these values. */
+void refh_geometry(refh *h, double *vol, double *area, double *frames) {
+  RUN *run = h->run;
+  const int64_t n = h->n;
+  for (int64_t c = 0; c < n; ++c) {
+    BRANCH *b = h->cells[c];
+    areaproperties(b, run);
+    volmproperties(0, b, run);
+    normalvectorcalc(run, b);
+    tagvectorcalc(run, b);
+    CELL *cl = b->cl;
+    vol[c] = cl->Vol;
+    for (int f = 0; f < 6; ++f) {
+      for (int s = 0; s < 4; ++s) area[((int64_t)f * 4 + s) * n + c] = s < b->nsfc[f] ? cl->Area[f][s] : 0.0;
+      const double fr[9] = {cl->nx[f], cl->ny[f], cl->nz[f], cl->nxt1[f], cl->nyt1[f],
+                            cl->nzt1[f], cl->nxt2[f], cl->nyt2[f], cl->nzt2[f]};
+      for (int k = 0; k < 9; ++k) frames[((int64_t)f * 9 + k) * n + c] = fr[k];
+    }
+  }
 }

@@ -116,3 +116,39 @@ def test_conservation_sums_sequential_order():
     ref, orc = RefHarness(t, phys(cfg)), Oracle(t, cfg)
     ref.set_state(U)
     assert bits_equal(orc.conservation(U), ref.conservation())
+
+
+def _geometry_meshes():
+    m = uniform_mesh(2, periodic=(1, 0, 1))
+    refine_by(m, lambda l, c: ((c[0] - 0.6) ** 2 + (c[1] - 0.5) ** 2 + (c[2] - 0.45) ** 2) < 0.07, 4)
+    return {"amr_unit": m.flatten(),
+            "tgv_2pi": cases.tgv(base_level=3, extra_levels=2).tables,
+            "bubble": cases.bubble(base_level=3, extra_levels=1).tables,
+            "bump": cases.bump(base_level=3, extra_levels=2).tables}
+
+
+@pytest.mark.parametrize("name", ["amr_unit", "tgv_2pi", "bubble", "bump"])
+def test_geometry_equals_the_references_own(name):
+    """Cell volumes, face and 1:4 sub-face areas and face frames of the mesh
+    tables equal, bit for bit, what the reference's own meshproperties.c,
+    normalvector.c and tagvector.c compute from the leaves' node coordinates
+    (the 2*pi Taylor-Green box is the case where coordinates round)."""
+    t = _geometry_meshes()[name]
+    ref = RefHarness(t, PhysConfig(model=1, ns=0, ischeme=2, iprimtv=0, eos=0, i_case=0, gamma=1.4, pinf=0.0,
+                                   visc=0.0, ymin=0.0, dt=1e-3))
+    try:
+        vol, area, frames = ref.geometry()
+    finally:
+        ref.close()
+    n = t.ncells
+    want = np.zeros((6, 4, n))
+    for f in range(6):
+        for c in range(n):
+            code = int(t.nbr[f, c])
+            if code <= -16:
+                want[f, :, c] = t.hang_area[-16 - code]
+            else:
+                want[f, 0, c] = t.area[f, c]
+    assert bits_equal(vol, t.vol)
+    assert bits_equal(area, want)
+    assert bits_equal(frames, np.repeat(np.asarray(t.frames).reshape(6, 9)[:, :, None], n, axis=2))
