@@ -443,7 +443,45 @@ def amr_workloads(args, torch, flush, hbm_peak):
             err[names[v]] = float(np.linalg.norm(a[v] - b[v])) / den
         res["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
         res["rel_l2_mixed_vs_fp64"] = {"steps": args.err_steps_amr, "momentum_against": "|rho u| norm", **err}
+        if key in ADAPTIVE:
+            res["adaptive"] = adaptive_run(make, ADAPTIVE[key], torch)
         out[key] = res
+    return out
+
+
+# C2 as configured: 200 steps with an adaptation every 10 (|grad rho| h > 50
+# kg/m^3 asks for the finest level; levels 4..7)
+ADAPTIVE = {"C2": dict(steps=200, every=10, threshold=50.0, min_level=4, max_level=7)}
+
+
+def adaptive_run(make, cfg, torch):
+    """The whole configured run on each path: CFL SSP-RK3 steps, the device
+    criterion, host adaptation with state transfer and re-upload every
+    `every` steps.  Host wall clock over the run (adaptations included);
+    cell-updates counted on the mesh each segment ran on."""
+    from fv_140823_gb300 import abi
+    from fv_140823_gb300.abi import SolverConfig
+    from fv_140823_gb300.adaptive import AdaptConfig, run_adaptive_gpu
+    from fv_140823_gb300.solver import Solver
+    ac = AdaptConfig(every=cfg["every"], kind=abi.CRIT_GRAD_RHO_H, threshold=cfg["threshold"],
+                     min_level=cfg["min_level"], max_level=cfg["max_level"])
+    out = {"steps": cfg["steps"], "every": cfg["every"], "criterion": "|grad rho| h > %g" % cfg["threshold"],
+           "levels": [cfg["min_level"], cfg["max_level"]], "timing": "host wall clock over the whole run, "
+           "adaptations (criterion, host refine/merge, transfer, re-upload) included"}
+    for prec, name in ((abi.MIXED, "mixed"), (abi.FP64, "fp64")):
+        case = make()
+        n0 = case.tables.ncells
+        with Solver(case.tables, SolverConfig(**{**case.cfg.__dict__, "precision": prec})) as s:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            run = run_adaptive_gpu(s, case.mesh, case.U, cfg["steps"], ac, "ssprk3", case.cfl)
+            s.synchronize()
+            wall = time.perf_counter() - t0
+        seg = [n0] + list(run.cells)
+        updates = sum(c * min(cfg["every"], cfg["steps"] - i * cfg["every"]) for i, c in enumerate(seg))
+        out[name] = {"value": updates / wall / 1e6, "unit": UNIT, "seconds": wall, "adaptations": len(run.cells),
+                     "cells_first_last": [n0, run.cells[-1] if run.cells else n0]}
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     return out
 
 
