@@ -32,7 +32,7 @@ def _run(cmd: list[str]) -> None:
 def build_mesh() -> str:
     os.makedirs(LIB, exist_ok=True)
     out = os.path.join(LIB, "libfvmesh.so")
-    _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+    _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-fopenmp",
           "-Wall", "-I", INCLUDE, os.path.join(CSRC, "host", "fvmesh.cpp"),
           os.path.join(CSRC, "host", "fvexport.cpp"), "-o", out])
     return out

@@ -92,6 +92,8 @@ struct fvgpu_ctx {
   // adjoint work arrays (allocated by the first adjoint call)
   unsigned bc_mask = 0;  // bit b set when boundary code b occurs in the mesh
   uint64_t mesh_sig = 0;  // FNV-1a of the uploaded tables (restart files carry it)
+  bool mesh_sig_valid = false;  // formed on first use from the resident tables
+  bool mesh_has_level = false;  // the upload carried per-cell levels
   DevBuf adjL, adjR, adjRh, adjW, adjG, adjAcc, adjOut, adjY1, adjY2, adjSN, adjCK;
   DevBuf adjGo, adjRg, adjRgh;  // viscous: gradient bars
   // halo exchange index lists
@@ -865,21 +867,9 @@ static int finish_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   ctx->halo_send.release();
   ctx->halo_recv.release();
   ctx->nsend = ctx->nrecv = 0;
-  {
-    uint64_t h = kFnvSeed;
-    h = fnv1a(h, &m->ncells, sizeof(int64_t));
-    h = fnv1a(h, &m->nhang, sizeof(int64_t));
-    h = fnv1a(h, m->nbr, sizeof(int32_t) * 6 * size_t(n));
-    h = fnv1a(h, m->nbr_face, sizeof(int32_t) * 6 * size_t(n));
-    h = fnv1a(h, m->area, sizeof(double) * 6 * size_t(n));
-    h = fnv1a(h, m->vol, sizeof(double) * size_t(n));
-    if (nh > 0) {
-      h = fnv1a(h, m->hang_nbr, sizeof(int32_t) * 4 * size_t(nh));
-      h = fnv1a(h, m->hang_area, sizeof(double) * 4 * size_t(nh));
-    }
-    if (m->level) h = fnv1a(h, m->level, sizeof(int32_t) * size_t(n));
-    ctx->mesh_sig = h;
-  }
+  // the signature is formed when a restart or a caller first asks for it
+  ctx->mesh_sig_valid = false;
+  ctx->mesh_has_level = m->level != nullptr;
   ctx->bc_mask = 0;
   for (int64_t i = 0; i < 6 * n; ++i) {
     const int32_t code = m->nbr[i];
@@ -1329,10 +1319,43 @@ int fvgpu_checkpoint_read(const char *path, double *U, int neq, int64_t ncells, 
   return rc;
 }
 
+// FNV-1a over the resident tables, in the order and over the bytes the
+// upload received them (counts, neighbour codes and faces, areas, volumes,
+// 1:4 records, levels); formed once per mesh, on first use, from device copies.
+static int ensure_mesh_sig(fvgpu_ctx *ctx) {
+  if (ctx->mesh_sig_valid) return FVGPU_OK;
+  const int64_t n = ctx->n, nh = ctx->nhang;
+  cudaSetDevice(ctx->cfg.device);
+  FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint64_t h = kFnvSeed;
+  h = fnv1a(h, &n, sizeof(int64_t));
+  h = fnv1a(h, &nh, sizeof(int64_t));
+  std::vector<unsigned char> buf;
+  auto add = [&](const DevBuf &b, size_t bytes) -> cudaError_t {
+    buf.resize(bytes);
+    const cudaError_t e = cudaMemcpy(buf.data(), b.p, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) h = fnv1a(h, buf.data(), bytes);
+    return e;
+  };
+  FV_CUDA(ctx, add(ctx->nbr, sizeof(int32_t) * 6 * size_t(n)));
+  FV_CUDA(ctx, add(ctx->nbr_face, sizeof(int32_t) * 6 * size_t(n)));
+  FV_CUDA(ctx, add(ctx->area, sizeof(double) * 6 * size_t(n)));
+  FV_CUDA(ctx, add(ctx->vol, sizeof(double) * size_t(n)));
+  if (nh > 0) {
+    FV_CUDA(ctx, add(ctx->hang_nbr, sizeof(int32_t) * 4 * size_t(nh)));
+    FV_CUDA(ctx, add(ctx->hang_area, sizeof(double) * 4 * size_t(nh)));
+  }
+  if (ctx->mesh_has_level) FV_CUDA(ctx, add(ctx->level, sizeof(int32_t) * size_t(n)));
+  ctx->mesh_sig = h;
+  ctx->mesh_sig_valid = true;
+  return FVGPU_OK;
+}
+
 int fvgpu_mesh_signature(fvgpu_ctx *ctx, uint64_t *sig) {
   int rc = ensure_state(ctx);
   if (rc) return rc;
   if (!sig) return set_err(ctx, FVGPU_ERR_ARG, "null output");
+  if ((rc = ensure_mesh_sig(ctx))) return rc;
   *sig = ctx->mesh_sig;
   return FVGPU_OK;
 }
@@ -1343,6 +1366,7 @@ int fvgpu_checkpoint_save(fvgpu_ctx *ctx, const char *path, double time, int64_t
   std::vector<double> U(size_t(ctx->neq) * size_t(ctx->n));
   rc = fvgpu_download_state(ctx, U.data(), ctx->n);
   if (rc) return rc;
+  if ((rc = ensure_mesh_sig(ctx))) return rc;
   rc = fvgpu_checkpoint_write(path, U.data(), ctx->neq, ctx->n, ctx->mesh_sig, time, step);
   return rc ? set_err(ctx, rc, "cannot write restart file %s", path ? path : "(null)") : FVGPU_OK;
 }
@@ -1350,6 +1374,7 @@ int fvgpu_checkpoint_save(fvgpu_ctx *ctx, const char *path, double time, int64_t
 int fvgpu_checkpoint_load(fvgpu_ctx *ctx, const char *path, double *time, int64_t *step) {
   int rc = ensure_state(ctx);
   if (rc) return rc;
+  if ((rc = ensure_mesh_sig(ctx))) return rc;
   std::vector<double> U(size_t(ctx->neq) * size_t(ctx->n));
   rc = fvgpu_checkpoint_read(path, U.data(), ctx->neq, ctx->n, ctx->mesh_sig, time, step);
   if (rc) return set_err(ctx, rc, "restart file %s does not match this mesh or is damaged", path ? path : "(null)");

@@ -197,6 +197,16 @@ struct fvmesh {
     return table.find(pack_key(level, p[0], p[1], p[2]));
   }
 
+  // Face f of leaf L is a 1:4 face: its neighbour region at L's level is
+  // split (neither a leaf of that level nor of the one above covers it).
+  bool hanging_face(const Leaf &L, int f) const {
+    int64_t w[3], u[3];
+    if (!neighbour_pos(L, f, w, u)) return false;
+    if (find(L.level, w) >= 0) return false;
+    const int64_t q[3] = {floordiv2(w[0]), floordiv2(w[1]), floordiv2(w[2])};
+    return find(L.level - 1, q) < 0;
+  }
+
   // Neighbour position across face f at the cell's level.  Returns false at a
   // non-periodic domain side.  `unwrapped` keeps the image position.
   bool neighbour_pos(const Leaf &L, int f, int64_t wrapped[3], int64_t unwrapped[3]) const {
@@ -288,9 +298,13 @@ struct fvmesh {
   // Refine until every face sees at most one level of difference.
   int balance(std::vector<int32_t> *carry = nullptr) {
     for (int iter = 0; iter < 64; ++iter) {
+      // marking is idempotent (a leaf is marked or not, whoever marks it),
+      // so the leaves are checked in parallel; marks are relaxed atomic stores
       std::vector<uint8_t> mark(leaves.size(), 0);
       bool any = false;
-      for (size_t n = 0; n < leaves.size(); ++n) {
+#pragma omp parallel for schedule(dynamic, 1024) reduction(|| : any)
+      for (int64_t nn = 0; nn < int64_t(leaves.size()); ++nn) {
+        const size_t n = size_t(nn);
         const Leaf &L = leaves[n];
         for (int f = 0; f < 6; ++f) {
           int64_t w[3], u[3];
@@ -302,8 +316,8 @@ struct fvmesh {
               for (int l = L.level; l > cl; --l)
                 for (int a = 0; a < 3; ++a) q[a] = floordiv2(q[a]);
               const int32_t idx = find(cl, q);
-              if (idx >= 0 && !mark[idx]) {
-                mark[idx] = 1;
+              if (idx >= 0) {
+                __atomic_store_n(&mark[size_t(idx)], uint8_t(1), __ATOMIC_RELAXED);
                 any = true;
               }
             }
@@ -313,10 +327,8 @@ struct fvmesh {
           near_children(L.level, w, f, q);
           for (int s = 0; s < 4; ++s) {
             if (find(L.level + 1, q[s]) < 0) {  // deeper than one level
-              if (!mark[n]) {
-                mark[n] = 1;
-                any = true;
-              }
+              __atomic_store_n(&mark[n], uint8_t(1), __ATOMIC_RELAXED);
+              any = true;
               break;
             }
           }
@@ -348,12 +360,18 @@ struct fvmesh {
       const int want = std::min(std::max(int(split[i]), min_level), max_level);
       dir[i] = want > leaves[i].level ? 1 : (want < leaves[i].level ? -1 : 0);
     }
+    // merge groups: the checks read only the old leaves and dir, so each
+    // leaf is tested independently; groups are then numbered in leaf order
     std::vector<int32_t> group_of(n, -1);
+    std::vector<std::array<int32_t, 8>> kids_of(n);
+    std::vector<uint8_t> first_child(n, 0);
     groups.clear();
-    for (size_t i = 0; i < n; ++i) {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t ii = 0; ii < int64_t(n); ++ii) {
+      const size_t i = size_t(ii);
       const Leaf &L = leaves[i];
       if (dir[i] >= 0 || L.level <= min_level || (L.p[0] | L.p[1] | L.p[2]) & 1) continue;
-      std::array<int32_t, 8> kids;
+      std::array<int32_t, 8> &kids = kids_of[i];
       bool ok = true;
       for (int ch = 0; ch < 8 && ok; ++ch) {
         const int64_t q[3] = {L.p[0] + (ch & 1), L.p[1] + ((ch >> 1) & 1), L.p[2] + ((ch >> 2) & 1)};
@@ -377,9 +395,12 @@ struct fvmesh {
           ok = k >= 0 && dir[size_t(k)] <= 0;
         }
       }
-      if (!ok) continue;
-      for (int ch = 0; ch < 8; ++ch) group_of[size_t(kids[ch])] = int32_t(groups.size());
-      groups.push_back(kids);
+      if (ok) first_child[i] = 1;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      if (!first_child[i]) continue;
+      for (int ch = 0; ch < 8; ++ch) group_of[size_t(kids_of[i][ch])] = int32_t(groups.size());
+      groups.push_back(kids_of[i]);
     }
     std::vector<Leaf> next;
     std::vector<int32_t> carry;
@@ -470,15 +491,10 @@ int fvmesh_domain(const fvmesh *m, double lo[3], double len[3], int periodic[3],
 int fvmesh_sizes(const fvmesh *m, int64_t *ncells, int64_t *nhang) {
   if (!m) return fail(FVMESH_ERR_ARG, "null mesh");
   int64_t nh = 0;
-  for (const Leaf &L : m->leaves)
-    for (int f = 0; f < 6; ++f) {
-      int64_t w[3], u[3];
-      if (!m->neighbour_pos(L, f, w, u)) continue;
-      if (m->find(L.level, w) >= 0) continue;
-      int64_t q[3] = {floordiv2(w[0]), floordiv2(w[1]), floordiv2(w[2])};
-      if (m->find(L.level - 1, q) >= 0) continue;
-      ++nh;
-    }
+  const int64_t N = int64_t(m->leaves.size());
+#pragma omp parallel for schedule(static) reduction(+ : nh)
+  for (int64_t c = 0; c < N; ++c)
+    for (int f = 0; f < 6; ++f) nh += m->hanging_face(m->leaves[size_t(c)], f) ? 1 : 0;
   if (ncells) *ncells = int64_t(m->leaves.size());
   if (nhang) *nhang = nh;
   return 0;
@@ -551,16 +567,29 @@ int fvmesh_cell_nodes(const fvmesh *m, int level, int i, int j, int k, double xy
 int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
   if (!m || !t) return fail(FVMESH_ERR_ARG, "null argument");
   const int64_t N = int64_t(m->leaves.size());
-  int64_t nh = 0;
 
   // Frames per face index: outward normal, t1 along the face's first edge
   // and t2, as normalvector.c / tagvector.c form them (signed zeros included)
   if (t->frames) fv_box_frames(t->frames);
 
+  // 1:4 records are numbered in cell order: count each cell's, then number
+  // them by a prefix sum, so the cells can be filled independently
+  std::vector<int64_t> first(size_t(N) + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < N; ++c) {
+    int64_t k = 0;
+    for (int f = 0; f < 6; ++f) k += m->hanging_face(m->leaves[size_t(c)], f) ? 1 : 0;
+    first[size_t(c) + 1] = k;
+  }
+  for (int64_t c = 0; c < N; ++c) first[size_t(c) + 1] += first[size_t(c)];
+
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
   for (int64_t c = 0; c < N; ++c) {
     const Leaf &L = m->leaves[size_t(c)];
     const int l = L.level;
     const int64_t pos[3] = {L.p[0], L.p[1], L.p[2]};
+    int64_t nh = first[size_t(c)];
     if (t->level) t->level[c] = l;
     if (t->ijk)
       for (int a = 0; a < 3; ++a) t->ijk[a * N + c] = L.p[a];
@@ -611,7 +640,7 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
           int32_t kids[4];
           for (int s = 0; s < 4; ++s) {
             kids[s] = m->find(l + 1, q[s]);
-            if (kids[s] < 0) return fail(FVMESH_ERR_BALANCE, "face sees more than one level of refinement");
+            if (kids[s] < 0) bad = 1;  // a face sees more than one level of refinement
           }
           code = FVMESH_HANG0 - int32_t(nh);
           // areaproperties: each sub-face area is the fine neighbour's own
@@ -641,6 +670,7 @@ int fvmesh_flatten(const fvmesh *m, const fvmesh_tables *t) {
       if (t->dcc) t->dcc[fc] = dcc;
     }
   }
+  if (bad) return fail(FVMESH_ERR_BALANCE, "face sees more than one level of refinement");
   return 0;
 }
 
