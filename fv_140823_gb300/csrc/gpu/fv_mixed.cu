@@ -3,7 +3,8 @@
 // FP32-mixed path: fused kernels per RK stage.
 //
 // Arithmetic.  Reconstruction, equation of state and HLLC fluxes run in FP32
-// (the mixture EOS pressure inversion stays FP64).  The state is kept in FP64
+// (model 3, in fv_mixed_amr.cu, keeps its density words and the mixture EOS
+// inversion in float-float).  The state is kept in FP64
 // as the step-start state SN; a stage carries only the FP32 increment
 // D_k = S_k - SN, so the RK stage formulas of RK.c become
 //     RK(1): D1 = dt/V R(S0)                  (S1 = SN + dt/V R)

@@ -10,7 +10,8 @@
 // and sums a cell's residual face by face.
 //
 // Arithmetic.  Reconstruction, equation of state and HLLC fluxes run in FP32
-// (the mixture EOS pressure inversion stays FP64).  The state is kept in FP64
+// (model 3's paired density words, their reconstruction and the mixture EOS
+// pressure inversion in float-float, 48 bits).  The state is kept in FP64
 // as the step-start state SN; a stage carries only the FP32 increment
 // D_k = S_k - SN, so the RK stage formulas of RK.c become
 //     RK(1): D1 = dt/V R(S0)                  (S1 = SN + dt/V R)
@@ -319,7 +320,7 @@ __device__ __forceinline__ bool mixed_face_state(const MixedConst &mc, const flo
     s.y = 0.0f;
     return true;
   }
-  // model 3: pressure inversion in FP64 on the paired words
+  // model 3: pressure inversion in float-float on the paired words
   const bool ok = mixture_face_eos(mc, q, clip, s.r, s.y, s.p, s.c);
   const float rinv = fast_rcp(s.r);
   s.u = q[1] * rinv;
@@ -461,7 +462,7 @@ __device__ __forceinline__ bool local_state(const MixedConst &mc, int f, const f
     s.c = fast_sqrt(mc.gamma * (s.p + mc.pinf) * rinv);
     return true;
   }
-  // model 3: pressure inversion in FP64 on the paired words
+  // model 3: pressure inversion in float-float on the paired words
   const bool ok = mixture_face_eos(mc, q, clip, s.r, s.y, s.p, s.c);
   s.q4 = q[4];
   frame_in<F>(f, q, s.mn, s.mm, s.ml);
@@ -1945,7 +1946,7 @@ int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *
   std::vector<char> is_block4(size_t(n), 0), is_brick4(size_t(n), 0);
   // bricks for model 1, inviscid or viscous (both kernels read the cells'
   // gradients straight from the gradient pass); model 3 (paired state words,
-  // FP64 reconstruction of the partial densities) runs the general kernel
+  // float-float reconstruction of the partial densities) runs the general kernel
   if (!r.force_general && ph.model == 1) {
     find_blocks<Brick8>(m, is_block8);
     for (int64_t i = 0; i < n; ++i)
