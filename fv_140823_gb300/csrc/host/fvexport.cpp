@@ -110,7 +110,8 @@ int fvmesh_export_tecplot(const fvmesh_tecplot *cfg, int64_t n, const int32_t *l
     return export_fail(FVMESH_ERR_ARG, "null argument");
   if (cfg->model < 1 || cfg->model > 3 || cfg->neq != (cfg->model == 2 ? 4 : 5))
     return export_fail(FVMESH_ERR_ARG, "model must be 1 (neq 5), 2 (neq 4) or 3 (neq 5)");
-  if (n < 1 || n > (int64_t(1) << 28)) return export_fail(FVMESH_ERR_ARG, "leaf count out of range");
+  // links are numbered in int32 (at most 8 per leaf), as the file's %d fields are
+  if (n < 1 || n > (int64_t(1) << 27)) return export_fail(FVMESH_ERR_ARG, "leaf count out of range");
   const int neq = cfg->neq;
   const int rl = cfg->root_level;
   for (int64_t c = 0; c < n; ++c)
