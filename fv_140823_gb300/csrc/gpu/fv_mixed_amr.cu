@@ -956,10 +956,10 @@ struct Block {
 };
 
 // register budgets: model 1 four blocks per SM (64 registers, as shared
-// memory allows), model 3 two (the float-float reconstruction of the paired
-// words and the pressure inversion take about 100 registers)
+// memory allows), model 3 three (80 registers without spills; its 64 KB of
+// shared memory fits three blocks)
 template <int MODEL, bool MUSCL>
-__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 2 : 4)
+__global__ void __launch_bounds__(kBlock, MODEL == 3 ? 3 : 4)
     k_mixed_general(MixedConst mc, StageArgs a, const __grid_constant__ GeoTables geo_tab) {
   constexpr int NV = kNv<MODEL>;
   __shared__ float st[NV][kBlock];
