@@ -24,7 +24,8 @@ thread_local std::string g_create_error;
 
 struct DevBuf {
   void *p = nullptr;
-  size_t bytes = 0;
+  size_t bytes = 0;  // the size asked for last
+  size_t cap = 0;    // the size allocated (kept across meshes, reused when large enough)
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
@@ -32,13 +33,17 @@ struct DevBuf {
   void release() {
     if (p) cudaFree(p);
     p = nullptr;
-    bytes = 0;
+    bytes = cap = 0;
   }
   cudaError_t alloc(size_t b) {
-    release();
     if (b == 0) b = 16;
+    if (p && b <= cap) {
+      bytes = b;
+      return cudaSuccess;
+    }
+    release();
     cudaError_t e = cudaMalloc(&p, b);
-    if (e == cudaSuccess) bytes = b;
+    if (e == cudaSuccess) bytes = cap = b;
     else p = nullptr;
     return e;
   }
@@ -818,7 +823,7 @@ int fvgpu_upload_mesh(fvgpu_ctx *ctx, const fvgpu_mesh_soa *m) {
   cudaSetDevice(ctx->cfg.device);
   FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->drop_graphs();
-  fv::release_mixed(ctx->mixed);
+  fv::reset_mixed(ctx->mixed);
   ctx->has_mesh = false;
   const int64_t n = m->ncells, nh = m->nhang;
   const int neq = ctx->neq;
@@ -913,7 +918,7 @@ int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *lv) {
   cudaSetDevice(ctx->cfg.device);
   FV_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->drop_graphs();
-  fv::release_mixed(ctx->mixed);
+  fv::reset_mixed(ctx->mixed);
   ctx->has_mesh = false;
   // pass 1: keys, 1:4 counts, record numbers
   DevBuf d_level, d_ijk, d_keys, d_off, d_tiles, d_scal;

@@ -1415,11 +1415,20 @@ enum {
 };
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
+  const size_t want = bytes ? bytes : 16;
+  if (r.buf[slot] && want <= r.cap[slot]) {  // an earlier mesh's buffer is large enough
+    r.bytes[slot] = bytes;
+    return cudaSuccess;
+  }
   if (r.buf[slot]) cudaFree(r.buf[slot]);
   r.buf[slot] = nullptr;
   r.bytes[slot] = 0;
-  cudaError_t e = cudaMalloc(&r.buf[slot], bytes ? bytes : 16);
-  if (e == cudaSuccess) r.bytes[slot] = bytes;
+  r.cap[slot] = 0;
+  cudaError_t e = cudaMalloc(&r.buf[slot], want);
+  if (e == cudaSuccess) {
+    r.bytes[slot] = bytes;
+    r.cap[slot] = want;
+  }
   return e;
 }
 
@@ -1758,10 +1767,18 @@ void release_mixed(MixedResources &r) {
     if (r.buf[i]) cudaFree(r.buf[i]);
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
+    r.cap[i] = 0;
   }
   r.ready = false;
   r.snf_valid = false;
   r.nbricks = r.nbricks4 = r.ngeneral = 0;
+}
+
+void reset_mixed(MixedResources &r) {
+  r.ready = false;
+  r.snf_valid = false;
+  r.nbricks = r.nbricks4 = r.ngeneral = 0;
+  r.n = 0;
 }
 
 double *mixed_alt_state(MixedResources &r) { return static_cast<double *>(r.buf[kBufAlt]); }

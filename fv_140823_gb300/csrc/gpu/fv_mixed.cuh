@@ -19,6 +19,7 @@ namespace fv {
 struct MixedResources {
   void *buf[11] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t bytes[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  size_t cap[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // allocated bytes (kept across meshes)
   int64_t n = 0;
   int model = 1;           // EOS model the FP32 state layout follows (model 3: density offset)
   int64_t nbricks = 0;     // 8x8x4 brick blocks (structured fast path)
@@ -47,6 +48,9 @@ bool mixed_supported(const Phys &ph, char *why, size_t whylen);
 // with the reason in `why`.
 int mixed_prepare_host(MixedResources &r, const Phys &ph, const fvgpu_mesh_soa *m, char *why, size_t whylen);
 void release_mixed(MixedResources &r);
+// Forget the prepared mesh but keep the device buffers, streams and events
+// for the next one (buffers are reused when large enough).
+void reset_mixed(MixedResources &r);
 // the second FP64 state buffer (steps write into it; the caller swaps)
 double *mixed_alt_state(MixedResources &r);
 // exchange the caller's state buffer with the second buffer after a step

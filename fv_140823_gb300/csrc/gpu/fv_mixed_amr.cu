@@ -1711,11 +1711,20 @@ enum {
 };
 
 cudaError_t alloc_slot(MixedResources &r, int slot, size_t bytes) {
+  const size_t want = bytes ? bytes : 16;
+  if (r.buf[slot] && want <= r.cap[slot]) {  // an earlier mesh's buffer is large enough
+    r.bytes[slot] = bytes;
+    return cudaSuccess;
+  }
   if (r.buf[slot]) cudaFree(r.buf[slot]);
   r.buf[slot] = nullptr;
   r.bytes[slot] = 0;
-  cudaError_t e = cudaMalloc(&r.buf[slot], bytes ? bytes : 16);
-  if (e == cudaSuccess) r.bytes[slot] = bytes;
+  r.cap[slot] = 0;
+  cudaError_t e = cudaMalloc(&r.buf[slot], want);
+  if (e == cudaSuccess) {
+    r.bytes[slot] = bytes;
+    r.cap[slot] = want;
+  }
   return e;
 }
 
@@ -2046,6 +2055,7 @@ void release_mixed(MixedResources &r) {
     if (r.buf[i]) cudaFree(r.buf[i]);
     r.buf[i] = nullptr;
     r.bytes[i] = 0;
+    r.cap[i] = 0;
   }
   for (int k = 0; k < 2; ++k) {
     if (r.side[k]) cudaStreamDestroy(r.side[k]);
