@@ -199,6 +199,22 @@ def test_mixed_viscous_taylor_green_within_1e6(eos):
         assert np.max(rel_l2(s.state(), b)[[1, 2]]) > 1e-4
 
 
+def test_uniform_two_pi_box_on_the_brick_kernel():
+    """The 2*pi Taylor-Green box, uniform: its face areas follow the node
+    coordinates and vary in the last bits from cell to cell (as the
+    reference's areaproperties gives them); the slope-sharing brick kernel
+    takes one FP32 area per level and axis and stays within 1e-6 of FP64."""
+    c = cases.tgv(base_level=5, extra_levels=0)
+    t = c.tables
+    assert bricks_throughout(t)
+    assert len(np.unique(t.area)) > 1  # the areas do vary
+    dt = fixed_dt(c)
+    a = run(c, abi.MIXED, 10, dt)
+    b = run(c, abi.FP64, 10, dt)
+    err = rel_l2_mom(a, b)
+    assert np.all(err <= 1e-6), err
+
+
 def _mixed_state(case, flags, nsteps, dt):
     cfg = SolverConfig(**{**case.cfg.__dict__, "precision": abi.MIXED, "flags": flags})
     with solver(case.tables, cfg) as s:
