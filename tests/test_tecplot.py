@@ -80,6 +80,33 @@ def test_writer_matches_reference_writer_on_amr(periodic, tmp_path):
         assert a.read() == b.read()
 
 
+@pytest.mark.skipif(not _ref_available(), reason="the reference's objects (oracle/_ref) are not built here")
+def test_writer_matches_reference_writer_model2(tmp_path):
+    """The barotropic liquid (model 2, four variables, barotropic_eos.c:3-30
+    for the pressure column) on an AMR mesh, against the reference writer."""
+    rng = np.random.default_rng(11)
+    m = uniform_mesh(2)
+    refine_by(m, lambda l, c: ((c - 0.5) ** 2).sum(0) < 0.04, 4)
+    t = m.flatten()
+    n = t.ncells
+    U = np.vstack([997.0 + 3.0 * rng.random(n), 0.1 * rng.standard_normal((3, n))])
+    from fv_140823_gb300.abi import SolverConfig
+
+    cfg = SolverConfig(model=2, ischeme=1)
+    ref = RefHarness(t, PhysConfig(model=2, ns=0, ischeme=1, iprimtv=0, eos=0, i_case=0, gamma=1.4, pinf=0.0,
+                                   visc=0.0, ymin=0.0, dt=1e-3))
+    try:
+        ref.set_state(U)
+        (tmp_path / "ref").mkdir()
+        p_ref = ref.export(2, 5, str(tmp_path / "ref"))
+    finally:
+        ref.close()
+    p_our = tecplot.write_field_linked(str(tmp_path / tecplot.file_name(5)), t, U, Oracle(t, cfg).gradcalc(U),
+                                       model=2, gamma=1.4, pinf=0.0, root_level=2)
+    with open(p_ref, "rb") as a, open(p_our, "rb") as b:
+        assert a.read() == b.read()
+
+
 def test_links_are_shared_corners(tmp_path):
     """Uniform 4^3 non-periodic: 5^3 links, each leaf's 8 link numbers are its
     corners on the 5^3 lattice, one-based, in Tecplot brick order."""
