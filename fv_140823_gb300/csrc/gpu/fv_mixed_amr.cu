@@ -955,6 +955,98 @@ struct Block {
   }
 };
 
+// The flux(es) through one face of a cell of a general block, added to the
+// cell's residual R (a 1:4 face: its four sub-faces in order).  P_ >= 0: a
+// + face known at compile time; P_ < 0: face f_rt, a + face when plus_rt.
+// A + face's flux is always computed, in the frame of that face, and
+// published for the upper cell when the face has a single neighbour; a -
+// face reads the published flux when the lower cell is in the block and its
+// + face carries this cell alone, and otherwise recomputes the canonical
+// flux (lower side first, frame of the lower cell's + face; a
+// domain-boundary face in its own frame).
+template <int MODEL, bool MUSCL>
+struct FaceCtx {
+  static constexpr int NV = kNv<MODEL>;
+  const Block<MODEL> &blk;
+  const MixedConst &mc;
+  const StageArgs &a;
+  const GeoTables *geo;
+  int32_t g;
+  int lev, t, c;
+  float (*sf)[NV][kBlock];
+  float (*fp)[kNeqMax][kBlock];
+
+  template <int P_>
+  __device__ __forceinline__ void face(int f_rt, bool plus_rt, int32_t code, float R[kNeqMax], bool &ok) const {
+    const bool plus = P_ >= 0 || plus_rt;
+    const int f = P_ >= 0 ? P_ : f_rt;
+    const int fo = opp_face(f);
+    const int c0 = blk.c0;
+    const bool boundary = is_boundary(code);
+    const bool hanging = is_hanging(code);
+    const int rel = rel_of(g, f);
+    const int nsub = hanging ? 4 : 1;
+    const int32_t *hk = hanging ? a.hang_nbr + 4 * hang_index(code) : nullptr;
+    const float A = hanging ? geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
+#pragma unroll 1
+    for (int s = 0; s < nsub; ++s) {
+      const int other = boundary ? -1 : (hanging ? __ldg(hk + s) : code);
+      float Fn[kNeqMax];
+      const bool published = !plus && !boundary && (hanging || rel == kRelSame) && blk.in_block(other);
+      if (published) {
+        const int tl = other - c0;
+#pragma unroll
+        for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
+      } else {
+        float own[kNvMax], oth[kNvMax];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          own[v] = sf[f][v][t];
+          oth[v] = own[v];
+        }
+        if (!boundary) {
+          if (blk.in_block(other)) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) oth[v] = sf[fo][v][other - c0];
+          } else if (MUSCL) {
+            blk.recon_any(other, fo, oth);
+          } else {
+            blk.state(other, oth);
+          }
+        }
+        const bool own_low = plus || boundary;
+        float lo[kNvMax], hi[kNvMax];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          lo[v] = own_low ? own[v] : oth[v];
+          hi[v] = own_low ? oth[v] : own[v];
+        }
+        const int bc = boundary ? -1 - code : 0;
+        if constexpr (P_ >= 0)
+          ok &= canonical_flux<MODEL, P_>(mc, P_, bc, MUSCL, lo, hi, Fn);
+        else
+          ok &= canonical_flux<MODEL>(mc, own_low ? f : fo, bc, MUSCL, lo, hi, Fn);
+        if (mc.ns == 1) {  // (F - FV).n + FH
+          float gl[9], gh[9], FVn[kNeqMax];
+          const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
+          load_grad9f(a.SG, a.n, clo, gl);
+          load_grad9f(a.SG, a.n, chi, gh);
+          viscous_normal<MODEL>(mc, own_low ? f : fo, bc, lo, hi, gl, gh, FVn);
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
+        }
+        if (plus && !boundary && !hanging) {
+#pragma unroll
+          for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
+        }
+      }
+      const float sA = (plus || boundary) ? -A : A;
+#pragma unroll
+      for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];  // separate roundings: equal and opposite face fluxes cancel exactly
+    }
+  }
+};
+
 // register budgets: model 1 four blocks per SM (64 registers, as shared
 // memory allows), model 3 three (80 registers without spills; its 64 KB of
 // shared memory fits three blocks)
@@ -1034,78 +1126,38 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 3 : 4)
   }
   __syncthreads();
 
-  // C: fluxes, + faces (publish), barrier, - faces
+  // C: fluxes, + faces (publish), barrier, - faces.  Model 1 lays its +
+  // faces out one by one with the face known at compile time (frames as
+  // register choices, fixed shared-memory slots; measured faster on the
+  // viscous Taylor-Green mesh) and shares one loop among the - faces, mostly
+  // read from the published + fluxes; model 3, whose float-float flux code
+  // is larger, runs all six faces through one loop (measured faster on the
+  // bubble).
   float R[kNeqMax] = {0.f, 0.f, 0.f, 0.f, 0.f};
   bool ok = true;
   const int lev = level_of(g);
+  const FaceCtx<MODEL, MUSCL> fc{blk, mc, a, geo, g, lev, t, c, sf, fp};
+  if constexpr (MODEL == 1) {
+    if (active) {
+      fc.template face<1>(1, true, nb[1], R, ok);
+      fc.template face<2>(2, true, nb[2], R, ok);
+      fc.template face<5>(5, true, nb[5], R, ok);
+    }
+    __syncthreads();
+    if (active) {
 #pragma unroll 1
-  for (int it = 0; it < 6; ++it) {
-    if (it == 3) __syncthreads();
-    if (!active) continue;
-    const int f = face_of_iter(it);
-    const bool plus = it < 3;
-    const int fo = opp_face(f);
-    const int32_t code = nb[f];
-    const bool boundary = is_boundary(code);
-    const bool hanging = is_hanging(code);
-    const int rel = rel_of(g, f);
-    const int nsub = hanging ? 4 : 1;
-    const int32_t *hk = hanging ? a.hang_nbr + 4 * hang_index(code) : nullptr;
-    const float A = hanging ? geo->sub_area[lev * 6 + f] : geo_face(geo, lev, f, rel)[2];
-#pragma unroll 1
-    for (int s = 0; s < nsub; ++s) {
-      const int other = boundary ? -1 : (hanging ? __ldg(hk + s) : code);
-      float Fn[kNeqMax];
-      // the - side reads a published flux when the lower cell is in the block
-      // and its + face carries a single neighbour (this cell)
-      const bool published = !plus && !boundary && (hanging || rel == kRelSame) && blk.in_block(other);
-      if (published) {
-        const int tl = other - c0;
-#pragma unroll
-        for (int v = 0; v < kNeqMax; ++v) Fn[v] = fp[plus_slot(fo)][v][tl];
-      } else {
-        float own[kNvMax], oth[kNvMax];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          own[v] = sf[f][v][t];
-          oth[v] = own[v];
-        }
-        if (!boundary) {
-          if (blk.in_block(other)) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) oth[v] = sf[fo][v][other - c0];
-          } else if (muscl) {
-            blk.recon_any(other, fo, oth);
-          } else {
-            blk.state(other, oth);
-          }
-        }
-        // canonical orientation: lower side first, frame of the lower cell's + face
-        const bool own_low = plus || boundary;
-        float lo[kNvMax], hi[kNvMax];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          lo[v] = own_low ? own[v] : oth[v];
-          hi[v] = own_low ? oth[v] : own[v];
-        }
-        ok &= canonical_flux<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, muscl, lo, hi, Fn);
-        if (mc.ns == 1) {  // (F - FV).n + FH
-          float gl[9], gh[9], FVn[kNeqMax];
-          const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
-          load_grad9f(a.SG, n, clo, gl);
-          load_grad9f(a.SG, n, chi, gh);
-          viscous_normal<MODEL>(mc, own_low ? f : fo, boundary ? -1 - code : 0, lo, hi, gl, gh, FVn);
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) Fn[v] -= FVn[v];
-        }
-        if (plus && !boundary && !hanging) {
-#pragma unroll
-          for (int v = 0; v < kNeqMax; ++v) fp[plus_slot(f)][v][t] = Fn[v];
-        }
+      for (int it = 3; it < 6; ++it) {
+        const int f = face_of_iter(it);
+        fc.template face<-1>(f, false, f == 3 ? nb[3] : (f == 0 ? nb[0] : nb[4]), R, ok);
       }
-      const float sA = (plus || boundary) ? -A : A;
-#pragma unroll
-      for (int v = 0; v < kNeqMax; ++v) R[v] = R[v] + sA * Fn[v];  // separate roundings: equal and opposite face fluxes cancel exactly
+    }
+  } else {
+#pragma unroll 1
+    for (int it = 0; it < 6; ++it) {
+      if (it == 3) __syncthreads();
+      if (!active) continue;
+      const int f = face_of_iter(it);
+      fc.template face<-1>(f, it < 3, nb[f], R, ok);
     }
   }
 
