@@ -38,6 +38,7 @@ def load_mesh_lib() -> C.CDLL:
         lib.fvmesh_destroy.restype = None
         lib.fvmesh_sizes.argtypes = [vp, i64p, i64p]
         lib.fvmesh_leaves.argtypes = [vp, vp, vp]
+        lib.fvmesh_leaf_cells.argtypes = [vp, vp, vp]
         lib.fvmesh_refine.argtypes = [vp, vp, C.c_int]
         lib.fvmesh_adapt.argtypes = [vp, vp, C.c_int, C.c_int]
         lib.fvmesh_transfer.argtypes = [vp, C.c_int, C.c_int64, vp, vp]

@@ -12,8 +12,9 @@ again and re-uploads the tables once.  One adaptation here is:
    (criterionsmth.c), siblings merge (refineh_1.c), 2:1 face balance;
 3. ``OctreeMesh.transfer``: children inherit the parent's state (split.c:493),
    a merged parent takes the mean of its children (merge.c:93-101);
-4. ``fvgpu_upload_mesh`` of the new tables and ``fvgpu_upload_state`` of the
-   transferred state.
+4. the new tables (``OctreeMesh.flatten`` and ``fvgpu_upload_mesh``, or the
+   leaf list flattened on the device by ``fvgpu_upload_leaves``) and
+   ``fvgpu_upload_state`` of the transferred state.
 
 :func:`run_adaptive` is the loop with the stepping, criterion and reload
 supplied by the caller; :func:`run_adaptive_gpu` binds it to a
@@ -45,14 +46,15 @@ class AdaptiveRun:
     cells: list = field(default_factory=list)  # leaf count after each adaptation
 
 
-def run_adaptive(mesh: OctreeMesh, U: np.ndarray, nsteps: int, ac: AdaptConfig, step, criterion, reload):
+def run_adaptive(mesh: OctreeMesh, U: np.ndarray, nsteps: int, ac: AdaptConfig, step, criterion, reload,
+                 flatten=True):
     """Advance `nsteps` steps, adapting the mesh after every `ac.every` steps
     (not after the last one).
 
     step(k) advances the current state k steps; criterion() returns
     (state, target levels) of the current mesh; reload(tables, state) puts
-    the adapted mesh and the transferred state in place and returns the
-    state-reading callable for the end of the run."""
+    the adapted mesh and the transferred state in place (with flatten=False
+    reload receives the mesh itself instead of its flattened tables)."""
     done = 0
     cells = []
     final = None
@@ -65,7 +67,7 @@ def run_adaptive(mesh: OctreeMesh, U: np.ndarray, nsteps: int, ac: AdaptConfig, 
         S, split = criterion()
         mesh.adapt(split, ac.min_level, ac.max_level)
         S_new = mesh.transfer(S)
-        reload(mesh.flatten(), S_new)
+        reload(mesh.flatten() if flatten else mesh, S_new)
         cells.append(mesh.ncells)
     return AdaptiveRun(state=final() if callable(final) else final, steps=done, cells=cells)
 
@@ -74,7 +76,9 @@ def run_adaptive_gpu(solver, mesh: OctreeMesh, U: np.ndarray, nsteps: int, ac: A
                      scheme: str = "ssprk3", cfl: float = 0.5) -> AdaptiveRun:
     """The loop on a :class:`Solver` whose tables are ``mesh.flatten()``:
     CFL steps of `scheme`, the criterion on the device (the FP64 Green-Gauss
-    gradients of the current state), adaptation on the host."""
+    gradients of the current state), adaptation on the host, and the adapted
+    leaf list flattened on the device (``fvgpu_upload_leaves``, the same
+    tables as the host flattener's)."""
     solver.set_state(U)
 
     def step(k):
@@ -86,8 +90,9 @@ def run_adaptive_gpu(solver, mesh: OctreeMesh, U: np.ndarray, nsteps: int, ac: A
         solver.gradcalc()
         return S, solver.criterion(ac.kind, ac.threshold, ac.max_level)
 
-    def reload(tables, S):
-        solver.upload_mesh(tables)
+    def reload(m, S):
+        level, ijk = m.leaf_cells()
+        solver.upload_leaves(level, ijk, m.lo, m.length, m.periodic, m.side_bc)
         solver.set_state(S)
 
-    return run_adaptive(mesh, U, nsteps, ac, step, criterion, reload)
+    return run_adaptive(mesh, U, nsteps, ac, step, criterion, reload, flatten=False)

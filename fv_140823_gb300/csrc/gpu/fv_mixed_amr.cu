@@ -1157,7 +1157,10 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 3 : 4)
       if (it == 3) __syncthreads();
       if (!active) continue;
       const int f = face_of_iter(it);
-      fc.template face<-1>(f, it < 3, nb[f], R, ok);
+      // the neighbour code by selects: indexing nb by the loop's face would
+      // put the array in local memory
+      const int32_t code = f == 1 ? nb[1] : f == 2 ? nb[2] : f == 5 ? nb[5] : f == 3 ? nb[3] : f == 0 ? nb[0] : nb[4];
+      fc.template face<-1>(f, it < 3, code, R, ok);
     }
   }
 

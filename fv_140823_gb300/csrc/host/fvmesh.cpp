@@ -516,6 +516,18 @@ int fvmesh_leaves(const fvmesh *m, int32_t *level, double *centroid) {
   return 0;
 }
 
+int fvmesh_leaf_cells(const fvmesh *m, int32_t *level, int32_t *ijk) {
+  if (!m || !level || !ijk) return fail(FVMESH_ERR_ARG, "null argument");
+  const int64_t n = int64_t(m->leaves.size());
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < n; ++c) {
+    const Leaf &L = m->leaves[size_t(c)];
+    level[c] = L.level;
+    for (int a = 0; a < 3; ++a) ijk[a * n + c] = int32_t(L.p[a]);
+  }
+  return 0;
+}
+
 int fvmesh_refine(fvmesh *m, const uint8_t *flags, int max_level) {
   if (!m || !flags) return fail(FVMESH_ERR_ARG, "null argument");
   if (max_level > FVMESH_MAX_LEVEL) return fail(FVMESH_ERR_LEVEL, "max_level too large");

@@ -108,6 +108,15 @@ class OctreeMesh:
         self._check(self._lib.fvmesh_leaves(self._h, C.c_void_p(_p(level)), C.c_void_p(_p(cen))))
         return level, cen
 
+    def leaf_cells(self) -> tuple[np.ndarray, np.ndarray]:
+        """Leaf levels (n,) and lattice positions (3, n), Morton order: the
+        leaf list :meth:`Solver.upload_leaves` flattens on the device."""
+        n, _ = self.sizes()
+        level = np.empty(n, np.int32)
+        ijk = np.empty((3, n), np.int32)
+        self._check(self._lib.fvmesh_leaf_cells(self._h, C.c_void_p(_p(level)), C.c_void_p(_p(ijk))))
+        return level, ijk
+
     def refine(self, flags, max_level: int) -> None:
         f = np.ascontiguousarray(np.asarray(flags, dtype=np.uint8))
         if f.shape != (self.ncells,):

@@ -84,6 +84,11 @@ int fvmesh_sizes(const fvmesh *m, int64_t *ncells, int64_t *nhang);
 /* Leaf levels and centroids (centroids as distance.c forms them: node average). */
 int fvmesh_leaves(const fvmesh *m, int32_t *level, double *centroid /*[3][n]*/);
 
+/* Leaf levels and lattice positions (ijk[a * n + c]: the leaf's index along
+ * axis a at its own level), in Morton order: the leaf list fvgpu_upload_leaves
+ * takes, without flattening on the host. */
+int fvmesh_leaf_cells(const fvmesh *m, int32_t *level, int32_t *ijk /*[3][n]*/);
+
 /* Refine every leaf whose flag is nonzero (up to max_level), then refine more
  * leaves until every face sees at most one level of difference.  Leaves are
  * re-sorted along the Morton curve. */

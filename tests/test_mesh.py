@@ -95,6 +95,13 @@ def test_morton_order_and_levels():
     assert np.all(np.diff(key) > 0)
 
 
+def test_leaf_cells_equal_the_flattened_leaf_list():
+    m = amr()
+    level, ijk = m.leaf_cells()
+    t = m.flatten()
+    assert np.array_equal(level, t.level) and np.array_equal(ijk, t.ijk)
+
+
 def test_uniform_distances_follow_distance_c():
     # distance.c, same level: dist_cc = |dx| / 2, dist_cf = |dx| / 4
     t = uniform_mesh(4, periodic=(1, 1, 1)).flatten()
