@@ -83,6 +83,11 @@ struct fvgpu_ctx {
   int64_t n = 0, nhang = 0;
   bool has_mesh = false;
   DevBuf nbr, nbr_face, area, dcf, dcc, vol, hang_nbr, hang_area, level, inner;
+  // device flattening (fvgpu_upload_leaves): work arrays and the host copies
+  // of the tables, kept across meshes and reused when large enough
+  DevBuf lv_level, lv_ijk, lv_keys, lv_off, lv_tiles, lv_scal;
+  std::vector<int32_t> lv_h32;
+  std::vector<double> lv_h64;
   // state and work arrays
   DevBuf S, SN, R, SF, SG;
   DevBuf scal;      // Scalars
@@ -921,7 +926,8 @@ int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *lv) {
   fv::reset_mixed(ctx->mixed);
   ctx->has_mesh = false;
   // pass 1: keys, 1:4 counts, record numbers
-  DevBuf d_level, d_ijk, d_keys, d_off, d_tiles, d_scal;
+  DevBuf &d_level = ctx->lv_level, &d_ijk = ctx->lv_ijk, &d_keys = ctx->lv_keys, &d_off = ctx->lv_off,
+         &d_tiles = ctx->lv_tiles, &d_scal = ctx->lv_scal;
   const int64_t ntiles = (n + 1023) / 1024;
   FV_CUDA(ctx, d_level.alloc(sizeof(int32_t) * size_t(n)));
   FV_CUDA(ctx, d_ijk.alloc(sizeof(int32_t) * 3 * size_t(n)));
@@ -966,32 +972,37 @@ int fvgpu_upload_leaves(fvgpu_ctx *ctx, const fvgpu_leaves *lv) {
   if (hs[1]) return leaf_error(uint64_t(hs[1]));
   // host copies for the signature, the boundary codes and the mixed path's brick detection
   const size_t un = static_cast<size_t>(n), unh = static_cast<size_t>(nh);
-  std::vector<int32_t> h_nbr(6 * un), h_nface(6 * un), h_hnbr(4 * unh), h_level(un);
-  std::vector<double> h_area(6 * un), h_dcf(6 * un), h_dcc(6 * un), h_vol(un), h_harea(4 * unh);
+  const size_t n32 = 13 * un + 4 * unh, n64 = 19 * un + 4 * unh;  // int32: nbr, nbr_face, level, hang_nbr
+  if (ctx->lv_h32.size() < n32) ctx->lv_h32.resize(n32);
+  if (ctx->lv_h64.size() < n64) ctx->lv_h64.resize(n64);
+  int32_t *h_nbr = ctx->lv_h32.data(), *h_nface = h_nbr + 6 * un, *h_level = h_nface + 6 * un,
+          *h_hnbr = h_level + un;
+  double *h_area = ctx->lv_h64.data(), *h_dcf = h_area + 6 * un, *h_dcc = h_dcf + 6 * un, *h_vol = h_dcc + 6 * un,
+         *h_harea = h_vol + un;
   struct Down {
     void *dst;
     const DevBuf *src;
     size_t bytes;
-  } downs[] = {{h_nbr.data(), &ctx->nbr, h_nbr.size() * 4},         {h_nface.data(), &ctx->nbr_face, h_nface.size() * 4},
-               {h_area.data(), &ctx->area, h_area.size() * 8},      {h_dcf.data(), &ctx->dcf, h_dcf.size() * 8},
-               {h_dcc.data(), &ctx->dcc, h_dcc.size() * 8},         {h_vol.data(), &ctx->vol, h_vol.size() * 8},
-               {h_hnbr.data(), &ctx->hang_nbr, h_hnbr.size() * 4}, {h_harea.data(), &ctx->hang_area, h_harea.size() * 8},
-               {h_level.data(), &ctx->level, h_level.size() * 4}};
+  } downs[] = {{h_nbr, &ctx->nbr, 6 * un * 4},        {h_nface, &ctx->nbr_face, 6 * un * 4},
+               {h_area, &ctx->area, 6 * un * 8},      {h_dcf, &ctx->dcf, 6 * un * 8},
+               {h_dcc, &ctx->dcc, 6 * un * 8},        {h_vol, &ctx->vol, un * 8},
+               {h_hnbr, &ctx->hang_nbr, 4 * unh * 4}, {h_harea, &ctx->hang_area, 4 * unh * 8},
+               {h_level, &ctx->level, un * 4}};
   for (auto &d : downs)
     if (d.bytes) FV_CUDA(ctx, cudaMemcpy(d.dst, d.src->p, d.bytes, cudaMemcpyDeviceToHost));
   fvgpu_mesh_soa m{};
   m.ncells = n;
   m.nhang = nh;
-  m.nbr = h_nbr.data();
-  m.nbr_face = h_nface.data();
-  m.area = h_area.data();
-  m.dcf = h_dcf.data();
-  m.dcc = h_dcc.data();
-  m.vol = h_vol.data();
-  m.hang_nbr = h_hnbr.data();
-  m.hang_area = h_harea.data();
+  m.nbr = h_nbr;
+  m.nbr_face = h_nface;
+  m.area = h_area;
+  m.dcf = h_dcf;
+  m.dcc = h_dcc;
+  m.vol = h_vol;
+  m.hang_nbr = h_hnbr;
+  m.hang_area = h_harea;
   m.frames = kBoxFrames.v;
-  m.level = h_level.data();
+  m.level = h_level;
   return finish_mesh(ctx, &m);
 }
 
