@@ -977,7 +977,8 @@ struct FaceCtx {
   float (*fp)[kNeqMax][kBlock];
 
   template <int P_>
-  __device__ __forceinline__ void face(int f_rt, bool plus_rt, int32_t code, float R[kNeqMax], bool &ok) const {
+  __device__ __forceinline__ void face(int f_rt, bool plus_rt, int32_t code, float R[kNeqMax], bool &ok,
+                                       const float *gown = nullptr) const {
     const bool plus = P_ >= 0 || plus_rt;
     const int f = P_ >= 0 ? P_ : f_rt;
     const int fo = opp_face(f);
@@ -1029,7 +1030,12 @@ struct FaceCtx {
         if (mc.ns == 1) {  // (F - FV).n + FH
           float gl[9], gh[9], FVn[kNeqMax];
           const int clo = own_low ? c : other, chi = own_low ? (boundary ? c : other) : c;
-          load_grad9f(a.SG, a.n, clo, gl);
+          if (P_ >= 0 && gown) {  // a + face: the lower cell is this one, its gradients at hand
+#pragma unroll
+            for (int i = 0; i < 9; ++i) gl[i] = gown[i];
+          } else {
+            load_grad9f(a.SG, a.n, clo, gl);
+          }
           load_grad9f(a.SG, a.n, chi, gh);
           viscous_normal<MODEL>(mc, own_low ? f : fo, bc, lo, hi, gl, gh, FVn);
 #pragma unroll
@@ -1139,9 +1145,11 @@ __global__ void __launch_bounds__(kBlock, MODEL == 3 ? 3 : 4)
   const FaceCtx<MODEL, MUSCL> fc{blk, mc, a, geo, g, lev, t, c, sf, fp};
   if constexpr (MODEL == 1) {
     if (active) {
-      fc.template face<1>(1, true, nb[1], R, ok);
-      fc.template face<2>(2, true, nb[2], R, ok);
-      fc.template face<5>(5, true, nb[5], R, ok);
+      float gown[9];
+      if (mc.ns == 1) load_grad9f(a.SG, n, c, gown);
+      fc.template face<1>(1, true, nb[1], R, ok, gown);
+      fc.template face<2>(2, true, nb[2], R, ok, gown);
+      fc.template face<5>(5, true, nb[5], R, ok, gown);
     }
     __syncthreads();
     if (active) {
